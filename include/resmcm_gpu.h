@@ -1,0 +1,207 @@
+/*
+ * resmcm_gpu.h — C ABI of the GB300 (sm_103a) sparse-matrix-chain engine.
+ *
+ * Drop-in for the RESMCM chain path of efficient/resmcm.cpp
+ * (swordzlim/RESMCM_ARI): RES row-wise sparsity estimator → chain-order DP →
+ * Gustavson SpGEMM chain.  The reference has no library boundary; its seam is
+ * the function SSP_dynamic (efficient/resmcm.cpp:653-772) called by
+ * build_pair (:774-779) from main (:782-895).  Each entry point below names
+ * the reference interface it replaces.
+ *
+ * Conventions
+ *   - Every function returns an rmcm_status (0 = RMCM_OK); no C++ exception
+ *     crosses the boundary.  rmcm_last_error() gives a message for the last
+ *     failing call on a handle.
+ *   - Plain pointers and sizes only.  Host arrays are caller-owned; device
+ *     matrices (rmcm_mat) are owned by the handle that made them and freed
+ *     with rmcm_mat_free (leaf matrices are owned by their graph).
+ *   - Vertex ids inside matrices are per-type LOCAL ids: the rank of a vertex
+ *     among the ascending global ids of its type (the order of
+ *     HeteroGraph::bins, efficient/resmcm.cpp:214-222).  Rows of every matrix
+ *     have ascending column indices.
+ *   - Work is issued on the handle's CUDA stream (rmcm_set_stream).  Calls
+ *     that return host data synchronise that stream.
+ *   - A handle is not thread-safe; use one handle per host thread.
+ */
+#ifndef RESMCM_GPU_H
+#define RESMCM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define RMCM_API __attribute__((visibility("default")))
+#else
+#define RMCM_API
+#endif
+
+typedef enum rmcm_status {
+    RMCM_OK = 0,
+    RMCM_EINVAL = 1,        /* bad argument, shape mismatch, bad meta-path */
+    RMCM_ENOMEM = 2,        /* device memory budget or device allocation exhausted */
+    RMCM_EOVERFLOW = 3,     /* a path count exceeded the value type (structure still exact) */
+    RMCM_ETIMEOUT = 4,      /* a bounded device wait gave up */
+    RMCM_ECUDA = 5,         /* CUDA runtime error */
+    RMCM_EIO = 6,           /* file could not be read */
+    RMCM_EPARSE = 7,        /* malformed input file */
+    RMCM_EINTERNAL = 8      /* a device-side invariant check failed */
+} rmcm_status;
+
+typedef enum rmcm_valtype {
+    RMCM_VAL_U32 = 0,       /* uint32 path counts */
+    RMCM_VAL_U64 = 1,       /* uint64 path counts */
+    RMCM_VAL_AUTO = 2       /* uint32, re-run in uint64 if a count overflows */
+} rmcm_valtype;
+
+typedef struct rmcm_handle rmcm_handle;
+typedef struct rmcm_graph rmcm_graph;
+typedef struct rmcm_mat rmcm_mat;
+
+typedef struct rmcm_opts {
+    int32_t device;            /* CUDA device ordinal */
+    int32_t valtype;           /* rmcm_valtype used by rmcm_run_metapath / rmcm_chain */
+    int64_t mem_budget_bytes;  /* 0 = 90% of the device memory free at create time */
+    void *stream;              /* cudaStream_t to use; NULL = the handle creates one */
+} rmcm_opts;
+
+/* Times of one chain, with the region definitions of the reference's timers
+ * (efficient/resmcm.cpp:18-21): es = estimator (:506-517), dp = DP (:519-538),
+ * spgemm = sum of the products (:620-645), total = whole chain after the
+ * leaf matrices exist (:679-771).  Seconds. */
+typedef struct rmcm_timings {
+    double total_s;
+    double spgemm_s;
+    double dp_s;
+    double es_s;
+    int64_t nnz;               /* result nnz (Boolean structure size) */
+    int64_t flops;             /* sum over the products of the multiply-adds */
+    int32_t valtype;           /* value type the result was computed in */
+    int32_t n_products;
+} rmcm_timings;
+
+/* Per-product record kept while profiling is on (rmcm_set_profiling,
+ * rmcm_get_product_stats).
+ * Bytes are the algorithmic (compulsory) bytes of C = A*B: with ip = 8
+ * (row pointers) and iv = value bytes, bytes_a = (rows+1)*ip + nnz_a*(4+iv),
+ * bytes_b_touched = sum over the distinct columns c of A of
+ * (2*ip + |B[c]|*(4+iv)), bytes_c = (rows+1)*ip + nnz_c*(4+iv). */
+typedef struct rmcm_product_stats {
+    int64_t rows, inner, cols;          /* A is rows x inner, B is inner x cols */
+    int64_t nnz_a, nnz_b, nnz_c, flops;
+    int64_t touched_rows;               /* distinct columns of A (B rows read); level 2 only */
+    int64_t touched_nnz;                /* entries of those B rows; level 2 only */
+    int64_t bytes_a, bytes_b_touched, bytes_c;   /* level 2 only */
+    double analyze_ms, symbolic_ms, numeric_ms;  /* CUDA-event times on the handle's stream */
+    int32_t valtype;
+    int32_t bin_rows[5];                /* rows per bin: tiny, hash512, hash2k, hash8k, dense */
+} rmcm_product_stats;
+
+/* ---- handle -------------------------------------------------------------- */
+RMCM_API const char *rmcm_status_string(int32_t status);
+RMCM_API int32_t rmcm_create(rmcm_handle **out, const rmcm_opts *opts);
+RMCM_API int32_t rmcm_destroy(rmcm_handle *h);
+RMCM_API const char *rmcm_last_error(const rmcm_handle *h);
+RMCM_API int32_t rmcm_set_stream(rmcm_handle *h, void *stream);
+RMCM_API void *rmcm_get_stream(const rmcm_handle *h);
+/* Bytes of device memory currently held by matrices and scratch. */
+RMCM_API int64_t rmcm_mem_in_use(const rmcm_handle *h);
+/* Number of kernels this handle has launched so far. */
+RMCM_API int64_t rmcm_kernel_launches(const rmcm_handle *h);
+/* Profiling of SpGEMM products: 0 off, 1 CUDA-event times, 2 times and
+ * algorithmic byte counts (adds a small kernel and a sync per product). */
+RMCM_API int32_t rmcm_set_profiling(rmcm_handle *h, int32_t level);
+/* Copies up to cap records (oldest first) of the products run since the
+ * last reset; *count = records available.  reset != 0 drops them after the
+ * copy.  Synchronises the handle's stream. */
+RMCM_API int32_t rmcm_get_product_stats(rmcm_handle *h, rmcm_product_stats *out, int32_t cap, int32_t *count,
+                                        int32_t reset);
+
+/* ---- typed graph: replaces DataReader + HeteroGraph, efficient/resmcm.cpp:49-240 ---- */
+/* Reads vertex.txt (vid vt), edge.txt (eid et) and graph.txt (vid (nbr eid)*). */
+RMCM_API int32_t rmcm_graph_load_text(rmcm_handle *h, const char *graph_file, const char *vertex_file,
+                                      const char *edge_file, rmcm_graph **out);
+/* Same graph from arrays: vtype[n], adjacency adj_ptr[n+1] / adj_nbr[m] / adj_et[m]
+ * (global ids, graph.txt order, adj_et = edge TYPE of each entry). */
+RMCM_API int32_t rmcm_graph_from_adjacency(rmcm_handle *h, int64_t n, const int32_t *vtype,
+                                           const int64_t *adj_ptr, const int32_t *adj_nbr,
+                                           const int32_t *adj_et, rmcm_graph **out);
+RMCM_API int32_t rmcm_graph_free(rmcm_graph *g);
+RMCM_API int32_t rmcm_graph_info(const rmcm_graph *g, int64_t *n, int64_t *m, int32_t *max_vt);
+/* Vertices of type vt (HeteroGraph::dimensions, efficient/resmcm.cpp:206-212). */
+RMCM_API int64_t rmcm_graph_dim(const rmcm_graph *g, int32_t vt);
+
+/* ---- meta-path: replaces MetaPath(string) / toString, efficient/resmcm.cpp:269-308 ---- */
+/* vts needs cap+1 slots, ets cap slots; *len = number of edge types (matrices). */
+RMCM_API int32_t rmcm_metapath_parse(const char *s, int32_t *vts, int32_t *ets, int32_t cap, int32_t *len);
+RMCM_API int32_t rmcm_metapath_format(const int32_t *vts, const int32_t *ets, int32_t len, char *buf,
+                                      int64_t cap);
+
+/* ---- matrices ------------------------------------------------------------ */
+/* Leaf matrix of one edge type: replaces BoolMatrix(HIN, vt, src, sink, et, n),
+ * efficient/resmcm.cpp:374-396.  Rows = vertices of type src, columns =
+ * vertices of type sink, one entry (value 1) per adjacency entry of edge type
+ * et whose neighbour has type sink; repeated neighbours stay separate entries.
+ * Device resident and cached in the graph (owned by it; do not free). */
+RMCM_API int32_t rmcm_leaf(rmcm_handle *h, rmcm_graph *g, int32_t src_vt, int32_t sink_vt, int32_t et,
+                           int32_t valtype, rmcm_mat **out);
+/* Upload a CSR from host memory (rowptr[rows+1], col[nnz], val[nnz] of
+ * valtype or NULL for all ones).  Rows need not be sorted: they are sorted on
+ * the device.  Columns are checked against cols. */
+RMCM_API int32_t rmcm_mat_upload(rmcm_handle *h, int64_t rows, int64_t cols, const int64_t *rowptr,
+                                 const int32_t *col, const void *val, int32_t valtype, rmcm_mat **out);
+RMCM_API int32_t rmcm_mat_info(const rmcm_mat *m, int64_t *rows, int64_t *cols, int64_t *nnz,
+                               int32_t *valtype);
+/* Copy a device matrix to host arrays (rowptr[rows+1], col[nnz], val[nnz]);
+ * any pointer may be NULL to skip that array. */
+RMCM_API int32_t rmcm_mat_download(rmcm_handle *h, const rmcm_mat *m, int64_t *rowptr, int32_t *col,
+                                   void *val);
+RMCM_API int32_t rmcm_mat_free(rmcm_handle *h, rmcm_mat *m);
+
+/* ---- stage (a): RES estimator ---------------------------------------------
+ * Replaces the estimator loop of rows_sparse_optimal_matrix_chain_order
+ * (efficient/resmcm.cpp:506-517) with getSparsities (:442-452) and
+ * compute_sparsities (:468-485).  c_out[len*len] receives c_[i*len+j]
+ * (estimated nnz of M_i..M_j, j > i; 0 elsewhere) in FP64. */
+RMCM_API int32_t rmcm_estimate(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, double *c_out);
+
+/* ---- stage (b): chain-order DP --------------------------------------------
+ * Replaces the DP of rows_sparse_optimal_matrix_chain_order
+ * (efficient/resmcm.cpp:519-536) and get_optimal_chain_order (:563-573).
+ * Runs as one warp on the device, 2 <= len <= 16.  split/cost are len*len
+ * (may be NULL); pairs[2*(len-1)] receives the post-order (k,l) list where -1
+ * means "the top of the temporary stack". */
+RMCM_API int32_t rmcm_order(rmcm_handle *h, const double *c, int32_t len, int32_t *split, double *cost,
+                            int32_t *pairs);
+
+/* ---- stage (c): Gustavson SpGEMM ------------------------------------------
+ * Replaces SpGEMM / row_wise_SpGEMM_based_on_bitmap (efficient/resmcm.cpp:586-647).
+ * C = A*B with exact integer path counts in A's value type; C's rows are
+ * sorted.  Returns RMCM_EOVERFLOW (C kept) if a count overflowed. */
+RMCM_API int32_t rmcm_spgemm(rmcm_handle *h, const rmcm_mat *A, const rmcm_mat *B, rmcm_mat **C);
+
+/* ---- (a)+(b)+(c): one chain -----------------------------------------------
+ * Replaces SSP_dynamic (efficient/resmcm.cpp:653-772) on matrices that are
+ * already device resident.  The chain's matrices are not modified.  When
+ * pairs is non-NULL it overrides the DP's order (same encoding as rmcm_order). */
+RMCM_API int32_t rmcm_chain(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, const int32_t *pairs,
+                            rmcm_mat **C, rmcm_timings *t);
+
+/* ---- whole meta-path over a graph -----------------------------------------
+ * build_pair + nnz count of main (efficient/resmcm.cpp:774-779, :859-868):
+ * leaf matrices (cached in the graph), then rmcm_chain.  C may be NULL, in
+ * which case the result is freed after its nnz is taken. */
+RMCM_API int32_t rmcm_run_metapath(rmcm_handle *h, rmcm_graph *g, const char *metapath, rmcm_mat **C,
+                                   rmcm_timings *t);
+
+/* Estimated nnz of the whole chain, c_[0][len-1]: the estimator-only program
+ * accuracy/res.cpp (final_result_estimate :564-600, output :698). */
+RMCM_API int32_t rmcm_estimate_metapath(rmcm_handle *h, rmcm_graph *g, const char *metapath,
+                                        double *est_nnz);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RESMCM_GPU_H */

@@ -1,0 +1,385 @@
+"""GB300 (sm_103a) engine for RESMCM sparse matrix chain multiplication.
+
+Python mirror of the reference program's interface (efficient/resmcm.cpp of
+swordzlim/RESMCM_ARI) over the C ABI of ``libresmcm_gpu.so``
+(``include/resmcm_gpu.h``):
+
+==========================  ==============================================
+reference                   here
+==========================  ==============================================
+``HeteroGraph(g, v, e)``    ``HeteroGraph.from_text(engine, g, v, e)``
+``MetaPath(str)``           ``MetaPath(str)``  (same grammar, ``toString``)
+``BoolMatrix(HIN, ...)``    ``HeteroGraph.leaf(src, sink, et)``
+``getSparsities`` +         ``Engine.estimate(chain)``
+``compute_sparsities``
+DP + order                  ``Engine.order(c)``
+``SpGEMM``                  ``Engine.spgemm(A, B)``
+``SSP_dynamic``             ``Engine.chain(chain)`` / ``Engine.run_metapath``
+``accuracy/res`` estimate   ``Engine.estimate_metapath``
+==========================  ==============================================
+
+Every product runs on the GPU through the native library; there is no CPU
+fallback.  Importing the package never needs a GPU; creating an ``Engine``
+does, and raises ``RuntimeError`` when the library or the device is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_build", "libresmcm_gpu.so")
+CLI_PATH = os.path.join(_PKG, "_build", "resmcm_gpu")
+HEADER_PATH = os.path.join(os.path.dirname(_PKG), "include", "resmcm_gpu.h")
+
+OK, EINVAL, ENOMEM, EOVERFLOW, ETIMEOUT, ECUDA, EIO, EPARSE, EINTERNAL = range(9)
+VAL_U32, VAL_U64, VAL_AUTO = 0, 1, 2
+_VAL_DTYPE = {VAL_U32: np.uint32, VAL_U64: np.uint64}
+
+
+class RmcmError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+class Opts(C.Structure):
+    _fields_ = [("device", C.c_int32), ("valtype", C.c_int32), ("mem_budget_bytes", C.c_int64),
+                ("stream", C.c_void_p)]
+
+
+class Timings(C.Structure):
+    _fields_ = [("total_s", C.c_double), ("spgemm_s", C.c_double), ("dp_s", C.c_double), ("es_s", C.c_double),
+                ("nnz", C.c_int64), ("flops", C.c_int64), ("valtype", C.c_int32), ("n_products", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class ProductStats(C.Structure):
+    _fields_ = [("rows", C.c_int64), ("inner", C.c_int64), ("cols", C.c_int64),
+                ("nnz_a", C.c_int64), ("nnz_b", C.c_int64), ("nnz_c", C.c_int64), ("flops", C.c_int64),
+                ("touched_rows", C.c_int64), ("touched_nnz", C.c_int64),
+                ("bytes_a", C.c_int64), ("bytes_b_touched", C.c_int64), ("bytes_c", C.c_int64),
+                ("analyze_ms", C.c_double), ("symbolic_ms", C.c_double), ("numeric_ms", C.c_double),
+                ("valtype", C.c_int32), ("bin_rows", C.c_int32 * 5)]
+
+    def as_dict(self) -> dict:
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f != "bin_rows"}
+        d["bin_rows"] = list(self.bin_rows)
+        return d
+
+
+_lib = None
+
+
+def build(verbose: bool = False) -> str:
+    from . import native_build
+    return native_build.build(verbose=verbose)
+
+
+def lib():
+    """Load libresmcm_gpu.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"native library missing: {LIB_PATH} (run resmcm_ari_gb300.build())")
+    L = C.CDLL(LIB_PATH)
+    vp, i32, i64, f64p = C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_double)
+    pp = C.POINTER(C.c_void_p)
+    sig = {
+        "rmcm_status_string": ([i32], C.c_char_p),
+        "rmcm_create": ([pp, C.POINTER(Opts)], i32),
+        "rmcm_destroy": ([vp], i32),
+        "rmcm_last_error": ([vp], C.c_char_p),
+        "rmcm_set_stream": ([vp, vp], i32),
+        "rmcm_get_stream": ([vp], vp),
+        "rmcm_mem_in_use": ([vp], i64),
+        "rmcm_kernel_launches": ([vp], i64),
+        "rmcm_set_profiling": ([vp, i32], i32),
+        "rmcm_get_product_stats": ([vp, C.POINTER(ProductStats), i32, C.POINTER(i32), i32], i32),
+        "rmcm_graph_load_text": ([vp, C.c_char_p, C.c_char_p, C.c_char_p, pp], i32),
+        "rmcm_graph_from_adjacency": ([vp, i64, vp, vp, vp, vp, pp], i32),
+        "rmcm_graph_free": ([vp], i32),
+        "rmcm_graph_info": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i32)], i32),
+        "rmcm_graph_dim": ([vp, i32], i64),
+        "rmcm_metapath_parse": ([C.c_char_p, vp, vp, i32, C.POINTER(i32)], i32),
+        "rmcm_metapath_format": ([vp, vp, i32, C.c_char_p, i64], i32),
+        "rmcm_leaf": ([vp, vp, i32, i32, i32, i32, pp], i32),
+        "rmcm_mat_upload": ([vp, i64, i64, vp, vp, vp, i32, pp], i32),
+        "rmcm_mat_info": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i32)], i32),
+        "rmcm_mat_download": ([vp, vp, vp, vp, vp], i32),
+        "rmcm_mat_free": ([vp, vp], i32),
+        "rmcm_estimate": ([vp, vp, i32, vp], i32),
+        "rmcm_order": ([vp, vp, i32, vp, vp, vp], i32),
+        "rmcm_spgemm": ([vp, vp, vp, pp], i32),
+        "rmcm_chain": ([vp, vp, i32, vp, pp, C.POINTER(Timings)], i32),
+        "rmcm_run_metapath": ([vp, vp, C.c_char_p, pp, C.POINTER(Timings)], i32),
+        "rmcm_estimate_metapath": ([vp, vp, C.c_char_p, f64p], i32),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def header_symbols() -> list:
+    """Names of every entry point declared in include/resmcm_gpu.h."""
+    import re
+    text = open(HEADER_PATH).read()
+    return re.findall(r"RMCM_API\s+[\w\s\*]+?\b(rmcm_\w+)\s*\(", text)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class MetaPath:
+    """Meta-path string grammar of MetaPath(string), efficient/resmcm.cpp:269-299."""
+
+    def __init__(self, s: str):
+        vts = np.zeros(65, np.int32)
+        ets = np.zeros(64, np.int32)
+        n = C.c_int32(0)
+        rc = lib().rmcm_metapath_parse(s.encode(), _ptr(vts), _ptr(ets), 64, C.byref(n))
+        if rc != OK:
+            raise ValueError(f"the meta-path is incorrect: {s!r}")
+        self.vertex_types = vts[:n.value + 1].copy()
+        self.edge_types = ets[:n.value].copy()
+        self.path_len = n.value
+        self.source = s
+
+    def to_string(self) -> str:
+        """MetaPath::toString, efficient/resmcm.cpp:301-308."""
+        buf = C.create_string_buffer(16 * (2 * self.path_len + 1) + 16)
+        lib().rmcm_metapath_format(_ptr(self.vertex_types), _ptr(self.edge_types), self.path_len, buf, len(buf))
+        return buf.value.decode()
+
+    toString = to_string
+
+
+class Matrix:
+    """A device-resident CSR owned by an Engine (or by a graph for leaves)."""
+
+    def __init__(self, engine: "Engine", handle: int, owned: bool = True):
+        self.engine = engine
+        self._h = C.c_void_p(handle)
+        self.owned = owned
+
+    @property
+    def shape(self):
+        rows, cols, nnz, vt = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int32()
+        lib().rmcm_mat_info(self._h, C.byref(rows), C.byref(cols), C.byref(nnz), C.byref(vt))
+        return rows.value, cols.value
+
+    @property
+    def nnz(self) -> int:
+        nnz = C.c_int64()
+        lib().rmcm_mat_info(self._h, None, None, C.byref(nnz), None)
+        return nnz.value
+
+    @property
+    def valtype(self) -> int:
+        vt = C.c_int32()
+        lib().rmcm_mat_info(self._h, None, None, None, C.byref(vt))
+        return vt.value
+
+    def download(self, values: bool = True):
+        """(rowptr int64, col int32, val uint32/uint64 or None) on the host."""
+        rows, _ = self.shape
+        nnz = self.nnz
+        rp = np.zeros(rows + 1, np.int64)
+        col = np.zeros(max(nnz, 1), np.int32)
+        val = np.zeros(max(nnz, 1), _VAL_DTYPE[self.valtype]) if values else None
+        self.engine._check(lib().rmcm_mat_download(self.engine._h, self._h, _ptr(rp), _ptr(col),
+                                                   _ptr(val) if values else None))
+        return rp, col[:nnz], (val[:nnz] if values else None)
+
+    def free(self):
+        if self.owned and self._h:
+            lib().rmcm_mat_free(self.engine._h, self._h)
+        self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class HeteroGraph:
+    """Typed graph (HeteroGraph, efficient/resmcm.cpp:181-240) with a device leaf cache."""
+
+    def __init__(self, engine: "Engine", handle: int):
+        self.engine = engine
+        self._h = C.c_void_p(handle)
+
+    @classmethod
+    def from_text(cls, engine: "Engine", graph: str, vertex: str, edge: str) -> "HeteroGraph":
+        h = C.c_void_p()
+        engine._check(lib().rmcm_graph_load_text(engine._h, graph.encode(), vertex.encode(), edge.encode(),
+                                                 C.byref(h)))
+        return cls(engine, h.value)
+
+    @classmethod
+    def from_adjacency(cls, engine: "Engine", vtype, adj_ptr, adj_nbr, adj_et) -> "HeteroGraph":
+        vtype = np.ascontiguousarray(vtype, np.int32)
+        adj_ptr = np.ascontiguousarray(adj_ptr, np.int64)
+        adj_nbr = np.ascontiguousarray(adj_nbr, np.int32)
+        adj_et = np.ascontiguousarray(adj_et, np.int32)
+        h = C.c_void_p()
+        engine._check(lib().rmcm_graph_from_adjacency(engine._h, vtype.size, _ptr(vtype), _ptr(adj_ptr),
+                                                      _ptr(adj_nbr), _ptr(adj_et), C.byref(h)))
+        return cls(engine, h.value)
+
+    @classmethod
+    def from_synthetic(cls, engine: "Engine", g) -> "HeteroGraph":
+        ptr, nbr, et = g.adjacency()
+        return cls.from_adjacency(engine, g.vertex_types(), ptr, nbr, et)
+
+    def info(self):
+        n, m, mv = C.c_int64(), C.c_int64(), C.c_int32()
+        lib().rmcm_graph_info(self._h, C.byref(n), C.byref(m), C.byref(mv))
+        return n.value, m.value, mv.value
+
+    def dim(self, vt: int) -> int:
+        return lib().rmcm_graph_dim(self._h, vt)
+
+    def leaf(self, src: int, sink: int, et: int, valtype: int = VAL_U32) -> Matrix:
+        """BoolMatrix(HIN, vt, src, sink, et, n), efficient/resmcm.cpp:374-396 (graph-owned)."""
+        h = C.c_void_p()
+        self.engine._check(lib().rmcm_leaf(self.engine._h, self._h, src, sink, et, valtype, C.byref(h)))
+        return Matrix(self.engine, h.value, owned=False)
+
+    def leaves(self, metapath: str, valtype: int = VAL_U32) -> list:
+        mp = MetaPath(metapath)
+        return [self.leaf(int(mp.vertex_types[i]), int(mp.vertex_types[i + 1]), int(mp.edge_types[i]), valtype)
+                for i in range(mp.path_len)]
+
+    def close(self):
+        if self._h:
+            lib().rmcm_graph_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Engine:
+    """One handle on one GPU (rmcm_create); not thread-safe."""
+
+    def __init__(self, device: int = 0, valtype: int = VAL_AUTO, mem_budget_bytes: int = 0, stream=None):
+        o = Opts(device, valtype, mem_budget_bytes, stream)
+        h = C.c_void_p()
+        rc = lib().rmcm_create(C.byref(h), C.byref(o))
+        if rc != OK:
+            raise RmcmError(rc, f"rmcm_create failed: {lib().rmcm_status_string(rc).decode()}")
+        self._h = h
+
+    def _check(self, rc: int, allow=(OK,)):
+        if rc not in allow:
+            msg = lib().rmcm_last_error(self._h).decode() if self._h else ""
+            raise RmcmError(rc, f"{lib().rmcm_status_string(rc).decode()}: {msg}")
+        return rc
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().rmcm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return lib().rmcm_get_stream(self._h) or 0
+
+    def set_stream(self, stream: int):
+        self._check(lib().rmcm_set_stream(self._h, C.c_void_p(stream)))
+
+    @property
+    def mem_in_use(self) -> int:
+        return lib().rmcm_mem_in_use(self._h)
+
+    @property
+    def kernel_launches(self) -> int:
+        return lib().rmcm_kernel_launches(self._h)
+
+    def set_profiling(self, level: int):
+        self._check(lib().rmcm_set_profiling(self._h, level))
+
+    def product_stats(self, reset: bool = True) -> list:
+        n = C.c_int32()
+        self._check(lib().rmcm_get_product_stats(self._h, None, 0, C.byref(n), 0))
+        arr = (ProductStats * max(n.value, 1))()
+        self._check(lib().rmcm_get_product_stats(self._h, arr, n.value, C.byref(n), 1 if reset else 0))
+        return [arr[i].as_dict() for i in range(n.value)]
+
+    def upload(self, rowptr, col, cols: int, val=None, valtype: int = VAL_U32) -> Matrix:
+        rowptr = np.ascontiguousarray(rowptr, np.int64)
+        col = np.ascontiguousarray(col, np.int32)
+        v = None if val is None else np.ascontiguousarray(val, _VAL_DTYPE[valtype])
+        h = C.c_void_p()
+        self._check(lib().rmcm_mat_upload(self._h, rowptr.size - 1, cols, _ptr(rowptr), _ptr(col),
+                                          None if v is None else _ptr(v), valtype, C.byref(h)))
+        return Matrix(self, h.value)
+
+    @staticmethod
+    def _chain_ptrs(chain):
+        arr = (C.c_void_p * len(chain))(*[m._h.value for m in chain])
+        return arr
+
+    def estimate(self, chain) -> np.ndarray:
+        L = len(chain)
+        c = np.zeros(L * L, np.float64)
+        self._check(lib().rmcm_estimate(self._h, self._chain_ptrs(chain), L, _ptr(c)))
+        return c.reshape(L, L)
+
+    def order(self, c: np.ndarray):
+        c = np.ascontiguousarray(c, np.float64)
+        L = c.shape[0]
+        s = np.zeros(L * L, np.int32)
+        m = np.zeros(L * L, np.float64)
+        pairs = np.zeros(max(2 * (L - 1), 1), np.int32)
+        self._check(lib().rmcm_order(self._h, _ptr(c), L, _ptr(s), _ptr(m), _ptr(pairs)))
+        return s.reshape(L, L), m.reshape(L, L), pairs[:2 * (L - 1)].reshape(-1, 2)
+
+    def spgemm(self, A: Matrix, B: Matrix) -> Matrix:
+        h = C.c_void_p()
+        self._check(lib().rmcm_spgemm(self._h, A._h, B._h, C.byref(h)), allow=(OK, EOVERFLOW))
+        return Matrix(self, h.value)
+
+    def chain(self, chain, pairs=None):
+        h = C.c_void_p()
+        t = Timings()
+        p = None
+        if pairs is not None:
+            pa = np.ascontiguousarray(np.asarray(pairs).reshape(-1), np.int32)
+            p = _ptr(pa)
+        rc = self._check(lib().rmcm_chain(self._h, self._chain_ptrs(chain), len(chain), p, C.byref(h), C.byref(t)),
+                         allow=(OK, EOVERFLOW))
+        return Matrix(self, h.value), t.as_dict(), rc
+
+    def run_metapath(self, graph: HeteroGraph, metapath: str, keep: bool = True):
+        h = C.c_void_p()
+        t = Timings()
+        rc = self._check(lib().rmcm_run_metapath(self._h, graph._h, metapath.encode(),
+                                                 C.byref(h) if keep else None, C.byref(t)),
+                         allow=(OK, EOVERFLOW))
+        return (Matrix(self, h.value) if keep else None), t.as_dict(), rc
+
+    def estimate_metapath(self, graph: HeteroGraph, metapath: str) -> float:
+        est = C.c_double()
+        self._check(lib().rmcm_estimate_metapath(self._h, graph._h, metapath.encode(), C.byref(est)))
+        return est.value

@@ -1,0 +1,962 @@
+// C ABI of the GB300 chain engine: handle, device memory, typed graph, leaf
+// matrices, the three stages and the chain executor.
+//
+// The executor restates SSP_dynamic (efficient/resmcm.cpp:653-772): leaf
+// matrices first (not timed, :664-667), then inside the timed region the
+// estimator, the DP, the order and a stack machine over the (k, l) pairs
+// (:709-760) that multiplies leaves and temporaries and frees every operand
+// right after its last use.  Leaves stay resident in the graph's cache.
+#include <cuda_runtime.h>
+#include <omp.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+using namespace rmcm;
+
+namespace rmcm {
+
+int32_t set_error(rmcm_handle *h, int32_t status, const std::string &msg) {
+    if (h) h->last_error = msg;
+    return status;
+}
+
+int32_t cuda_error(rmcm_handle *h, cudaError_t e, const char *what) {
+    std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return set_error(h, RMCM_ENOMEM, msg);
+    return set_error(h, RMCM_ECUDA, msg);
+}
+
+int32_t dev_alloc(rmcm_handle *h, void **p, int64_t bytes) {
+    *p = nullptr;
+    if (bytes <= 0) bytes = 256;
+    if (h->in_use + bytes > h->budget)
+        return set_error(h, RMCM_ENOMEM,
+                         "device memory budget exhausted: need " + std::to_string(bytes) + " bytes, " +
+                             std::to_string(h->budget - h->in_use) + " left");
+    cudaError_t e = cudaMallocAsync(p, (size_t)bytes, h->stream);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return cuda_error(h, e, "cudaMallocAsync");
+    }
+    h->in_use += bytes;
+    return RMCM_OK;
+}
+
+void dev_free(rmcm_handle *h, void *p, int64_t bytes) {
+    if (!p) return;
+    if (bytes <= 0) bytes = 256;
+    cudaFreeAsync(p, h->stream);
+    h->in_use -= bytes;
+}
+
+int32_t scratch_reserve(rmcm_handle *h, int64_t bytes) {
+    if (bytes <= h->scratch_bytes) return RMCM_OK;
+    int64_t want = std::max<int64_t>(bytes, h->scratch_bytes + h->scratch_bytes / 2);
+    if (h->scratch) {
+        dev_free(h, h->scratch, h->scratch_bytes);
+        h->scratch = nullptr;
+        h->scratch_bytes = 0;
+    }
+    int32_t rc = dev_alloc(h, &h->scratch, want);
+    if (rc != RMCM_OK) {
+        rc = dev_alloc(h, &h->scratch, bytes);
+        if (rc != RMCM_OK) return rc;
+        want = bytes;
+    }
+    h->scratch_bytes = want;
+    return RMCM_OK;
+}
+
+// Creates *out with its row pointer when *out is null; allocates col/val for
+// nnz entries when nnz >= 0.
+int32_t mat_alloc(rmcm_handle *h, int64_t rows, int64_t cols, int64_t nnz, int32_t valtype, rmcm_mat **out) {
+    rmcm_mat *m = *out;
+    if (!m) {
+        m = new rmcm_mat();
+        m->valtype = valtype;
+        m->d.rows = rows;
+        m->d.cols = cols;
+        void *rp = nullptr;
+        int32_t rc = dev_alloc(h, &rp, 8 * (rows + 1));
+        if (rc != RMCM_OK) {
+            delete m;
+            return rc;
+        }
+        m->d.rowptr = (int64_t *)rp;
+        m->bytes = 8 * (rows + 1);
+        *out = m;
+    }
+    if (nnz >= 0) {
+        void *c = nullptr, *v = nullptr;
+        RMCM_TRY(dev_alloc(h, &c, 4 * nnz));
+        int32_t rc = dev_alloc(h, &v, val_bytes(m->valtype) * nnz);
+        if (rc != RMCM_OK) {
+            dev_free(h, c, 4 * nnz);
+            return rc;
+        }
+        m->d.col = (int32_t *)c;
+        m->d.val = v;
+        m->d.nnz = nnz;
+        m->bytes += (4 + val_bytes(m->valtype)) * nnz;
+    }
+    return RMCM_OK;
+}
+
+void mat_release(rmcm_handle *h, rmcm_mat *m) {
+    if (!m) return;
+    dev_free(h, m->d.rowptr, 8 * (m->d.rows + 1));
+    if (m->d.col) dev_free(h, m->d.col, 4 * m->d.nnz);
+    if (m->d.val) dev_free(h, m->d.val, val_bytes(m->valtype) * m->d.nnz);
+    delete m;
+}
+
+int32_t check_status(rmcm_handle *h) {
+    RMCM_CUDA(h, cudaMemcpyAsync(h->h_status, h->d_status, sizeof(int) * kNumStatus, cudaMemcpyDeviceToHost, h->stream));
+    RMCM_CUDA(h, cudaStreamSynchronize(h->stream));
+    int st[kNumStatus];
+    memcpy(st, h->h_status, sizeof(st));
+    bool any = false;
+    for (int i = 0; i < kNumStatus; i++) any |= st[i] != 0;
+    if (!any) return RMCM_OK;
+    RMCM_CUDA(h, cudaMemsetAsync(h->d_status, 0, sizeof(int) * kNumStatus, h->stream));
+    if (st[kInvariant]) return set_error(h, RMCM_EINTERNAL, "device invariant check failed");
+    if (st[kTimeout]) return set_error(h, RMCM_ETIMEOUT, "a bounded device wait gave up");
+    if (st[kArena]) return set_error(h, RMCM_ENOMEM, "device arena exhausted");
+    return set_error(h, RMCM_EOVERFLOW, "a path count overflowed the value type");
+}
+
+}  // namespace rmcm
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// text loader (reference file formats of DataReader, efficient/resmcm.cpp:49-177)
+// ---------------------------------------------------------------------------
+
+bool read_file(const char *path, std::string &buf) {
+    FILE *f = fopen(path, "rb");
+    if (!f) return false;
+    if (fseek(f, 0, SEEK_END) != 0) {
+        fclose(f);
+        return false;
+    }
+    long sz = ftell(f);
+    if (sz < 0) {
+        fclose(f);
+        return false;
+    }
+    rewind(f);
+    buf.resize((size_t)sz);
+    size_t got = sz ? fread(&buf[0], 1, (size_t)sz, f) : 0;
+    fclose(f);
+    buf.resize(got);
+    return true;
+}
+
+// One line at a time; numbers are non-negative decimal integers separated by
+// blanks (a leading '+' is accepted, as istringstream does).
+struct LineReader {
+    const char *p, *end;
+    explicit LineReader(const std::string &s) : p(s.data()), end(s.data() + s.size()) {}
+    bool next_line(const char *&b, const char *&e) {
+        if (p >= end) return false;
+        b = p;
+        const char *q = (const char *)memchr(p, '\n', (size_t)(end - p));
+        e = q ? q : end;
+        p = q ? q + 1 : end;
+        return true;
+    }
+};
+
+inline bool is_blank(char c) { return c == ' ' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; }
+
+// 1 = number read, 0 = end of line, -1 = malformed
+inline int parse_num(const char *&p, const char *e, int64_t &out) {
+    while (p < e && is_blank(*p)) p++;
+    if (p >= e) return 0;
+    if (*p == '+') p++;
+    if (p >= e || *p < '0' || *p > '9') return -1;
+    int64_t v = 0;
+    while (p < e && *p >= '0' && *p <= '9') {
+        v = v * 10 + (*p - '0');
+        if (v > ((int64_t)1 << 50)) return -1;
+        p++;
+    }
+    if (p < e && !is_blank(*p)) return -1;
+    out = v;
+    return 1;
+}
+
+int32_t graph_finish(rmcm_graph *g) {
+    const int32_t nt = g->max_vt + 1;
+    g->dims.assign(nt, 0);
+    for (int64_t v = 0; v < g->n; v++) g->dims[g->vtype[v]]++;
+    g->bin_ptr.assign(nt + 1, 0);
+    for (int32_t t = 0; t < nt; t++) g->bin_ptr[t + 1] = g->bin_ptr[t] + g->dims[t];
+    g->bin_ids.resize(g->n);
+    g->local.resize(g->n);
+    std::vector<int64_t> fill(nt, 0);
+    for (int64_t v = 0; v < g->n; v++) {
+        const int32_t t = g->vtype[v];
+        g->local[v] = (int32_t)fill[t];
+        g->bin_ids[g->bin_ptr[t] + fill[t]++] = (int32_t)v;
+    }
+    return RMCM_OK;
+}
+
+int32_t load_text(rmcm_handle *h, const char *gfile, const char *vfile, const char *efile, rmcm_graph *g) {
+    std::string vb, eb, gb;
+    if (!read_file(vfile, vb)) return set_error(h, RMCM_EIO, std::string("cannot open ") + vfile);
+    if (!read_file(efile, eb)) return set_error(h, RMCM_EIO, std::string("cannot open ") + efile);
+    if (!read_file(gfile, gb)) return set_error(h, RMCM_EIO, std::string("cannot open ") + gfile);
+    // n = number of lines of vertex.txt
+    int64_t n = 0;
+    for (char c : vb) n += c == '\n';
+    if (!vb.empty() && vb.back() != '\n') n++;
+    g->n = n;
+    g->vtype.assign(n, 0);
+    g->max_vt = 0;
+    {
+        LineReader lr(vb);
+        const char *b, *e;
+        int64_t line = 0;
+        while (lr.next_line(b, e)) {
+            line++;
+            int64_t v, t;
+            int a = parse_num(b, e, v);
+            if (a == 0) continue;
+            if (a < 0 || parse_num(b, e, t) != 1 || v >= n || t > 1000000)
+                return set_error(h, RMCM_EPARSE, "vertex file line " + std::to_string(line) + ": expected 'vid vt'");
+            g->vtype[v] = (int32_t)t;
+            g->max_vt = std::max<int32_t>(g->max_vt, (int32_t)t);
+        }
+    }
+    // graph.txt, pass 1: m and per-vertex counts
+    std::vector<int64_t> cnt(n + 1, 0);
+    std::vector<unsigned char> seen(n, 0);
+    int64_t m = 0;
+    {
+        LineReader lr(gb);
+        const char *b, *e;
+        int64_t line = 0;
+        while (lr.next_line(b, e)) {
+            line++;
+            int64_t vid, x;
+            int a = parse_num(b, e, vid);
+            if (a == 0) continue;
+            if (a < 0 || vid >= n) return set_error(h, RMCM_EPARSE, "graph file line " + std::to_string(line) + ": bad vertex id");
+            if (seen[vid]) return set_error(h, RMCM_EPARSE, "graph file: vertex " + std::to_string(vid) + " listed twice");
+            seen[vid] = 1;
+            int64_t toks = 0;
+            while ((a = parse_num(b, e, x)) == 1) toks++;
+            if (a < 0 || toks % 2) return set_error(h, RMCM_EPARSE, "graph file line " + std::to_string(line) + ": expected 'vid (nbr eid)*'");
+            cnt[vid] = toks / 2;
+            m += toks / 2;
+        }
+    }
+    g->m = m;
+    std::vector<int32_t> etype(m, -1);
+    {
+        LineReader lr(eb);
+        const char *b, *e;
+        int64_t line = 0;
+        while (lr.next_line(b, e)) {
+            line++;
+            int64_t id, t;
+            int a = parse_num(b, e, id);
+            if (a == 0) continue;
+            if (a < 0 || parse_num(b, e, t) != 1 || id >= m)
+                return set_error(h, RMCM_EPARSE, "edge file line " + std::to_string(line) + ": expected 'eid et' with eid < m");
+            etype[id] = (int32_t)t;
+        }
+    }
+    g->adj_ptr.assign(n + 1, 0);
+    for (int64_t v = 0; v < n; v++) g->adj_ptr[v + 1] = g->adj_ptr[v] + cnt[v];
+    g->adj_nbr.resize(m);
+    g->adj_et.resize(m);
+    {
+        LineReader lr(gb);
+        const char *b, *e;
+        while (lr.next_line(b, e)) {
+            int64_t vid, nb, id;
+            if (parse_num(b, e, vid) != 1) continue;
+            int64_t pos = g->adj_ptr[vid];
+            while (parse_num(b, e, nb) == 1) {
+                parse_num(b, e, id);
+                if (nb >= n || id >= m || etype[id] < 0)
+                    return set_error(h, RMCM_EPARSE, "graph file: neighbour or edge id out of range at vertex " + std::to_string(vid));
+                g->adj_nbr[pos] = (int32_t)nb;
+                g->adj_et[pos] = etype[id];
+                pos++;
+            }
+        }
+    }
+    return graph_finish(g);
+}
+
+// ---------------------------------------------------------------------------
+// leaf matrices (BoolMatrix(HIN, vt, src, sink, et, n), efficient/resmcm.cpp:374-396)
+// ---------------------------------------------------------------------------
+
+int32_t upload_csr(rmcm_handle *h, int64_t rows, int64_t cols, const int64_t *rowptr, const int32_t *col,
+                   const void *val, int32_t valtype, rmcm_mat **out) {
+    const int64_t nnz = rows > 0 ? rowptr[rows] : 0;
+    rmcm_mat *m = nullptr;
+    RMCM_TRY(mat_alloc(h, rows, cols, nnz, valtype, &m));
+    cudaStream_t s = h->stream;
+    cudaError_t e = cudaMemcpyAsync(m->d.rowptr, rowptr, 8 * (rows + 1), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && nnz > 0) e = cudaMemcpyAsync(m->d.col, col, 4 * nnz, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && nnz > 0 && val)
+        e = cudaMemcpyAsync(m->d.val, val, val_bytes(valtype) * nnz, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) {
+        mat_release(h, m);
+        return cuda_error(h, e, "upload");
+    }
+    if (!val) {
+        int32_t rc = fill_ones(h, m->d.val, nnz, valtype);
+        if (rc != RMCM_OK) {
+            mat_release(h, m);
+            return rc;
+        }
+    }
+    *out = m;
+    return RMCM_OK;
+}
+
+int32_t build_leaf(rmcm_handle *h, rmcm_graph *g, int32_t src, int32_t sink, int32_t et, int32_t valtype,
+                   rmcm_mat **out) {
+    const int64_t rows = g->dims[src], cols = g->dims[sink];
+    const int64_t b0 = g->bin_ptr[src];
+    std::vector<int64_t> rp(rows + 1, 0);
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t r = 0; r < rows; r++) {
+        const int32_t u = g->bin_ids[b0 + r];
+        int64_t c = 0;
+        for (int64_t q = g->adj_ptr[u]; q < g->adj_ptr[u + 1]; q++)
+            c += (g->adj_et[q] == et && g->vtype[g->adj_nbr[q]] == sink);
+        rp[r + 1] = c;
+    }
+    for (int64_t r = 0; r < rows; r++) rp[r + 1] += rp[r];
+    std::vector<int32_t> col(std::max<int64_t>(rp[rows], 1));
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t r = 0; r < rows; r++) {
+        const int32_t u = g->bin_ids[b0 + r];
+        int64_t o = rp[r];
+        for (int64_t q = g->adj_ptr[u]; q < g->adj_ptr[u + 1]; q++)
+            if (g->adj_et[q] == et && g->vtype[g->adj_nbr[q]] == sink) col[o++] = g->local[g->adj_nbr[q]];
+        std::sort(col.begin() + rp[r], col.begin() + rp[r + 1]);
+    }
+    return upload_csr(h, rows, cols, rp.data(), col.data(), nullptr, valtype, out);
+}
+
+int32_t get_leaf(rmcm_handle *h, rmcm_graph *g, int32_t src, int32_t sink, int32_t et, int32_t valtype,
+                 rmcm_mat **out) {
+    if (src < 0 || src > g->max_vt || sink < 0 || sink > g->max_vt)
+        return set_error(h, RMCM_EINVAL, "meta-path names a vertex type the graph does not have");
+    auto key = std::make_tuple(src, sink, et, valtype);
+    auto it = g->leaves.find(key);
+    if (it != g->leaves.end()) {
+        *out = it->second;
+        return RMCM_OK;
+    }
+    rmcm_mat *m = nullptr;
+    RMCM_TRY(build_leaf(h, g, src, sink, et, valtype, &m));
+    m->graph_owned = true;
+    g->leaves[key] = m;
+    *out = m;
+    return RMCM_OK;
+}
+
+int32_t parse_path(const char *s, std::vector<int32_t> &vts, std::vector<int32_t> &ets) {
+    // MetaPath(string), efficient/resmcm.cpp:269-299: maximal digit runs; every
+    // non-digit closes a number (0 when no digit preceded it); alternate vt, et.
+    vts.clear();
+    ets.clear();
+    if (!s) return RMCM_EINVAL;
+    const size_t L = strlen(s);
+    if (L == 0) return RMCM_EPARSE;
+    int64_t num = 0;
+    int i = 0;
+    for (size_t q = 0; q < L; q++) {
+        const char ch = s[q];
+        if (ch >= '0' && ch <= '9') {
+            num = num * 10 + (ch - '0');
+            if (num > 1000000000) return RMCM_EPARSE;
+        } else {
+            (i % 2 == 0 ? vts : ets).push_back((int32_t)num);
+            num = 0;
+            i++;
+        }
+    }
+    if (s[L - 1] >= '0' && s[L - 1] <= '9') {
+        (i % 2 == 0 ? vts : ets).push_back((int32_t)num);
+        i++;
+    }
+    if (vts.size() != ets.size() + 1) return RMCM_EPARSE;
+    return RMCM_OK;
+}
+
+double elapsed_s(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms / 1000.0;
+}
+
+int32_t copy_mat(rmcm_handle *h, const rmcm_mat *src, rmcm_mat **out) {
+    rmcm_mat *m = nullptr;
+    RMCM_TRY(mat_alloc(h, src->d.rows, src->d.cols, src->d.nnz, src->valtype, &m));
+    cudaStream_t s = h->stream;
+    cudaError_t e = cudaMemcpyAsync(m->d.rowptr, src->d.rowptr, 8 * (src->d.rows + 1), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && src->d.nnz)
+        e = cudaMemcpyAsync(m->d.col, src->d.col, 4 * src->d.nnz, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && src->d.nnz)
+        e = cudaMemcpyAsync(m->d.val, src->d.val, val_bytes(src->valtype) * src->d.nnz, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) {
+        mat_release(h, m);
+        return cuda_error(h, e, "copy");
+    }
+    *out = m;
+    return RMCM_OK;
+}
+
+// SSP_dynamic on device-resident matrices (see file comment).
+int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int32_t *fixed_pairs, rmcm_mat **Cout,
+                   rmcm_timings *t) {
+    rmcm_timings tm{};
+    *Cout = nullptr;
+    if (len < 1 || len > 16) return set_error(h, RMCM_EINVAL, "chain length must be 1..16");
+    for (int i = 0; i < len; i++) {
+        if (!mats[i]) return set_error(h, RMCM_EINVAL, "null matrix in chain");
+        if (mats[i]->valtype != mats[0]->valtype) return set_error(h, RMCM_EINVAL, "chain mixes value types");
+        if (i + 1 < len && mats[i]->d.cols != mats[i + 1]->d.rows)
+            return set_error(h, RMCM_EINVAL, "consecutive matrices do not chain");
+    }
+    cudaStream_t s = h->stream;
+    tm.valtype = mats[0]->valtype;
+    if (len == 1) {
+        // efficient/resmcm.cpp:670-677: the leaf itself is the result (no timed work)
+        RMCM_TRY(copy_mat(h, mats[0], Cout));
+        RMCM_CUDA(h, cudaStreamSynchronize(s));
+        tm.nnz = (*Cout)->d.nnz;
+        if (t) *t = tm;
+        return RMCM_OK;
+    }
+    cudaEvent_t *ev = h->ev;
+    RMCM_CUDA(h, cudaEventRecord(ev[0], s));
+    // (a) estimator
+    double *c_dev = nullptr;
+    char *ord = nullptr;
+    const int64_t ord_bytes = 8 * 256 + 4 * 256 + 4 * 64;
+    RMCM_TRY(dev_alloc(h, (void **)&c_dev, 8 * 256));
+    int32_t rc = estimate(h, mats, len, c_dev);
+    if (rc == RMCM_OK) rc = dev_alloc(h, (void **)&ord, ord_bytes);
+    if (rc != RMCM_OK) {
+        dev_free(h, c_dev, 8 * 256);
+        return rc;
+    }
+    cudaEventRecord(ev[1], s);
+    // (b) DP + order
+    int32_t *pairs_dev = (int32_t *)(ord + 8 * 256 + 4 * 256);
+    rc = chain_order_dev(h, c_dev, len, (int32_t *)(ord + 8 * 256), (double *)ord, pairs_dev);
+    cudaEventRecord(ev[2], s);
+    int32_t pairs[32];
+    if (rc == RMCM_OK) {
+        if (fixed_pairs) {
+            memcpy(pairs, fixed_pairs, sizeof(int32_t) * 2 * (len - 1));
+        } else {
+            cudaError_t e = cudaMemcpyAsync(h->h_pinned, pairs_dev, sizeof(int32_t) * 2 * (len - 1), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) rc = cuda_error(h, e, "order download");
+            else memcpy(pairs, h->h_pinned, sizeof(int32_t) * 2 * (len - 1));
+        }
+    }
+    dev_free(h, ord, ord_bytes);
+    dev_free(h, c_dev, 8 * 256);
+    if (rc != RMCM_OK) return rc;
+    // validate the pair list against the stack machine before running it
+    {
+        int depth = 0;
+        std::vector<char> used(len, 0);
+        for (int p = 0; p < len - 1; p++) {
+            const int k = pairs[2 * p], l = pairs[2 * p + 1];
+            const int need = (k < 0) + (l < 0);
+            if ((k >= 0 && (k >= len || used[k])) || (l >= 0 && (l >= len || used[l])) || k < -1 || l < -1 || depth < need)
+                return set_error(h, RMCM_EINVAL, "invalid chain order pair list");
+            if (k >= 0) used[k] = 1;
+            if (l >= 0) used[l] = 1;
+            depth += 1 - need;
+        }
+        if (depth != 1) return set_error(h, RMCM_EINVAL, "invalid chain order pair list");
+    }
+    // (c) executor, efficient/resmcm.cpp:709-760
+    std::vector<rmcm_mat *> stack;
+    double spgemm_s = 0;
+    for (int p = 0; p < len - 1 && rc == RMCM_OK; p++) {
+        const int k = pairs[2 * p], l = pairs[2 * p + 1];
+        const int sz = (int)stack.size();
+        const rmcm_mat *A, *B;
+        if (k >= 0 && l >= 0) { A = mats[k]; B = mats[l]; }
+        else if (k == -1 && l >= 0) { A = stack[sz - 1]; B = mats[l]; }
+        else if (k >= 0 && l == -1) { A = mats[k]; B = stack[sz - 1]; }
+        else { A = stack[sz - 2]; B = stack[sz - 1]; }
+        cudaEventRecord(ev[3], s);
+        rmcm_mat *C = nullptr;
+        int64_t fl = 0;
+        rc = spgemm(h, A, B, &C, &fl);
+        tm.flops += fl;
+        cudaEventRecord(ev[4], s);
+        if (rc != RMCM_OK) break;
+        cudaEventSynchronize(ev[4]);
+        spgemm_s += elapsed_s(ev[3], ev[4]);
+        tm.n_products++;
+        if (k >= 0 && l >= 0) {
+            stack.push_back(C);
+        } else if (k == -1 && l >= 0) {
+            mat_release(h, stack[sz - 1]);
+            stack[sz - 1] = C;
+        } else if (k >= 0 && l == -1) {
+            mat_release(h, stack[sz - 1]);
+            stack[sz - 1] = C;
+        } else {
+            mat_release(h, stack[sz - 1]);
+            mat_release(h, stack[sz - 2]);
+            stack.pop_back();
+            stack[sz - 2] = C;
+        }
+    }
+    if (rc != RMCM_OK) {
+        for (auto *m : stack) mat_release(h, m);
+        return rc;
+    }
+    cudaEventRecord(ev[5], s);
+    RMCM_CUDA(h, cudaEventSynchronize(ev[5]));
+    tm.es_s = elapsed_s(ev[0], ev[1]);
+    tm.dp_s = elapsed_s(ev[1], ev[2]);
+    tm.spgemm_s = spgemm_s;
+    tm.total_s = elapsed_s(ev[0], ev[5]);
+    *Cout = stack[0];
+    tm.nnz = stack[0]->d.nnz;
+    rc = check_status(h);
+    if (t) *t = tm;
+    return rc;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+extern "C" {
+
+RMCM_API const char *rmcm_status_string(int32_t status) {
+    switch (status) {
+        case RMCM_OK: return "ok";
+        case RMCM_EINVAL: return "invalid argument";
+        case RMCM_ENOMEM: return "out of device memory budget";
+        case RMCM_EOVERFLOW: return "path count overflow";
+        case RMCM_ETIMEOUT: return "device wait timed out";
+        case RMCM_ECUDA: return "CUDA error";
+        case RMCM_EIO: return "I/O error";
+        case RMCM_EPARSE: return "parse error";
+        case RMCM_EINTERNAL: return "internal invariant violated";
+        default: return "unknown status";
+    }
+}
+
+RMCM_API int32_t rmcm_create(rmcm_handle **out, const rmcm_opts *opts) {
+    if (!out) return RMCM_EINVAL;
+    *out = nullptr;
+    rmcm_handle *h = new rmcm_handle();
+    rmcm_opts o{};
+    o.valtype = RMCM_VAL_AUTO;
+    if (opts) o = *opts;
+    h->device = o.device;
+    h->valtype = o.valtype;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0 || o.device < 0 || o.device >= ndev) {
+        cudaGetLastError();
+        delete h;
+        return RMCM_ECUDA;
+    }
+    e = cudaSetDevice(o.device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, o.device);
+    if (e == cudaSuccess) {
+        if (o.stream) h->stream = (cudaStream_t)o.stream;
+        else {
+            e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+            h->own_stream = true;
+        }
+    }
+    for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&h->ev[i]);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_status, sizeof(int) * kNumStatus);
+    if (e == cudaSuccess) e = cudaMemset(h->d_status, 0, sizeof(int) * kNumStatus);
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&h->h_status, sizeof(int) * kNumStatus);
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&h->h_pinned, sizeof(int64_t) * 64);
+    size_t free_b = 0, total_b = 0;
+    if (e == cudaSuccess) e = cudaMemGetInfo(&free_b, &total_b);
+    if (e == cudaSuccess) {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, o.device) == cudaSuccess) {
+            uint64_t thr = ~0ull;   // keep freed blocks cached in the pool
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        rmcm_destroy(h);
+        return RMCM_ECUDA;
+    }
+    h->budget = o.mem_budget_bytes > 0 ? o.mem_budget_bytes : (int64_t)(0.9 * (double)free_b);
+    *out = h;
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_destroy(rmcm_handle *h) {
+    if (!h) return RMCM_OK;
+    for (auto &r : h->prof)
+        for (auto &e : r.ev)
+            if (e) cudaEventDestroy(e);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->scratch) dev_free(h, h->scratch, h->scratch_bytes);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->d_status) cudaFree(h->d_status);
+    if (h->h_status) cudaFreeHost(h->h_status);
+    if (h->h_pinned) cudaFreeHost(h->h_pinned);
+    for (auto &e : h->ev)
+        if (e) cudaEventDestroy(e);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return RMCM_OK;
+}
+
+RMCM_API const char *rmcm_last_error(const rmcm_handle *h) { return h ? h->last_error.c_str() : ""; }
+
+RMCM_API int32_t rmcm_set_stream(rmcm_handle *h, void *stream) {
+    if (!h) return RMCM_EINVAL;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    h->own_stream = false;
+    h->stream = (cudaStream_t)stream;
+    return RMCM_OK;
+}
+
+RMCM_API void *rmcm_get_stream(const rmcm_handle *h) { return h ? (void *)h->stream : nullptr; }
+RMCM_API int64_t rmcm_mem_in_use(const rmcm_handle *h) { return h ? h->in_use : 0; }
+RMCM_API int64_t rmcm_kernel_launches(const rmcm_handle *h) { return h ? h->launches : 0; }
+
+RMCM_API int32_t rmcm_set_profiling(rmcm_handle *h, int32_t level) {
+    if (!h || level < 0 || level > 2) return RMCM_EINVAL;
+    h->prof_level = level;
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_get_product_stats(rmcm_handle *h, rmcm_product_stats *out, int32_t cap, int32_t *count,
+                                        int32_t reset) {
+    if (!h) return RMCM_EINVAL;
+    RMCM_CUDA(h, cudaStreamSynchronize(h->stream));
+    const int32_t n = (int32_t)h->prof.size();
+    if (count) *count = n;
+    for (int32_t i = 0; i < n && out && i < cap; i++) {
+        rmcm::ProdRecord &r = h->prof[i];
+        float a = 0, b = 0, c = 0;
+        cudaEventElapsedTime(&a, r.ev[0], r.ev[1]);
+        cudaEventElapsedTime(&b, r.ev[2], r.ev[3]);
+        cudaEventElapsedTime(&c, r.ev[4], r.ev[5]);
+        r.st.analyze_ms = a;
+        r.st.symbolic_ms = b;
+        r.st.numeric_ms = c;
+        out[i] = r.st;
+    }
+    if (reset) {
+        for (auto &r : h->prof)
+            for (auto &e : r.ev)
+                if (e) cudaEventDestroy(e);
+        h->prof.clear();
+    }
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_graph_load_text(rmcm_handle *h, const char *graph_file, const char *vertex_file,
+                                      const char *edge_file, rmcm_graph **out) {
+    if (!h || !out || !graph_file || !vertex_file || !edge_file) return RMCM_EINVAL;
+    *out = nullptr;
+    rmcm_graph *g = new rmcm_graph();
+    g->h = h;
+    int32_t rc = load_text(h, graph_file, vertex_file, edge_file, g);
+    if (rc != RMCM_OK) {
+        delete g;
+        return rc;
+    }
+    *out = g;
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_graph_from_adjacency(rmcm_handle *h, int64_t n, const int32_t *vtype, const int64_t *adj_ptr,
+                                           const int32_t *adj_nbr, const int32_t *adj_et, rmcm_graph **out) {
+    if (!h || !out || n < 0 || (n > 0 && (!vtype || !adj_ptr))) return set_error(h, RMCM_EINVAL, "graph: bad arguments");
+    *out = nullptr;
+    const int64_t m = n > 0 ? adj_ptr[n] : 0;
+    if (m > 0 && (!adj_nbr || !adj_et)) return set_error(h, RMCM_EINVAL, "graph: missing adjacency arrays");
+    rmcm_graph *g = new rmcm_graph();
+    g->h = h;
+    g->n = n;
+    g->m = m;
+    g->vtype.assign(vtype, vtype + n);
+    g->adj_ptr.assign(adj_ptr, adj_ptr + n + 1);
+    g->adj_nbr.assign(adj_nbr, adj_nbr + m);
+    g->adj_et.assign(adj_et, adj_et + m);
+    g->max_vt = 0;
+    bool ok = adj_ptr[0] == 0;
+    for (int64_t v = 0; v < n && ok; v++) {
+        ok = vtype[v] >= 0 && vtype[v] <= 1000000 && adj_ptr[v + 1] >= adj_ptr[v];
+        g->max_vt = std::max(g->max_vt, vtype[v]);
+    }
+    for (int64_t q = 0; q < m && ok; q++) ok = adj_nbr[q] >= 0 && adj_nbr[q] < n;
+    if (!ok) {
+        delete g;
+        return set_error(h, RMCM_EINVAL, "graph: vertex type, row pointer or neighbour id out of range");
+    }
+    graph_finish(g);
+    *out = g;
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_graph_free(rmcm_graph *g) {
+    if (!g) return RMCM_OK;
+    for (auto &kv : g->leaves) mat_release(g->h, kv.second);
+    if (g->h && g->h->stream) cudaStreamSynchronize(g->h->stream);
+    delete g;
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_graph_info(const rmcm_graph *g, int64_t *n, int64_t *m, int32_t *max_vt) {
+    if (!g) return RMCM_EINVAL;
+    if (n) *n = g->n;
+    if (m) *m = g->m;
+    if (max_vt) *max_vt = g->max_vt;
+    return RMCM_OK;
+}
+
+RMCM_API int64_t rmcm_graph_dim(const rmcm_graph *g, int32_t vt) {
+    if (!g || vt < 0 || vt > g->max_vt) return 0;
+    return g->dims[vt];
+}
+
+RMCM_API int32_t rmcm_metapath_parse(const char *s, int32_t *vts, int32_t *ets, int32_t cap, int32_t *len) {
+    std::vector<int32_t> v, e;
+    int32_t rc = parse_path(s, v, e);
+    if (rc != RMCM_OK) return rc;
+    if ((int64_t)e.size() > cap) return RMCM_EINVAL;
+    if (vts) std::copy(v.begin(), v.end(), vts);
+    if (ets) std::copy(e.begin(), e.end(), ets);
+    if (len) *len = (int32_t)e.size();
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_metapath_format(const int32_t *vts, const int32_t *ets, int32_t len, char *buf, int64_t cap) {
+    // MetaPath::toString, efficient/resmcm.cpp:301-308
+    if (!vts || (len > 0 && !ets) || len < 0 || !buf || cap <= 0) return RMCM_EINVAL;
+    std::string str;
+    for (int i = 0; i < len; i++) str += std::to_string(vts[i]) + "-" + std::to_string(ets[i]) + "-";
+    str += std::to_string(vts[len]);
+    if ((int64_t)str.size() + 1 > cap) return RMCM_EINVAL;
+    memcpy(buf, str.c_str(), str.size() + 1);
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_leaf(rmcm_handle *h, rmcm_graph *g, int32_t src_vt, int32_t sink_vt, int32_t et,
+                           int32_t valtype, rmcm_mat **out) {
+    if (!h || !g || !out || (valtype != RMCM_VAL_U32 && valtype != RMCM_VAL_U64)) return RMCM_EINVAL;
+    return get_leaf(h, g, src_vt, sink_vt, et, valtype, out);
+}
+
+RMCM_API int32_t rmcm_mat_upload(rmcm_handle *h, int64_t rows, int64_t cols, const int64_t *rowptr,
+                                 const int32_t *col, const void *val, int32_t valtype, rmcm_mat **out) {
+    if (!h || !out || rows < 0 || cols < 0 || cols > INT32_MAX || !rowptr || (valtype != RMCM_VAL_U32 && valtype != RMCM_VAL_U64))
+        return set_error(h, RMCM_EINVAL, "upload: bad arguments");
+    *out = nullptr;
+    const int64_t nnz = rowptr[rows];
+    if (rowptr[0] != 0 || nnz < 0 || (nnz > 0 && !col)) return set_error(h, RMCM_EINVAL, "upload: bad row pointer");
+    // validate (rows ascending, columns in range); sort rows that are not ascending
+    int bad = 0, unsorted = 0;
+#pragma omp parallel for schedule(dynamic, 4096) reduction(| : bad, unsorted)
+    for (int64_t r = 0; r < rows; r++) {
+        const int64_t a = rowptr[r], b = rowptr[r + 1];
+        if (b < a || b > nnz) { bad = 1; continue; }
+        for (int64_t q = a; q < b; q++) {
+            if (col[q] < 0 || col[q] >= cols) bad = 1;
+            if (q > a && col[q] < col[q - 1]) unsorted = 1;
+        }
+    }
+    if (bad) return set_error(h, RMCM_EINVAL, "upload: row pointer not monotone or column out of range");
+    if (!unsorted) return upload_csr(h, rows, cols, rowptr, col, val, valtype, out);
+    std::vector<int32_t> c2(col, col + nnz);
+    std::vector<char> v2;
+    const int64_t vb = val_bytes(valtype);
+    if (val) v2.assign((const char *)val, (const char *)val + vb * nnz);
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t r = 0; r < rows; r++) {
+        const int64_t a = rowptr[r], b = rowptr[r + 1];
+        std::vector<int64_t> idx(b - a);
+        for (int64_t q = 0; q < b - a; q++) idx[q] = a + q;
+        std::stable_sort(idx.begin(), idx.end(), [&](int64_t x, int64_t y) { return col[x] < col[y]; });
+        for (int64_t q = 0; q < b - a; q++) {
+            c2[a + q] = col[idx[q]];
+            if (val) memcpy(&v2[(a + q) * vb], (const char *)val + idx[q] * vb, vb);
+        }
+    }
+    return upload_csr(h, rows, cols, rowptr, c2.data(), val ? v2.data() : nullptr, valtype, out);
+}
+
+RMCM_API int32_t rmcm_mat_info(const rmcm_mat *m, int64_t *rows, int64_t *cols, int64_t *nnz, int32_t *valtype) {
+    if (!m) return RMCM_EINVAL;
+    if (rows) *rows = m->d.rows;
+    if (cols) *cols = m->d.cols;
+    if (nnz) *nnz = m->d.nnz;
+    if (valtype) *valtype = m->valtype;
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_mat_download(rmcm_handle *h, const rmcm_mat *m, int64_t *rowptr, int32_t *col, void *val) {
+    if (!h || !m) return RMCM_EINVAL;
+    cudaStream_t s = h->stream;
+    if (rowptr) RMCM_CUDA(h, cudaMemcpyAsync(rowptr, m->d.rowptr, 8 * (m->d.rows + 1), cudaMemcpyDeviceToHost, s));
+    if (col && m->d.nnz) RMCM_CUDA(h, cudaMemcpyAsync(col, m->d.col, 4 * m->d.nnz, cudaMemcpyDeviceToHost, s));
+    if (val && m->d.nnz)
+        RMCM_CUDA(h, cudaMemcpyAsync(val, m->d.val, val_bytes(m->valtype) * m->d.nnz, cudaMemcpyDeviceToHost, s));
+    RMCM_CUDA(h, cudaStreamSynchronize(s));
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_mat_free(rmcm_handle *h, rmcm_mat *m) {
+    if (!h || !m) return RMCM_EINVAL;
+    if (m->graph_owned) return set_error(h, RMCM_EINVAL, "leaf matrices are owned by their graph");
+    mat_release(h, m);
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_estimate(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, double *c_out) {
+    if (!h || !chain || !c_out) return RMCM_EINVAL;
+    double *c_dev = nullptr;
+    RMCM_TRY(dev_alloc(h, (void **)&c_dev, 8 * 256));
+    int32_t rc = estimate(h, chain, len, c_dev);
+    if (rc == RMCM_OK) {
+        cudaError_t e = cudaMemcpyAsync(c_out, c_dev, sizeof(double) * len * len, cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) rc = cuda_error(h, e, "estimate download");
+    }
+    dev_free(h, c_dev, 8 * 256);
+    return rc;
+}
+
+RMCM_API int32_t rmcm_order(rmcm_handle *h, const double *c, int32_t len, int32_t *split, double *cost,
+                            int32_t *pairs) {
+    if (!h || !c || len < 1 || len > 16) return set_error(h, RMCM_EINVAL, "order: bad arguments");
+    char *buf = nullptr;
+    const int64_t bytes = 8 * 256 + 4 * 256 + 8 * 256 + 4 * 64;
+    RMCM_TRY(dev_alloc(h, (void **)&buf, bytes));
+    double *c_dev = (double *)buf;
+    int32_t *s_dev = (int32_t *)(buf + 8 * 256);
+    double *m_dev = (double *)(buf + 8 * 256 + 4 * 256);
+    int32_t *p_dev = (int32_t *)(buf + 8 * 256 + 4 * 256 + 8 * 256);
+    cudaStream_t s = h->stream;
+    int32_t rc = RMCM_OK;
+    cudaError_t e = cudaMemcpyAsync(c_dev, c, sizeof(double) * len * len, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) rc = cuda_error(h, e, "order upload");
+    if (rc == RMCM_OK) rc = chain_order_dev(h, c_dev, len, s_dev, m_dev, p_dev);
+    if (rc == RMCM_OK) {
+        e = cudaSuccess;
+        if (split) e = cudaMemcpyAsync(split, s_dev, 4 * len * len, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && cost) e = cudaMemcpyAsync(cost, m_dev, 8 * len * len, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && pairs && len > 1) e = cudaMemcpyAsync(pairs, p_dev, 4 * 2 * (len - 1), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = cuda_error(h, e, "order download");
+    }
+    dev_free(h, buf, bytes);
+    return rc;
+}
+
+RMCM_API int32_t rmcm_spgemm(rmcm_handle *h, const rmcm_mat *A, const rmcm_mat *B, rmcm_mat **C) {
+    if (!h || !C) return RMCM_EINVAL;
+    *C = nullptr;
+    int32_t rc = spgemm(h, A, B, C, nullptr);
+    if (rc != RMCM_OK) return rc;
+    rc = check_status(h);
+    if (rc != RMCM_OK && rc != RMCM_EOVERFLOW) {
+        mat_release(h, *C);
+        *C = nullptr;
+    }
+    return rc;
+}
+
+RMCM_API int32_t rmcm_chain(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, const int32_t *pairs,
+                            rmcm_mat **C, rmcm_timings *t) {
+    if (!h || !chain || !C) return RMCM_EINVAL;
+    int32_t rc = chain_exec(h, chain, len, pairs, C, t);
+    if (rc != RMCM_OK && rc != RMCM_EOVERFLOW && *C) {
+        mat_release(h, *C);
+        *C = nullptr;
+    }
+    return rc;
+}
+
+RMCM_API int32_t rmcm_run_metapath(rmcm_handle *h, rmcm_graph *g, const char *metapath, rmcm_mat **C,
+                                   rmcm_timings *t) {
+    if (!h || !g || !metapath) return RMCM_EINVAL;
+    if (C) *C = nullptr;
+    std::vector<int32_t> vts, ets;
+    if (parse_path(metapath, vts, ets) != RMCM_OK)
+        return set_error(h, RMCM_EINVAL, std::string("the meta-path is incorrect: ") + metapath);
+    const int len = (int)ets.size();
+    if (len < 1 || len > 16) return set_error(h, RMCM_EINVAL, "meta-path must have 1..16 edge types");
+    int32_t vt_try[2] = {h->valtype == RMCM_VAL_U64 ? RMCM_VAL_U64 : RMCM_VAL_U32, RMCM_VAL_U64};
+    const int tries = h->valtype == RMCM_VAL_AUTO ? 2 : 1;
+    int32_t rc = RMCM_OK;
+    for (int attempt = 0; attempt < tries; attempt++) {
+        std::vector<rmcm_mat *> mats(len);
+        for (int i = 0; i < len; i++) RMCM_TRY(get_leaf(h, g, vts[i], vts[i + 1], ets[i], vt_try[attempt], &mats[i]));
+        rmcm_mat *res = nullptr;
+        rc = chain_exec(h, mats.data(), len, nullptr, &res, t);
+        if (rc == RMCM_EOVERFLOW && attempt + 1 < tries) {
+            mat_release(h, res);
+            continue;
+        }
+        if (res && (rc == RMCM_OK || rc == RMCM_EOVERFLOW)) {
+            if (C) *C = res;
+            else mat_release(h, res);
+        } else if (res) {
+            mat_release(h, res);
+        }
+        break;
+    }
+    return rc;
+}
+
+RMCM_API int32_t rmcm_estimate_metapath(rmcm_handle *h, rmcm_graph *g, const char *metapath, double *est_nnz) {
+    if (!h || !g || !metapath || !est_nnz) return RMCM_EINVAL;
+    std::vector<int32_t> vts, ets;
+    if (parse_path(metapath, vts, ets) != RMCM_OK)
+        return set_error(h, RMCM_EINVAL, std::string("the meta-path is incorrect: ") + metapath);
+    const int len = (int)ets.size();
+    if (len < 1 || len > 16) return set_error(h, RMCM_EINVAL, "meta-path must have 1..16 edge types");
+    std::vector<rmcm_mat *> mats(len);
+    for (int i = 0; i < len; i++) RMCM_TRY(get_leaf(h, g, vts[i], vts[i + 1], ets[i], RMCM_VAL_U32, &mats[i]));
+    std::vector<double> c(len * len, 0.0);
+    RMCM_TRY(rmcm_estimate(h, mats.data(), len, c.data()));
+    *est_nnz = c[len - 1];   // c_[len - 1] = c[0][len-1], accuracy/res.cpp:522
+    return RMCM_OK;
+}
+
+}  // extern "C"

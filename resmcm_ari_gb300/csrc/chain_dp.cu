@@ -1,0 +1,136 @@
+// Chain-order dynamic program as a single warp (sm_103a).
+//
+// Replaces the DP of DynamicOptimizer::rows_sparse_optimal_matrix_chain_order
+// (efficient/resmcm.cpp:519-536) and get_optimal_chain_order (:563-573):
+//   m[i][j] = min_k  m[i][k] + m[k+1][j] + (c[i][k] + c[k+1][j] + c[i][j])
+// with c[i][i] = 0 and m[i][i] = 0, the smallest k winning ties (the
+// reference's strict '<' while k ascends).  Both sums are evaluated in the
+// reference's left-to-right order with explicit round-to-nearest adds, so the
+// same c gives the same split table bit for bit.
+// Lane i owns the interval [i, i+l] of each length l; the lengths advance in
+// lock step (__syncwarp between them).  Lane 0 then walks the split table in
+// post-order with an explicit stack and emits the (k, l) pair list, -1
+// standing for "the top of the temporary stack".
+// One warp per chain: `nchains` chains are ordered by one launch.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+
+#include "internal.h"
+
+namespace rmcm {
+namespace {
+
+constexpr int kMaxLen = 16;
+
+__global__ void __launch_bounds__(32) k_chain_dp(const double *c_all, const int32_t *lens, int32_t nchains,
+                                                 int32_t *split_all, double *cost_all, int32_t *pairs_all) {
+    const int chain = blockIdx.x;
+    if (chain >= nchains) return;
+    const int lane = threadIdx.x;
+    const int len = lens[chain];
+    const double *c = c_all + (int64_t)chain * kMaxLen * kMaxLen;
+    __shared__ double sc[kMaxLen * kMaxLen];
+    __shared__ double sm[kMaxLen * kMaxLen];
+    __shared__ int32_t ss[kMaxLen * kMaxLen];
+    for (int q = lane; q < kMaxLen * kMaxLen; q += 32) {
+        const int i = q / kMaxLen, j = q % kMaxLen;
+        sc[q] = (i < len && j < len && i != j) ? c[i * len + j] : 0.0;
+        sm[q] = 0.0;
+        ss[q] = 0;
+    }
+    __syncwarp();
+    for (int l = 1; l < len; l++) {
+        const int i = lane;
+        if (i < len - l) {
+            const int j = i + l;
+            double best = DBL_MAX;
+            int bk = 0;
+            for (int k = i; k < j; k++) {
+                const double tmp = __dadd_rn(__dadd_rn(sc[i * kMaxLen + k], sc[(k + 1) * kMaxLen + j]), sc[i * kMaxLen + j]);
+                const double cost = __dadd_rn(__dadd_rn(sm[i * kMaxLen + k], sm[(k + 1) * kMaxLen + j]), tmp);
+                if (cost < best) {
+                    best = cost;
+                    bk = k;
+                }
+            }
+            sm[i * kMaxLen + j] = best;
+            ss[i * kMaxLen + j] = bk;
+        }
+        __syncwarp();
+    }
+    int32_t *split = split_all + (int64_t)chain * kMaxLen * kMaxLen;
+    double *cost = cost_all + (int64_t)chain * kMaxLen * kMaxLen;
+    for (int q = lane; q < len * len; q += 32) {
+        const int i = q / len, j = q % len;
+        split[q] = ss[i * kMaxLen + j];
+        cost[q] = sm[i * kMaxLen + j];
+    }
+    if (lane == 0 && len > 1) {
+        // iterative post-order over the split tree
+        int32_t *pairs = pairs_all + (int64_t)chain * 2 * kMaxLen;
+        int st_i[2 * kMaxLen], st_j[2 * kMaxLen], st_state[2 * kMaxLen], st_left[2 * kMaxLen];
+        int sp = 0, np = 0, ret = 0;
+        st_i[0] = 0; st_j[0] = len - 1; st_state[0] = 0; sp = 1;
+        while (sp > 0) {
+            const int t = sp - 1;
+            const int i = st_i[t], j = st_j[t];
+            if (i == j) { ret = i; sp--; continue; }
+            const int k = ss[i * kMaxLen + j];
+            if (st_state[t] == 0) {
+                st_state[t] = 1;
+                st_i[sp] = i; st_j[sp] = k; st_state[sp] = 0; sp++;
+            } else if (st_state[t] == 1) {
+                st_left[t] = ret;
+                st_state[t] = 2;
+                st_i[sp] = k + 1; st_j[sp] = j; st_state[sp] = 0; sp++;
+            } else {
+                pairs[2 * np] = st_left[t];
+                pairs[2 * np + 1] = ret;
+                np++;
+                ret = -1;
+                sp--;
+            }
+        }
+    }
+}
+
+}  // namespace
+
+int32_t chain_order_dev(rmcm_handle *h, const double *c_dev, int32_t len, int32_t *split_dev, double *cost_dev,
+                        int32_t *pairs_dev) {
+    // single-chain form: c_dev is len*len; stage it into the 16x16 batched layout
+    if (len < 1 || len > kMaxLen) return set_error(h, RMCM_EINVAL, "order: chain length must be 1..16");
+    cudaStream_t s = h->stream;
+    const int64_t cbytes = sizeof(double) * kMaxLen * kMaxLen;
+    char *buf = nullptr;
+    const int64_t total = cbytes + 256 + 4 * kMaxLen * kMaxLen + cbytes + 4 * 2 * kMaxLen;
+    RMCM_TRY(dev_alloc(h, (void **)&buf, total + 1024));
+    double *c16 = (double *)buf;
+    int32_t *lens = (int32_t *)(buf + cbytes);
+    int32_t *sp16 = (int32_t *)(buf + cbytes + 256);
+    double *cost16 = (double *)(buf + cbytes + 256 + 4 * kMaxLen * kMaxLen);
+    int32_t *pairs16 = (int32_t *)((char *)cost16 + cbytes);
+    cudaError_t e = cudaMemcpyAsync(c16, c_dev, sizeof(double) * len * len, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) {
+        int32_t L = len;
+        e = cudaMemcpyAsync(lens, &L, sizeof(int32_t), cudaMemcpyHostToDevice, s);
+    }
+    if (e == cudaSuccess) {
+        k_chain_dp<<<1, 32, 0, s>>>(c16, lens, 1, sp16, cost16, pairs16);
+        h->launches++;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && split_dev)
+        e = cudaMemcpyAsync(split_dev, sp16, sizeof(int32_t) * len * len, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && cost_dev)
+        e = cudaMemcpyAsync(cost_dev, cost16, sizeof(double) * len * len, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && pairs_dev && len > 1)
+        e = cudaMemcpyAsync(pairs_dev, pairs16, sizeof(int32_t) * 2 * (len - 1), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);   // host value of L must outlive the copy
+    dev_free(h, buf, total + 1024);
+    if (e != cudaSuccess) return cuda_error(h, e, "chain order");
+    return RMCM_OK;
+}
+
+}  // namespace rmcm

@@ -1,0 +1,161 @@
+// RES row-wise sparsity estimator (sm_103a, FP64).
+//
+// Replaces the estimator loop of DynamicOptimizer::rows_sparse_optimal_matrix_chain_order
+// (efficient/resmcm.cpp:506-517), getSparsities (:442-452) and
+// compute_sparsities (:468-485):
+//   r_ii[u] = min(1, |M_i[u]| / dim(vts[i+1]))
+//   r_ij[u] = 1 - prod_{v in M_i[u]} (1 - r_{i+1,j}[v])          (j > i)
+//   c_ij    = sum_u r_ij[u] * dim(vts[j+1])
+// for i = len-1 .. 0.  dim(vts[j+1]) is the column count of M_j.
+//
+// One launch per level i computes every j > i at once, so each M_i is read
+// once: the sparsities of a level are stored row-major as r[v * len + j], and
+// a row's gathers for all j are one contiguous run of doubles.
+// Mapping: a warp per row; the warp is split into G groups of JP lanes
+// (JP = next power of two >= number of j), lane (g, j) multiplies the factors
+// of entries g, g+G, ... for target j, and the G partial products are
+// combined with shuffles in a fixed order.  Sums of c_ij are per-warp, then
+// per-block (fixed warp order), then a one-block pass over the block partials
+// (fixed order): the estimate is bit-for-bit reproducible run to run.
+// Every multiply and add is an explicit round-to-nearest intrinsic, so no
+// fused multiply-add changes the rounding against the reference's
+// `tmp_rho *= (1 - r)` and `nnz += s * dim`.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "internal.h"
+
+namespace rmcm {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kEstThreads = 256;
+constexpr int kMaxLen = 16;
+
+struct LevelArgs {
+    int32_t len;            // chain length (matrices)
+    int32_t i;              // level
+    int32_t nj;             // number of j > i (len - 1 - i)
+    int32_t jp;             // lanes per group (power of two >= nj, >= 1)
+    double dim_leaf;        // dim(vts[i+1]) = cols of M_i
+    double dims[kMaxLen];   // dims[j] = cols of M_j
+};
+
+__global__ void __launch_bounds__(kEstThreads) k_res_level(DevCsr M, const double *r_next, double *r_cur,
+                                                           LevelArgs la, double *partial) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int G = 32 / la.jp;
+    const int g = lane / la.jp;
+    const int jo = lane % la.jp;                 // offset of j above i+1
+    const bool active_j = jo < la.nj && g < G;
+    const int j = la.i + 1 + jo;
+    const double dimj = active_j ? la.dims[j] : 0.0;
+    double term_sum = 0.0;                       // held by group-0 lanes
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < M.rows; u += nwarps) {
+        const int64_t a0 = M.rowptr[u], a1 = M.rowptr[u + 1];
+        if (lane == 0) {
+            const double s = __ddiv_rn((double)(a1 - a0), la.dim_leaf);
+            r_cur[u * la.len + la.i] = s > 1.0 ? 1.0 : s;
+        }
+        if (la.nj == 0) continue;
+        double prod = 1.0;
+        if (active_j) {
+            for (int64_t k = a0 + g; k < a1; k += G) {
+                const int32_t v = M.col[k];
+                const double rv = r_next[(int64_t)v * la.len + j];
+                prod = __dmul_rn(prod, __dsub_rn(1.0, rv));
+            }
+        }
+        // combine the G group products (fixed butterfly order)
+        for (int d = la.jp; d < 32; d <<= 1) {
+            const double o = __shfl_xor_sync(kFull, prod, d);
+            prod = __dmul_rn(prod, o);
+        }
+        if (g == 0 && active_j) {
+            const double s = __dsub_rn(1.0, prod);
+            r_cur[u * la.len + j] = s;
+            term_sum = __dadd_rn(term_sum, __dmul_rn(s, dimj));
+        }
+    }
+    // block partials: partial[block * len + j]
+    __shared__ double s_part[kEstThreads / 32][kMaxLen];
+    if (g == 0 && active_j) s_part[warp][jo] = term_sum;
+    __syncthreads();
+    if (threadIdx.x < la.nj) {
+        double acc = 0.0;
+        for (int w = 0; w < kEstThreads / 32; w++) acc = __dadd_rn(acc, s_part[w][threadIdx.x]);
+        partial[(int64_t)blockIdx.x * kMaxLen + threadIdx.x] = acc;
+    }
+}
+
+// One block: c[i*len + j] = sum over blocks (fixed pairwise order).
+__global__ void __launch_bounds__(256) k_res_reduce(const double *partial, int32_t nblocks, LevelArgs la, double *c) {
+    __shared__ double s[256];
+    for (int jo = 0; jo < la.nj; jo++) {
+        double acc = 0.0;
+        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) acc = __dadd_rn(acc, partial[(int64_t)b * kMaxLen + jo]);
+        s[threadIdx.x] = acc;
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if ((int)threadIdx.x < w) s[threadIdx.x] = __dadd_rn(s[threadIdx.x], s[threadIdx.x + w]);
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) c[la.i * la.len + la.i + 1 + jo] = s[0];
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+int32_t estimate(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, double *c_dev) {
+    if (len < 1 || len > kMaxLen) return set_error(h, RMCM_EINVAL, "estimate: chain length must be 1..16");
+    cudaStream_t s = h->stream;
+    int64_t max_rows = 1;
+    for (int i = 0; i < len; i++) {
+        if (!chain[i]) return set_error(h, RMCM_EINVAL, "estimate: null matrix");
+        if (i + 1 < len && chain[i]->d.cols != chain[i + 1]->d.rows)
+            return set_error(h, RMCM_EINVAL, "estimate: consecutive matrices do not chain");
+        max_rows = std::max(max_rows, chain[i]->d.rows);
+    }
+    // grid is fixed by the row count only, so the reduction order is stable
+    const int64_t blocks_cap = (int64_t)h->sm_count * 8;
+    auto al = [](int64_t x) { return (x + 255) & ~255LL; };
+    const int64_t rbytes = al(8 * max_rows * len);
+    const int64_t pbytes = al(8 * blocks_cap * kMaxLen);
+    double *r_a = nullptr, *r_b = nullptr, *part = nullptr;
+    RMCM_TRY(dev_alloc(h, (void **)&r_a, 2 * rbytes + pbytes));
+    r_b = (double *)((char *)r_a + rbytes);
+    part = (double *)((char *)r_a + 2 * rbytes);
+    cudaError_t e = cudaMemsetAsync(c_dev, 0, sizeof(double) * len * len, s);
+    double *r_cur = r_a, *r_next = r_b;
+    for (int i = len - 1; i >= 0 && e == cudaSuccess; i--) {
+        const DevCsr &M = chain[i]->d;
+        LevelArgs la{};
+        la.len = len;
+        la.i = i;
+        la.nj = len - 1 - i;
+        int jp = 1;
+        while (jp < la.nj) jp <<= 1;
+        la.jp = jp;
+        la.dim_leaf = (double)M.cols;
+        for (int j = 0; j < len; j++) la.dims[j] = (double)chain[j]->d.cols;
+        int64_t blocks = (M.rows * 32 + kEstThreads - 1) / kEstThreads;
+        blocks = std::max<int64_t>(1, std::min(blocks, blocks_cap));
+        k_res_level<<<(unsigned)blocks, kEstThreads, 0, s>>>(M, r_next, r_cur, la, part);
+        h->launches++;
+        if (la.nj > 0) {
+            k_res_reduce<<<1, 256, 0, s>>>(part, (int32_t)blocks, la, c_dev);
+            h->launches++;
+        }
+        e = cudaGetLastError();
+        std::swap(r_cur, r_next);
+    }
+    dev_free(h, r_a, 2 * rbytes + pbytes);
+    if (e != cudaSuccess) return cuda_error(h, e, "estimator launch");
+    return RMCM_OK;
+}
+
+}  // namespace rmcm

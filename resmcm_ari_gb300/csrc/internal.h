@@ -1,0 +1,149 @@
+// Internal types shared by the host C++ and the CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "resmcm_gpu.h"
+
+struct rmcm_handle;
+struct rmcm_graph;
+struct rmcm_mat;
+
+namespace rmcm {
+
+// Device CSR descriptor: rowptr[rows+1] (int64), col[nnz] (int32, rows
+// ascending), val[nnz] (uint32 or uint64).  Passed to kernels by value.
+struct DevCsr {
+    int64_t rows = 0;
+    int64_t cols = 0;
+    int64_t nnz = 0;
+    int64_t *rowptr = nullptr;
+    int32_t *col = nullptr;
+    void *val = nullptr;
+};
+
+// Device-side status words, one int each (set with atomicOr, never cleared by kernels).
+enum StatusWord { kOverflow = 0, kInvariant = 1, kArena = 2, kTimeout = 3, kNumStatus = 8 };
+
+// Row bins of the SpGEMM (see spgemm.cu for the kernels that serve them).
+enum Bin {
+    kBinTiny = 0,      // flops <= 32: one warp per row, register bitonic sort
+    kBinHash512 = 1,   // shared-memory hash tables of 512 / 2048 / 8192 slots
+    kBinHash2k = 2,
+    kBinHash8k = 3,
+    kBinDense = 4,     // windowed dense accumulator (bitmap + counters) in shared memory
+    kNumBins = 5
+};
+
+// Tunables of the SpGEMM row binning (the autotuner searches these).
+struct Tuning {
+    int32_t tiny_max = 32;          // flops threshold of the warp-per-row bin (fixed by the kernel)
+    int32_t hash_max_flops = 4096;  // rows above go to the dense bin
+    int32_t dense_ratio = 16;       // dense when flops * dense_ratio >= cols (and one window covers cols)
+    int32_t dense_threads = 256;
+    double hash_load = 0.5;         // hash table load factor bound: slots >= min(f, cols) / load
+};
+
+// One profiled product: stats plus the six events that bracket its passes
+// (analyze, symbolic + scan, numeric).
+struct ProdRecord {
+    rmcm_product_stats st{};
+    cudaEvent_t ev[6] = {};
+};
+
+}  // namespace rmcm
+
+struct rmcm_mat {
+    rmcm::DevCsr d;
+    int32_t valtype = RMCM_VAL_U32;
+    bool graph_owned = false;
+    int64_t bytes = 0;
+};
+
+struct rmcm_handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int32_t valtype = RMCM_VAL_AUTO;
+    int64_t budget = 0;
+    int64_t in_use = 0;
+    int64_t launches = 0;
+    int sm_count = 0;
+    std::string last_error;
+    int *d_status = nullptr;        // kNumStatus ints
+    int *h_status = nullptr;        // pinned mirror
+    int64_t *h_pinned = nullptr;    // small pinned transfer area (64 int64)
+    // scratch (grown on demand, stream-ordered)
+    void *scratch = nullptr;
+    int64_t scratch_bytes = 0;
+    cudaEvent_t ev[8] = {};
+    rmcm::Tuning tune;
+    int32_t prof_level = 0;
+    std::vector<rmcm::ProdRecord> prof;
+};
+
+struct rmcm_graph {
+    rmcm_handle *h = nullptr;
+    int64_t n = 0, m = 0;
+    int32_t max_vt = 0;
+    std::vector<int32_t> vtype;
+    std::vector<int64_t> adj_ptr;
+    std::vector<int32_t> adj_nbr;
+    std::vector<int32_t> adj_et;
+    std::vector<int64_t> dims;       // per type
+    std::vector<int64_t> bin_ptr;    // per type, CSR over bin_ids
+    std::vector<int32_t> bin_ids;    // ascending global ids per type
+    std::vector<int32_t> local;      // global id -> local id
+    std::map<std::tuple<int32_t, int32_t, int32_t, int32_t>, rmcm_mat *> leaves;
+};
+
+namespace rmcm {
+
+// ---- error plumbing ------------------------------------------------------
+int32_t set_error(rmcm_handle *h, int32_t status, const std::string &msg);
+int32_t cuda_error(rmcm_handle *h, cudaError_t e, const char *what);
+
+#define RMCM_CUDA(h, call)                                       \
+    do {                                                         \
+        cudaError_t _e = (call);                                 \
+        if (_e != cudaSuccess) return rmcm::cuda_error((h), _e, #call); \
+    } while (0)
+
+#define RMCM_TRY(call)                      \
+    do {                                    \
+        int32_t _s = (call);                \
+        if (_s != RMCM_OK) return _s;       \
+    } while (0)
+
+// ---- device memory (stream ordered, budgeted) ----------------------------
+int32_t dev_alloc(rmcm_handle *h, void **p, int64_t bytes);
+void dev_free(rmcm_handle *h, void *p, int64_t bytes);
+// Grow the handle's scratch area to at least `bytes`.
+int32_t scratch_reserve(rmcm_handle *h, int64_t bytes);
+int32_t mat_alloc(rmcm_handle *h, int64_t rows, int64_t cols, int64_t nnz, int32_t valtype, rmcm_mat **out);
+void mat_release(rmcm_handle *h, rmcm_mat *m);
+// Read and clear the device status words; maps them to a status code.
+int32_t check_status(rmcm_handle *h);
+
+inline int64_t val_bytes(int32_t valtype) { return valtype == RMCM_VAL_U64 ? 8 : 4; }
+
+// ---- kernels (host launchers) --------------------------------------------
+// spgemm.cu
+int32_t spgemm(rmcm_handle *h, const rmcm_mat *A, const rmcm_mat *B, rmcm_mat **C, int64_t *flops_out);
+int32_t fill_ones(rmcm_handle *h, void *val, int64_t nnz, int32_t valtype);
+int32_t sort_rows(rmcm_handle *h, rmcm_mat *m);
+int32_t check_cols(rmcm_handle *h, const rmcm_mat *m);
+int32_t convert_values(rmcm_handle *h, const rmcm_mat *src, int32_t valtype, rmcm_mat **out);
+// estimator.cu: c_dev[len*len] on the device
+int32_t estimate(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, double *c_dev);
+// chain_dp.cu: split/cost/pairs on the device
+int32_t chain_order_dev(rmcm_handle *h, const double *c_dev, int32_t len, int32_t *split_dev, double *cost_dev,
+                        int32_t *pairs_dev);
+
+}  // namespace rmcm

@@ -1,0 +1,927 @@
+// Row-binned Gustavson SpGEMM with exact integer path counts (sm_103a).
+//
+// Replaces SpGEMM / row_wise_SpGEMM_based_on_bitmap of efficient/resmcm.cpp
+// (:586-647).  The reference's product is Boolean: for every row u of A it
+// walks B[a] for a in A[u], marks new columns in a per-thread n-byte bitmap
+// and appends them in discovery order.  Here every output row is computed
+// with its path counts (C[u][v] = sum_a A[u][a] * B[a][v]) and written with
+// ascending columns; its column SET is the reference's row.
+//
+// Pipeline of one product C = A * B (m = A.rows, n = B.cols):
+//   1. k_analyze    warp per row: flops(u) = sum |B[a]|, bin of the row.
+//   2. k_scatter    row ids into per-bin lists (device-computed offsets).
+//   3. symbolic     exact |C[u]| per bin kernel (same kernels, NUMERIC=false).
+//   4. scan         device exclusive scan of |C[u]| into C.rowptr (int64).
+//   5. numeric      columns + counts per bin kernel (NUMERIC=true).
+// Bins (see classify):
+//   tiny    flops <= 32     one warp per row; products in registers, bitonic
+//                           sort across the warp, segmented sum, ballot compaction.
+//   hash*   flops <= 4096   one CTA per row; linear-probing hash table in shared
+//                           memory sized 2*min(flops, n) (512/2048/8192 slots),
+//                           then compaction and a shared-memory bitonic sort.
+//   dense   otherwise       one CTA per row; bitmap + counters over a window of
+//                           W columns in shared memory; rows wider than W are
+//                           processed window by window with per-entry cursors
+//                           (B rows are sorted).  Output is emitted word by word
+//                           with ballot compaction, so stores are coalesced.
+// Overflow: products and sums are checked against the value type; an
+// overflow raises the kOverflow status word (the structure stays exact).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+#include <cstring>
+
+#include "internal.h"
+
+namespace rmcm {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kEmptyBin = 255;
+
+// Shared-memory windows of the dense bin (columns per window).
+constexpr int32_t kDenseWinU32 = 49152;       // 192 KB counters + 6 KB bitmap
+constexpr int32_t kDenseWinU64 = 24576;       // 192 KB counters + 3 KB bitmap
+constexpr int32_t kDenseWinSym = 1572864;     // bitmap only: 192 KB
+constexpr int kDenseThreads = 512;
+
+__device__ __forceinline__ void raise_status(int *st, int word) { atomicOr(st + word, 1); }
+
+__device__ __forceinline__ uint32_t mul_chk(uint32_t a, uint32_t b, int *st) {
+    unsigned long long p = (unsigned long long)a * b;
+    if (p > 0xffffffffull) raise_status(st, kOverflow);
+    return (uint32_t)p;
+}
+__device__ __forceinline__ uint64_t mul_chk(uint64_t a, uint64_t b, int *st) {
+    if (__umul64hi(a, b) != 0) raise_status(st, kOverflow);
+    return a * b;
+}
+__device__ __forceinline__ void add_shared_chk(uint32_t *p, uint32_t v, int *st) {
+    uint32_t old = atomicAdd(p, v);
+    if (old > 0xffffffffu - v) raise_status(st, kOverflow);
+}
+__device__ __forceinline__ void add_shared_chk(uint64_t *p, uint64_t v, int *st) {
+    unsigned long long old = atomicAdd((unsigned long long *)p, (unsigned long long)v);
+    if (old > ~0ull - v) raise_status(st, kOverflow);
+}
+__device__ __forceinline__ uint32_t add_chk(uint32_t a, uint32_t b, int *st) {
+    if (a > 0xffffffffu - b) raise_status(st, kOverflow);
+    return a + b;
+}
+__device__ __forceinline__ uint64_t add_chk(uint64_t a, uint64_t b, int *st) {
+    if (a > ~0ull - b) raise_status(st, kOverflow);
+    return a + b;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(kFull, v, d);
+    return v;
+}
+
+__device__ __forceinline__ int32_t warp_min(int32_t v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v = min(v, __shfl_xor_sync(kFull, v, d));
+    return v;
+}
+
+// ------------------------------------------------------------------------
+// 1. analysis and binning
+// ------------------------------------------------------------------------
+
+struct BinParams {
+    int64_t dense_win;      // columns one numeric dense window covers
+    int32_t hash_max;       // flops above -> dense
+    int32_t dense_ratio;    // dense when flops * ratio >= cols and one window covers cols
+};
+
+__device__ __forceinline__ int classify(int64_t f, int64_t ncols, const BinParams &bp) {
+    if (f == 0) return kEmptyBin;
+    if (f <= 32) return kBinTiny;
+    const bool one_window = ncols <= bp.dense_win;
+    if (f > bp.hash_max) return kBinDense;
+    if (one_window && f * (int64_t)bp.dense_ratio >= ncols) return kBinDense;
+    const int64_t need = 2 * min(f, ncols);
+    if (need <= 512) return kBinHash512;
+    if (need <= 2048) return kBinHash2k;
+    return kBinHash8k;
+}
+
+// Warp per row of A: flops and bin; per-bin row counts and the longest
+// A row of the dense bin (it sizes the cursor scratch).
+__global__ void k_analyze(DevCsr A, DevCsr B, BinParams bp, int64_t *flops, uint8_t *bin_of,
+                          int32_t *bin_count, int32_t *dense_max_alen, unsigned long long *flops_total) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < A.rows; r += nwarps) {
+        const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
+        int64_t f = 0;
+        for (int64_t k = a0 + lane; k < a1; k += 32) {
+            const int32_t a = A.col[k];
+            f += B.rowptr[a + 1] - B.rowptr[a];
+        }
+        f = warp_sum(f);
+        if (lane == 0) {
+            const int b = classify(f, B.cols, bp);
+            flops[r] = f;
+            bin_of[r] = (uint8_t)b;
+            if (f) atomicAdd(flops_total, (unsigned long long)f);
+            if (b != kEmptyBin) {
+                atomicAdd(bin_count + b, 1);
+                if (b == kBinDense) atomicMax(dense_max_alen, (int32_t)(a1 - a0 < (int64_t)INT_MAX ? a1 - a0 : (int64_t)INT_MAX));
+            }
+        }
+    }
+}
+
+// Row ids into per-bin lists laid out back to back (offsets from bin_count).
+__global__ void k_scatter(int64_t m, const uint8_t *bin_of, const int32_t *bin_count, int32_t *bin_cursor,
+                          int32_t *lists) {
+    __shared__ int32_t off[kNumBins];
+    if (threadIdx.x == 0) {
+        int32_t s = 0;
+        for (int b = 0; b < kNumBins; b++) { off[b] = s; s += bin_count[b]; }
+    }
+    __syncthreads();
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x) {
+        const int b = bin_of[r];
+        if (b == kEmptyBin) continue;
+        const int32_t pos = atomicAdd(bin_cursor + b, 1);
+        lists[off[b] + pos] = (int32_t)r;
+    }
+}
+
+__global__ void k_zero_counts(int64_t m, const uint8_t *bin_of, int64_t *cnt) {
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x)
+        if (bin_of[r] == kEmptyBin) cnt[r] = 0;
+}
+
+// ------------------------------------------------------------------------
+// tiny bin: one warp per row, <= 32 products held one per lane
+// ------------------------------------------------------------------------
+
+template <typename V, bool NUMERIC>
+__global__ void __launch_bounds__(256) k_tiny(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows, int32_t nrows,
+                                              int64_t *cnt, int *st) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const V *Aval = (const V *)A.val;
+    const V *Bval = (const V *)B.val;
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nrows; w += nwarps) {
+        const int32_t r = rows[w];
+        const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
+        int32_t key = INT_MAX;
+        unsigned long long val = 0;
+        int filled = 0;                                   // products placed so far (uniform)
+        for (int64_t k0 = a0; k0 < a1; k0 += 32) {
+            const int64_t k = k0 + lane;
+            int32_t len = 0;
+            int64_t bs = 0;
+            unsigned long long va = 0;
+            if (k < a1) {
+                const int32_t a = A.col[k];
+                bs = B.rowptr[a];
+                len = (int32_t)(B.rowptr[a + 1] - bs);
+                if (NUMERIC) va = Aval[k];
+            }
+            int32_t incl = len;                           // inclusive scan of lengths
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int32_t o = __shfl_up_sync(kFull, incl, d);
+                if (lane >= d) incl += o;
+            }
+            const int32_t excl = incl - len;
+            const int32_t tot = __shfl_sync(kFull, incl, 31);
+            // lanes [filled, filled + tot) take one product each from this chunk
+            const unsigned nz = __ballot_sync(kFull, len > 0);
+            unsigned starts = (len > 0 && filled + excl < 32) ? (1u << (filled + excl)) : 0u;
+            starts = __reduce_or_sync(kFull, starts);
+            const int p = lane - filled;
+            const bool mine = p >= 0 && p < tot;
+            int src = 0;
+            if (mine) {
+                const unsigned upto = (lane == 31) ? kFull : ((2u << lane) - 1u);
+                const int rank = __popc(starts & upto) - 1;   // source = rank-th lane with len > 0
+                unsigned rest = nz;
+                for (int t = 0; t < rank; t++) rest &= rest - 1u;
+                src = __ffs(rest) - 1;
+            }
+            const int64_t sbs = __shfl_sync(kFull, bs, src);
+            const int32_t sex = __shfl_sync(kFull, excl, src);
+            const unsigned long long sva = __shfl_sync(kFull, va, src);
+            if (mine) {
+                const int64_t q = sbs + (p - sex);
+                key = B.col[q];
+                if (NUMERIC) {
+                    const unsigned long long vb = Bval[q];
+                    if (sizeof(V) == 4) {
+                        val = sva * vb;
+                    } else {
+                        if (__umul64hi(sva, vb) != 0) raise_status(st, kOverflow);
+                        val = sva * vb;
+                    }
+                }
+            }
+            filled += tot;
+        }
+        // bitonic sort of (key, val) across the warp, ascending keys
+#pragma unroll
+        for (int kk = 2; kk <= 32; kk <<= 1) {
+#pragma unroll
+            for (int j = kk >> 1; j > 0; j >>= 1) {
+                const int32_t ok = __shfl_xor_sync(kFull, key, j);
+                const unsigned long long ov = NUMERIC ? __shfl_xor_sync(kFull, val, j) : 0ull;
+                const bool up = (lane & kk) == 0;
+                const bool lower = (lane & j) == 0;
+                const bool take = (lower == up) ? (ok < key) : (ok > key);
+                if (take) { key = ok; if (NUMERIC) val = ov; }
+            }
+        }
+        const int32_t prev = __shfl_up_sync(kFull, key, 1);
+        const bool head = key != INT_MAX && (lane == 0 || prev != key);
+        const unsigned heads = __ballot_sync(kFull, head);
+        if (!NUMERIC) {
+            if (lane == 0) cnt[r] = __popc(heads);
+        } else {
+            // segmented suffix sums: a head ends up with the sum of its run
+            unsigned long long s = val;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned long long o = __shfl_down_sync(kFull, s, d);
+                const int32_t okey = __shfl_down_sync(kFull, key, d);
+                if (lane + d < 32 && okey == key) {
+                    if (s > ~0ull - o) raise_status(st, kOverflow);
+                    s += o;
+                }
+            }
+            if (sizeof(V) == 4 && head && s > 0xffffffffull) raise_status(st, kOverflow);
+            const int64_t base = C.rowptr[r];
+            const int64_t rlen = C.rowptr[r + 1] - base;
+            if (lane == 0 && rlen != __popc(heads)) raise_status(st, kInvariant);
+            if (head) {
+                const int pos = __popc(heads & lt_mask);
+                if (pos < rlen) {
+                    C.col[base + pos] = key;
+                    ((V *)C.val)[base + pos] = (V)s;
+                }
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------
+// hash bins: one CTA per row, shared-memory linear probing
+// ------------------------------------------------------------------------
+
+template <int S>
+__device__ __forceinline__ uint32_t hash_slot(int32_t c) {
+    constexpr int LOG = 31 - __builtin_clz(S);
+    return ((uint32_t)c * 2654435761u) >> (32 - LOG);
+}
+
+template <typename V, bool NUMERIC, int S>
+__device__ __forceinline__ int hash_insert(int32_t *keys, V *vals, int32_t c, V p, int *st) {
+    uint32_t h = hash_slot<S>(c);
+    for (int probe = 0; probe < S; probe++) {
+        const int32_t k = ((volatile int32_t *)keys)[h];
+        if (k == c) {
+            if (NUMERIC) add_shared_chk(vals + h, p, st);
+            return 0;
+        }
+        if (k == -1) {
+            const int32_t old = atomicCAS(keys + h, -1, c);
+            if (old == -1 || old == c) {
+                if (NUMERIC) add_shared_chk(vals + h, p, st);
+                return old == -1;
+            }
+        }
+        h = (h + 1) & (S - 1);
+    }
+    raise_status(st, kInvariant);   // table full: cannot happen with slots >= 2 * nnz
+    return 0;
+}
+
+// Block-wide exclusive scan of one int per thread; returns the total.
+template <int NT>
+__device__ __forceinline__ int block_excl_scan(int v, int *excl, int *s_warp) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int o = __shfl_up_sync(kFull, incl, d);
+        if (lane >= d) incl += o;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    int base = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < NT / 32; w++) {
+        const int t = s_warp[w];
+        if (w < warp) base += t;
+        total += t;
+    }
+    *excl = base + incl - v;
+    __syncthreads();
+    return total;
+}
+
+template <typename V, bool NUMERIC, int S, int NT>
+__global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows, int32_t nrows,
+                                             int64_t *cnt, int *st) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    int32_t *keys = (int32_t *)smem;
+    V *vals = (V *)(keys + S);
+    int32_t *sk = (int32_t *)(vals + (NUMERIC ? S : 0));
+    V *sv = (V *)(sk + S / 2);
+    __shared__ int s_warp[NT / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const V *Aval = (const V *)A.val;
+    const V *Bval = (const V *)B.val;
+    for (int32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
+        const int32_t r = rows[ri];
+        const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
+        for (int i = tid; i < S; i += NT) {
+            keys[i] = -1;
+            if (NUMERIC) vals[i] = 0;
+        }
+        __syncthreads();
+        int fresh = 0;
+        for (int64_t k = a0 + warp; k < a1; k += NT / 32) {
+            const int32_t a = A.col[k];
+            const V va = NUMERIC ? Aval[k] : (V)0;
+            const int64_t bs = B.rowptr[a], be = B.rowptr[a + 1];
+            for (int64_t q = bs + lane; q < be; q += 32) {
+                const int32_t c = B.col[q];
+                const V p = NUMERIC ? mul_chk(va, Bval[q], st) : (V)0;
+                fresh += hash_insert<V, NUMERIC, S>(keys, vals, c, p, st);
+            }
+        }
+        __syncthreads();
+        if (!NUMERIC) {
+            int excl;
+            const int total = block_excl_scan<NT>(fresh, &excl, s_warp);
+            if (tid == 0) cnt[r] = total;
+        } else {
+            constexpr int PER = S / NT;
+            int mine = 0;
+#pragma unroll 4
+            for (int i = 0; i < PER; i++) mine += keys[tid * PER + i] != -1;
+            int off;
+            const int n = block_excl_scan<NT>(mine, &off, s_warp);
+            for (int i = 0; i < PER; i++) {
+                const int slot = tid * PER + i;
+                if (keys[slot] != -1) {
+                    sk[off] = keys[slot];
+                    sv[off] = vals[slot];
+                    off++;
+                }
+            }
+            int P = 1;
+            while (P < n) P <<= 1;
+            for (int i = n + tid; i < P; i += NT) sk[i] = INT_MAX;
+            __syncthreads();
+            for (int kk = 2; kk <= P; kk <<= 1) {
+                for (int j = kk >> 1; j > 0; j >>= 1) {
+                    for (int i = tid; i < P; i += NT) {
+                        const int ixj = i ^ j;
+                        if (ixj > i) {
+                            const bool up = (i & kk) == 0;
+                            const int32_t x = sk[i], y = sk[ixj];
+                            if ((x > y) == up) {
+                                sk[i] = y;
+                                sk[ixj] = x;
+                                const V t = sv[i];
+                                sv[i] = sv[ixj];
+                                sv[ixj] = t;
+                            }
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+            const int64_t base = C.rowptr[r];
+            const int64_t rlen = C.rowptr[r + 1] - base;
+            if (tid == 0 && rlen != n) raise_status(st, kInvariant);
+            const int lim = (int)((int64_t)n < rlen ? (int64_t)n : rlen);
+            for (int i = tid; i < lim; i += NT) {
+                C.col[base + i] = sk[i];
+                ((V *)C.val)[base + i] = sv[i];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------------
+// dense bin: one CTA per row, windowed bitmap + counters in shared memory
+// ------------------------------------------------------------------------
+
+template <typename V, bool NUMERIC>
+__global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows,
+                                                         int32_t nrows, int64_t *cnt, int32_t *cursors,
+                                                         int64_t cur_stride, int32_t W, int *st) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int nwords = W >> 5;
+    uint32_t *bm = (uint32_t *)smem;
+    V *acc = (V *)(smem + (((size_t)nwords * 4 + 15) & ~(size_t)15));
+    __shared__ int64_t s_warp[32];
+    __shared__ int32_t s_next;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const V *Aval = (const V *)A.val;
+    const V *Bval = (const V *)B.val;
+    for (int i = tid; i < nwords; i += blockDim.x) bm[i] = 0;
+    if (NUMERIC)
+        for (int i = tid; i < W; i += blockDim.x) acc[i] = 0;
+    const bool multi = B.cols > W;
+    int32_t *cur = multi ? cursors + (int64_t)blockIdx.x * cur_stride : nullptr;
+    __syncthreads();
+    for (int32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
+        const int32_t r = rows[ri];
+        const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
+        const int64_t row_base = NUMERIC ? C.rowptr[r] : 0;
+        const int64_t row_end = NUMERIC ? C.rowptr[r + 1] : 0;
+        int64_t out = row_base;
+        int64_t total = 0;
+        int64_t w0 = 0;
+        bool first = true;
+        while (true) {
+            const int64_t w1 = min(w0 + (int64_t)W, B.cols);
+            if (tid == 0) s_next = INT_MAX;
+            __syncthreads();
+            int32_t my_next = INT_MAX;
+            for (int64_t k = a0 + warp; k < a1; k += nwarps) {
+                const int32_t a = A.col[k];
+                const V va = NUMERIC ? Aval[k] : (V)0;
+                const int64_t bs = B.rowptr[a], be = B.rowptr[a + 1];
+                int64_t q0 = (multi && !first) ? bs + cur[k - a0] : bs;
+                int64_t stop = be;
+                for (; q0 < be; q0 += 32) {
+                    const int64_t q = q0 + lane;
+                    const bool valid = q < be;
+                    const int32_t c = valid ? B.col[q] : INT_MAX;
+                    if (valid && c < w1) {
+                        const int32_t lc = (int32_t)(c - w0);
+                        atomicOr(bm + (lc >> 5), 1u << (lc & 31));
+                        if (NUMERIC) add_shared_chk(acc + lc, mul_chk(va, Bval[q], st), st);
+                    }
+                    const unsigned beyond = __ballot_sync(kFull, valid && c >= w1);
+                    if (beyond) {
+                        const int src = __ffs(beyond) - 1;
+                        stop = q0 + src;
+                        my_next = min(my_next, __shfl_sync(kFull, c, src));
+                        break;
+                    }
+                }
+                if (multi && lane == 0) cur[k - a0] = (int32_t)(stop - bs);
+            }
+            if (multi) {
+                my_next = warp_min(my_next);
+                if (lane == 0 && my_next != INT_MAX) atomicMin(&s_next, my_next);
+            }
+            __syncthreads();
+            // count the window, warps own contiguous word ranges
+            const int win_words = (int)((w1 - w0 + 31) >> 5);
+            const int chunk = (win_words + nwarps - 1) / nwarps;
+            const int wb = min(warp * chunk, win_words), we = min(wb + chunk, win_words);
+            int64_t c_w = 0;
+            for (int i = wb + lane; i < we; i += 32) {
+                c_w += __popc(bm[i]);
+                if (!NUMERIC) bm[i] = 0;
+            }
+            c_w = warp_sum(c_w);
+            if (lane == 0) s_warp[warp] = c_w;
+            __syncthreads();
+            int64_t base = 0, wtot = 0;
+            for (int w = 0; w < nwarps; w++) {
+                const int64_t t = s_warp[w];
+                if (w < warp) base += t;
+                wtot += t;
+            }
+            if (NUMERIC) {
+                int64_t pos = out + base;
+                for (int i0 = wb; i0 < we; i0 += 32) {
+                    const int i = i0 + lane;
+                    const uint32_t word = i < we ? bm[i] : 0u;
+                    unsigned nz = __ballot_sync(kFull, word != 0);
+                    while (nz) {
+                        const int src = __ffs(nz) - 1;
+                        nz &= nz - 1;
+                        const uint32_t bits = __shfl_sync(kFull, word, src);
+                        if ((bits >> lane) & 1u) {
+                            const int64_t o = pos + __popc(bits & lt_mask);
+                            const int lc = (i0 + src) * 32 + lane;
+                            if (o < row_end) {
+                                C.col[o] = (int32_t)(w0 + lc);
+                                ((V *)C.val)[o] = acc[lc];
+                            }
+                            acc[lc] = 0;
+                        }
+                        pos += __popc(bits);
+                    }
+                    if (i < we) bm[i] = 0;
+                }
+            }
+            out += wtot;
+            total += wtot;
+            const int32_t nx = multi ? s_next : INT_MAX;
+            __syncthreads();
+            if (nx == INT_MAX) break;
+            w0 = ((int64_t)nx / W) * W;
+            first = false;
+        }
+        if (tid == 0) {
+            if (!NUMERIC) cnt[r] = total;
+            else if (total != row_end - row_base) raise_status(st, kInvariant);
+        }
+    }
+}
+
+// ------------------------------------------------------------------------
+// scan of row counts into the row pointer (int64), three phases
+// ------------------------------------------------------------------------
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int64_t block_scan_i64(int64_t v, int64_t *s_warp, int64_t *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int64_t incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int64_t o = __shfl_up_sync(kFull, incl, d);
+        if (lane >= d) incl += o;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    int64_t base = 0, tot = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+        const int64_t t = s_warp[w];
+        if (w < warp) base += t;
+        tot += t;
+    }
+    __syncthreads();
+    *total = tot;
+    return base + incl - v;
+}
+
+// rowptr[i+1] = inclusive partial sums within a tile; tile sums to tile_sum.
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int64_t *cnt, int64_t m, int64_t *rowptr,
+                                                             int64_t *tile_sum) {
+    __shared__ int64_t s_warp[32];
+    const int64_t t0 = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+    int64_t v[kScanItems];
+    int64_t s = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        v[i] = (t0 + i < m) ? cnt[t0 + i] : 0;
+        s += v[i];
+    }
+    int64_t tot;
+    int64_t run = block_scan_i64(s, s_warp, &tot);
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        run += v[i];
+        if (t0 + i < m) rowptr[t0 + i + 1] = run;
+    }
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = tot;
+}
+
+// One block: exclusive scan of the tile sums in place.
+__global__ void __launch_bounds__(1024) k_scan_sums(int64_t *tile_sum, int64_t ntiles, int64_t *rowptr) {
+    __shared__ int64_t s_warp[32];
+    __shared__ int64_t s_carry;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    for (int64_t b = 0; b < ntiles; b += blockDim.x) {
+        const int64_t i = b + threadIdx.x;
+        const int64_t v = i < ntiles ? tile_sum[i] : 0;
+        int64_t tot;
+        const int64_t ex = block_scan_i64(v, s_warp, &tot);
+        const int64_t carry = s_carry;
+        if (i < ntiles) tile_sum[i] = carry + ex;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry = carry + tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) rowptr[0] = 0;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_add(int64_t m, int64_t *rowptr, const int64_t *tile_sum) {
+    const int64_t t0 = (int64_t)blockIdx.x * kScanTile;
+    const int64_t add = tile_sum[blockIdx.x];
+    if (add == 0) return;
+    for (int i = threadIdx.x; i < kScanTile; i += kScanThreads) {
+        const int64_t r = t0 + i;
+        if (r < m) rowptr[r + 1] += add;
+    }
+}
+
+// ------------------------------------------------------------------------
+// small helpers
+// ------------------------------------------------------------------------
+
+// Profiling only: B rows touched by A (distinct columns of A) and their entries.
+__global__ void k_mark_touched(DevCsr A, uint8_t *mark) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < A.nnz; q += (int64_t)gridDim.x * blockDim.x)
+        mark[A.col[q]] = 1;
+}
+
+__global__ void k_sum_touched(DevCsr B, const uint8_t *mark, unsigned long long *out) {
+    unsigned long long rows = 0, ent = 0;
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < B.rows; c += (int64_t)gridDim.x * blockDim.x)
+        if (mark[c]) {
+            rows++;
+            ent += (unsigned long long)(B.rowptr[c + 1] - B.rowptr[c]);
+        }
+    rows = warp_sum(rows);
+    ent = warp_sum(ent);
+    if ((threadIdx.x & 31) == 0 && (rows || ent)) {
+        atomicAdd(out, rows);
+        atomicAdd(out + 1, ent);
+    }
+}
+
+template <typename V>
+__global__ void k_fill_ones(V *v, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v[i] = 1;
+}
+
+int grid_for(rmcm_handle *h, int64_t work, int threads, int per_sm) {
+    int64_t g = (work + threads - 1) / threads;
+    const int64_t cap = (int64_t)h->sm_count * per_sm;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+template <typename F>
+int32_t set_smem(rmcm_handle *h, F *kernel, int64_t bytes) {
+    if (bytes > 48 * 1024) RMCM_CUDA(h, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return RMCM_OK;
+}
+
+template <typename V, bool NUMERIC>
+int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevCsr &C, const int32_t *lists,
+                    const int32_t *counts, int32_t dense_max_alen, int64_t *cnt, int32_t *cursor_base,
+                    int64_t cursor_cap) {
+    cudaStream_t s = h->stream;
+    int *st = h->d_status;
+    int32_t off = 0;
+    const int64_t ncols = B.cols;
+    for (int b = 0; b < kNumBins; b++) {
+        const int32_t n = counts[b];
+        const int32_t *list = lists + off;
+        off += n;
+        if (n == 0) continue;
+        switch (b) {
+            case kBinTiny: {
+                const int grid = grid_for(h, (int64_t)n * 32, 256, 8);
+                k_tiny<V, NUMERIC><<<grid, 256, 0, s>>>(A, B, C, list, n, cnt, st);
+                break;
+            }
+            case kBinHash512: {
+                constexpr int S = 512, NT = 128;
+                const int64_t sm = S * 4 + (NUMERIC ? S * sizeof(V) + (S / 2) * (4 + sizeof(V)) : 0);
+                auto kern = k_hash<V, NUMERIC, S, NT>;
+                RMCM_TRY(set_smem(h, kern, sm));
+                kern<<<grid_for(h, (int64_t)n * NT, NT, 16), NT, sm, s>>>(A, B, C, list, n, cnt, st);
+                break;
+            }
+            case kBinHash2k: {
+                constexpr int S = 2048, NT = 256;
+                const int64_t sm = S * 4 + (NUMERIC ? S * sizeof(V) + (S / 2) * (4 + sizeof(V)) : 0);
+                auto kern = k_hash<V, NUMERIC, S, NT>;
+                RMCM_TRY(set_smem(h, kern, sm));
+                kern<<<grid_for(h, (int64_t)n * NT, NT, 8), NT, sm, s>>>(A, B, C, list, n, cnt, st);
+                break;
+            }
+            case kBinHash8k: {
+                constexpr int S = 8192, NT = 512;
+                const int64_t sm = S * 4 + (NUMERIC ? S * sizeof(V) + (S / 2) * (4 + sizeof(V)) : 0);
+                auto kern = k_hash<V, NUMERIC, S, NT>;
+                RMCM_TRY(set_smem(h, kern, sm));
+                kern<<<grid_for(h, (int64_t)n * NT, NT, 2), NT, sm, s>>>(A, B, C, list, n, cnt, st);
+                break;
+            }
+            case kBinDense: {
+                const int64_t wmax = NUMERIC ? (sizeof(V) == 4 ? kDenseWinU32 : kDenseWinU64) : kDenseWinSym;
+                const int64_t W = std::min<int64_t>(wmax, (ncols + 31) / 32 * 32);
+                const int64_t bm_bytes = ((W / 32) * 4 + 15) & ~15LL;
+                const int64_t sm = bm_bytes + (NUMERIC ? W * (int64_t)sizeof(V) : 0);
+                auto kern = k_dense<V, NUMERIC>;
+                RMCM_TRY(set_smem(h, kern, sm));
+                int per_sm = (int)std::max<int64_t>(1, std::min<int64_t>(4, (200 * 1024) / std::max<int64_t>(sm, 1)));
+                int grid = (int)std::min<int64_t>((int64_t)n, (int64_t)h->sm_count * per_sm);
+                const bool multi = ncols > W;
+                int64_t stride = multi ? std::max<int32_t>(dense_max_alen, 1) : 0;
+                if (multi && (int64_t)grid * stride > cursor_cap) {
+                    grid = (int)std::max<int64_t>(1, cursor_cap / stride);
+                }
+                kern<<<grid, kDenseThreads, sm, s>>>(A, B, C, list, n, cnt, cursor_base, stride, (int32_t)W, st);
+                break;
+            }
+        }
+        h->launches++;
+        RMCM_CUDA(h, cudaGetLastError());
+    }
+    return RMCM_OK;
+}
+
+int32_t scan_rowptr(rmcm_handle *h, const int64_t *cnt, int64_t m, int64_t *rowptr, int64_t *tile_sum) {
+    cudaStream_t s = h->stream;
+    const int64_t ntiles = std::max<int64_t>(1, (m + kScanTile - 1) / kScanTile);
+    if (m > 0) {
+        k_scan_tiles<<<(unsigned)ntiles, kScanThreads, 0, s>>>(cnt, m, rowptr, tile_sum);
+        h->launches++;
+    } else {
+        RMCM_CUDA(h, cudaMemsetAsync(tile_sum, 0, sizeof(int64_t), s));
+    }
+    k_scan_sums<<<1, 1024, 0, s>>>(tile_sum, ntiles, rowptr);
+    h->launches++;
+    if (m > 0) {
+        k_scan_add<<<(unsigned)ntiles, kScanThreads, 0, s>>>(m, rowptr, tile_sum);
+        h->launches++;
+    }
+    RMCM_CUDA(h, cudaGetLastError());
+    return RMCM_OK;
+}
+
+template <typename V>
+int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_mat **Cout, int64_t *flops_out) {
+    const DevCsr A = Am->d, B = Bm->d;
+    const int64_t m = A.rows;
+    cudaStream_t s = h->stream;
+    // scratch layout: flops[m] i64 | cnt[m] i64 | tile sums | bin_of[m] u8 | lists[m] i32 | small counters | cursors
+    const int64_t ntiles = std::max<int64_t>(1, (m + kScanTile - 1) / kScanTile);
+    auto al = [](int64_t x) { return (x + 255) & ~255LL; };
+    const int64_t o_flops = 0;
+    const int64_t o_cnt = o_flops + al(8 * m);
+    const int64_t o_tiles = o_cnt + al(8 * m);
+    const int64_t o_bin = o_tiles + al(8 * ntiles);
+    const int64_t o_lists = o_bin + al(m);
+    const int64_t o_small = o_lists + al(4 * m);
+    const int64_t o_cur = o_small + 256;
+    int64_t need = o_cur;
+    RMCM_TRY(scratch_reserve(h, need));
+    char *sc = (char *)h->scratch;
+    int64_t *flops = (int64_t *)(sc + o_flops);
+    int64_t *cnt = (int64_t *)(sc + o_cnt);
+    int64_t *tiles = (int64_t *)(sc + o_tiles);
+    uint8_t *bin_of = (uint8_t *)(sc + o_bin);
+    int32_t *lists = (int32_t *)(sc + o_lists);
+    int32_t *small = (int32_t *)(sc + o_small);   // [0..4] counts, [8..12] cursors, [16] dense max alen
+    RMCM_CUDA(h, cudaMemsetAsync(small, 0, 256, s));
+
+    ProdRecord *rec = nullptr;
+    size_t rec_idx = 0;
+    if (h->prof_level > 0) {
+        h->prof.emplace_back();
+        rec_idx = h->prof.size() - 1;
+        rec = &h->prof[rec_idx];
+        for (auto &e : rec->ev) RMCM_CUDA(h, cudaEventCreate(&e));
+        RMCM_CUDA(h, cudaEventRecord(rec->ev[0], s));
+    }
+    BinParams bp;
+    bp.dense_win = sizeof(V) == 4 ? kDenseWinU32 : kDenseWinU64;
+    bp.hash_max = h->tune.hash_max_flops;
+    bp.dense_ratio = h->tune.dense_ratio;
+    if (m > 0) {
+        k_analyze<<<grid_for(h, m * 32, 256, 8), 256, 0, s>>>(A, B, bp, flops, bin_of, small, small + 16,
+                                                               (unsigned long long *)(small + 32));
+        k_scatter<<<grid_for(h, m, 256, 8), 256, 0, s>>>(m, bin_of, small, small + 8, lists);
+        k_zero_counts<<<grid_for(h, m, 256, 8), 256, 0, s>>>(m, bin_of, cnt);
+        h->launches += 3;
+        RMCM_CUDA(h, cudaGetLastError());
+    }
+    if (rec) RMCM_CUDA(h, cudaEventRecord(h->prof[rec_idx].ev[1], s));
+    // bin counts, the longest dense A row and the flops to the host
+    RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned, small, 36 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    RMCM_CUDA(h, cudaStreamSynchronize(s));
+    int32_t counts[kNumBins];
+    memcpy(counts, h->h_pinned, sizeof(counts));
+    const int32_t dense_max_alen = ((int32_t *)h->h_pinned)[16];
+    int64_t flops_total = 0;
+    memcpy(&flops_total, (int32_t *)h->h_pinned + 32, sizeof(int64_t));
+    if (flops_out) *flops_out = flops_total;
+
+    // cursor scratch for multi-window dense rows
+    const int64_t wsym = kDenseWinSym, wnum = sizeof(V) == 4 ? kDenseWinU32 : kDenseWinU64;
+    int64_t cursor_cap = 0;
+    if (counts[kBinDense] > 0 && B.cols > wnum) {
+        const int64_t want = (int64_t)h->sm_count * 4 * std::max<int32_t>(dense_max_alen, 1);
+        cursor_cap = std::min<int64_t>(want, std::max<int64_t>(dense_max_alen, 1) * 1024);
+        need = o_cur + al(4 * cursor_cap);
+        RMCM_TRY(scratch_reserve(h, need));
+        sc = (char *)h->scratch;
+        flops = (int64_t *)(sc + o_flops);
+        cnt = (int64_t *)(sc + o_cnt);
+        tiles = (int64_t *)(sc + o_tiles);
+        lists = (int32_t *)(sc + o_lists);
+    }
+    (void)wsym;
+    int32_t *cursors = (int32_t *)(sc + o_cur);
+
+    // symbolic
+    rmcm_mat *C = nullptr;
+    RMCM_TRY(mat_alloc(h, m, B.cols, -1, Am->valtype, &C));
+    if (rec) RMCM_CUDA(h, cudaEventRecord(h->prof[rec_idx].ev[2], s));
+    RMCM_TRY((launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap)));
+    RMCM_TRY(scan_rowptr(h, cnt, m, C->d.rowptr, tiles));
+    if (rec) RMCM_CUDA(h, cudaEventRecord(h->prof[rec_idx].ev[3], s));
+    // nnz and the total flops to the host
+    int64_t *hp = h->h_pinned;
+    RMCM_CUDA(h, cudaMemcpyAsync(hp, C->d.rowptr + m, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    RMCM_CUDA(h, cudaStreamSynchronize(s));
+    const int64_t nnz = hp[0];
+    // allocate the output arrays
+    int32_t rc = mat_alloc(h, m, B.cols, nnz, Am->valtype, &C);
+    if (rc != RMCM_OK) {
+        mat_release(h, C);
+        return rc;
+    }
+    if (rec) RMCM_CUDA(h, cudaEventRecord(h->prof[rec_idx].ev[4], s));
+    rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap);
+    if (rc != RMCM_OK) {
+        mat_release(h, C);
+        return rc;
+    }
+    if (rec) {
+        ProdRecord &R = h->prof[rec_idx];
+        RMCM_CUDA(h, cudaEventRecord(R.ev[5], s));
+        rmcm_product_stats &st = R.st;
+        st.rows = m;
+        st.inner = A.cols;
+        st.cols = B.cols;
+        st.nnz_a = A.nnz;
+        st.nnz_b = B.nnz;
+        st.nnz_c = nnz;
+        st.flops = flops_total;
+        st.valtype = Am->valtype;
+        for (int b = 0; b < kNumBins; b++) st.bin_rows[b] = counts[b];
+        if (h->prof_level >= 2 && A.cols > 0) {
+            // after the numeric pass: the row lists are no longer needed, reuse them
+            uint8_t *mark = (uint8_t *)lists;
+            unsigned long long *acc = (unsigned long long *)(small + 48);
+            if (A.cols + 64 <= 4 * m) {
+                RMCM_CUDA(h, cudaMemsetAsync(mark, 0, A.cols, s));
+                RMCM_CUDA(h, cudaMemsetAsync(acc, 0, 16, s));
+                k_mark_touched<<<grid_for(h, std::max<int64_t>(A.nnz, 1), 256, 8), 256, 0, s>>>(A, mark);
+                k_sum_touched<<<grid_for(h, std::max<int64_t>(B.rows, 1), 256, 8), 256, 0, s>>>(B, mark, acc);
+                RMCM_CUDA(h, cudaMemcpyAsync(hp, acc, 16, cudaMemcpyDeviceToHost, s));
+                RMCM_CUDA(h, cudaStreamSynchronize(s));
+                st.touched_rows = hp[0];
+                st.touched_nnz = hp[1];
+            } else {
+                std::vector<uint8_t> hm(A.cols, 0);
+                std::vector<int32_t> hc(A.nnz);
+                std::vector<int64_t> hr(B.rows + 1);
+                RMCM_CUDA(h, cudaMemcpyAsync(hc.data(), A.col, 4 * A.nnz, cudaMemcpyDeviceToHost, s));
+                RMCM_CUDA(h, cudaMemcpyAsync(hr.data(), B.rowptr, 8 * (B.rows + 1), cudaMemcpyDeviceToHost, s));
+                RMCM_CUDA(h, cudaStreamSynchronize(s));
+                for (int32_t c : hc) hm[c] = 1;
+                for (int64_t c = 0; c < B.rows; c++)
+                    if (hm[c]) {
+                        st.touched_rows++;
+                        st.touched_nnz += hr[c + 1] - hr[c];
+                    }
+            }
+            const int64_t iv = sizeof(V);
+            st.bytes_a = (m + 1) * 8 + A.nnz * (4 + iv);
+            st.bytes_b_touched = st.touched_rows * 16 + st.touched_nnz * (4 + iv);
+            st.bytes_c = (m + 1) * 8 + nnz * (4 + iv);
+        }
+    }
+    *Cout = C;
+    return RMCM_OK;
+}
+
+}  // namespace
+
+int32_t spgemm(rmcm_handle *h, const rmcm_mat *A, const rmcm_mat *B, rmcm_mat **C, int64_t *flops_out) {
+    if (!A || !B || !C) return set_error(h, RMCM_EINVAL, "spgemm: null matrix");
+    if (A->d.cols != B->d.rows)
+        return set_error(h, RMCM_EINVAL, "spgemm: shape mismatch (A.cols != B.rows)");
+    if (A->valtype != B->valtype) return set_error(h, RMCM_EINVAL, "spgemm: value types differ");
+    if (A->valtype == RMCM_VAL_U64) return spgemm_t<uint64_t>(h, A, B, C, flops_out);
+    return spgemm_t<uint32_t>(h, A, B, C, flops_out);
+}
+
+int32_t fill_ones(rmcm_handle *h, void *val, int64_t nnz, int32_t valtype) {
+    if (nnz <= 0) return RMCM_OK;
+    const int grid = grid_for(h, nnz, 256, 8);
+    if (valtype == RMCM_VAL_U64) k_fill_ones<uint64_t><<<grid, 256, 0, h->stream>>>((uint64_t *)val, nnz);
+    else k_fill_ones<uint32_t><<<grid, 256, 0, h->stream>>>((uint32_t *)val, nnz);
+    h->launches++;
+    RMCM_CUDA(h, cudaGetLastError());
+    return RMCM_OK;
+}
+
+}  // namespace rmcm

@@ -1,0 +1,209 @@
+"""Edge cases of the GPU path: empty and ragged inputs, repeated neighbours,
+chains of one matrix, overflow detection (uint32 and uint64), the automatic
+uint64 re-run, bad arguments and the device memory budget."""
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from resmcm_ari_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def csr(dense):
+    dense = np.asarray(dense)
+    rp = [0]
+    col, val = [], []
+    for row in dense:
+        nz = np.nonzero(row)[0]
+        col += nz.tolist()
+        val += row[nz].tolist()
+        rp.append(len(col))
+    return np.array(rp, np.int64), np.array(col, np.int32), np.array(val, np.uint64)
+
+
+def test_repeated_neighbours_count_as_separate_paths(native, engine):
+    vtype = np.array([0, 1], np.int32)
+    hg = native.HeteroGraph.from_adjacency(engine, vtype, np.array([0, 2, 4]), np.array([1, 1, 0, 0]),
+                                           np.array([0, 0, 3, 3]))
+    C, t, _ = engine.run_metapath(hg, "1-3-0-0-1")
+    rp, col, val = C.download()
+    assert rp.tolist() == [0, 1] and col.tolist() == [0] and val.tolist() == [4]
+
+
+def test_empty_result_and_empty_rows(native, engine):
+    g = synth.tiny_dblp()
+    hg = native.HeteroGraph.from_synthetic(engine, g)
+    # edge type 9 does not exist: the leaf is empty, so is the product
+    C, t, _ = engine.run_metapath(hg, "1-3-0-9-2-4-0")
+    assert C.nnz == 0 and t["nnz"] == 0
+    rp, col, _ = C.download()
+    assert rp.tolist() == [0, 0, 0, 0]
+
+
+def test_chain_of_one_matrix_is_the_leaf(native, engine):
+    g = synth.tiny_dblp()
+    hg = native.HeteroGraph.from_synthetic(engine, g)
+    C, t, _ = engine.run_metapath(hg, "0-1-2")
+    rp, col, val = C.download()
+    assert rp.tolist() == [0, 1, 2, 3, 4] and col.tolist() == [0, 0, 0, 0] and val.tolist() == [1, 1, 1, 1]
+    assert t["total_s"] == 0.0
+
+
+def test_empty_matrices(native, engine):
+    A = engine.upload(np.zeros(1, np.int64), np.zeros(0, np.int32), cols=5)
+    B = engine.upload(np.zeros(6, np.int64), np.zeros(0, np.int32), cols=3)
+    C = engine.spgemm(A, B)
+    assert C.shape == (0, 3) and C.nnz == 0
+
+
+def _check_product(native, engine, A, B, vt):
+    A = A.tocsr(); B = B.tocsr()
+    A.sort_indices(); B.sort_indices()
+    ref = (A @ B).tocsr()
+    ref.sum_duplicates(); ref.sort_indices()
+    Am = engine.upload(A.indptr, A.indices, cols=A.shape[1], val=A.data.astype(np.uint64), valtype=vt)
+    Bm = engine.upload(B.indptr, B.indices, cols=B.shape[1], val=B.data.astype(np.uint64), valtype=vt)
+    Cm = engine.spgemm(Am, Bm)
+    rp, col, val = Cm.download()
+    assert np.array_equal(rp, ref.indptr) and np.array_equal(col, ref.indices)
+    assert np.array_equal(val.astype(np.uint64), ref.data.astype(np.uint64))
+
+
+def _random_csr(rng, m, n, row_nnz, vmax=3):
+    rows, cols = [], []
+    for r in range(m):
+        k = int(row_nnz[r])
+        rows += [r] * k
+        cols += rng.choice(n, k, replace=False).tolist()
+    data = rng.integers(1, vmax + 1, len(rows))
+    return sp.csr_matrix((data.astype(np.int64), (rows, cols)), shape=(m, n))
+
+
+def test_products_in_every_bin_match_scipy(native, engine):
+    """Rows spanning the tiny, hash and dense bins, with empty rows."""
+    rng = np.random.default_rng(5)
+    m, k, n = 300, 400, 20000
+    a_nnz = np.linspace(0, 120, m).astype(int)
+    a_nnz[::7] = 0
+    A = _random_csr(rng, m, k, a_nnz)
+    B = _random_csr(rng, k, n, rng.integers(0, 400, k))
+    for vt in (native.VAL_U32, native.VAL_U64):
+        _check_product(native, engine, A, B, vt)
+
+
+def test_hash_bins_with_wide_columns(native, engine):
+    rng = np.random.default_rng(6)
+    m, k, n = 500, 3000, 5_000_000
+    A = _random_csr(rng, m, k, rng.integers(1, 60, m))
+    B = _random_csr(rng, k, n, rng.integers(0, 70, k))
+    for vt in (native.VAL_U32, native.VAL_U64):
+        _check_product(native, engine, A, B, vt)
+
+
+def test_wide_rows_use_several_windows(native, engine):
+    """Dense-bin rows whose output spans more columns than one shared-memory window."""
+    rng = np.random.default_rng(9)
+    m, k, n = 40, 600, 200_000
+    A = _random_csr(rng, m, k, rng.integers(200, 400, m))
+    B = _random_csr(rng, k, n, np.full(k, 60))
+    for vt in (native.VAL_U32, native.VAL_U64):
+        _check_product(native, engine, A, B, vt)
+
+
+def test_uint32_overflow_is_reported_and_uint64_is_exact(native, engine):
+    import ctypes
+    big = np.uint64(1 << 31)
+    A = engine.upload(np.array([0, 2]), np.array([0, 1]), cols=2, val=np.array([big, big]), valtype=native.VAL_U32)
+    B = engine.upload(np.array([0, 1, 2]), np.array([0, 0]), cols=1, val=np.array([1, 1]), valtype=native.VAL_U32)
+    h = ctypes.c_void_p()
+    rc = native.lib().rmcm_spgemm(engine._h, A._h, B._h, ctypes.byref(h))
+    assert rc == native.EOVERFLOW
+    native.lib().rmcm_mat_free(engine._h, h)
+    A64 = engine.upload(np.array([0, 2]), np.array([0, 1]), cols=2, val=np.array([big, big]), valtype=native.VAL_U64)
+    B64 = engine.upload(np.array([0, 1, 2]), np.array([0, 0]), cols=1, val=np.array([1, 1]), valtype=native.VAL_U64)
+    C = engine.spgemm(A64, B64)
+    assert C.download()[2].tolist() == [1 << 32]
+
+
+def test_uint64_overflow_is_reported(native, engine):
+    big = np.uint64(1 << 40)
+    A = engine.upload(np.array([0, 1]), np.array([0]), cols=1, val=np.array([big]), valtype=native.VAL_U64)
+    B = engine.upload(np.array([0, 1]), np.array([0]), cols=1, val=np.array([big]), valtype=native.VAL_U64)
+    import ctypes
+    h = ctypes.c_void_p()
+    rc = native.lib().rmcm_spgemm(engine._h, A._h, B._h, ctypes.byref(h))
+    assert rc == native.EOVERFLOW
+
+
+def test_auto_mode_reruns_in_uint64(native):
+    """K(64,64): an 8-matrix alternating chain has 64^7 = 2^42 paths per pair."""
+    n = 64
+    src = np.repeat(np.arange(n), n)
+    dst = np.tile(np.arange(n), n)
+    g = synth.SyntheticHIN("k64", [n, n], [synth.Relation(0, 1, 0, 1, src, dst)])
+    eng = native.Engine(device=0, valtype=native.VAL_AUTO)
+    hg = native.HeteroGraph.from_synthetic(eng, g)
+    C, t, rc = eng.run_metapath(hg, "0-0-1-1-0-0-1-1-0-0-1-1-0-0-1-1-0")
+    assert rc == native.OK and C.valtype == native.VAL_U64
+    rp, col, val = C.download()
+    assert C.nnz == n * n and set(val.tolist()) == {n ** 7}
+    C.free()
+    hg.close()
+    eng.close()
+
+
+def test_bad_arguments(native, engine):
+    g = synth.tiny_dblp()
+    hg = native.HeteroGraph.from_synthetic(engine, g)
+    with pytest.raises(native.RmcmError) as e:
+        engine.run_metapath(hg, "1-3")
+    assert e.value.status == native.EINVAL
+    with pytest.raises(native.RmcmError):
+        engine.run_metapath(hg, "1-3-7-0-1")          # vertex type 7 is not in the graph
+    A = engine.upload(np.array([0, 1]), np.array([0]), cols=3)
+    B = engine.upload(np.array([0, 1, 1]), np.array([0]), cols=2)
+    with pytest.raises(native.RmcmError) as e:
+        engine.spgemm(A, B)
+    assert e.value.status == native.EINVAL
+    with pytest.raises(native.RmcmError) as e:
+        engine.upload(np.array([0, 1]), np.array([5]), cols=3)
+    assert e.value.status == native.EINVAL
+
+
+def test_unsorted_upload_is_sorted(native, engine):
+    M = engine.upload(np.array([0, 3]), np.array([4, 1, 2]), cols=5, val=np.array([7, 8, 9], np.uint64),
+                      valtype=native.VAL_U64)
+    rp, col, val = M.download()
+    assert col.tolist() == [1, 2, 4] and val.tolist() == [8, 9, 7]
+
+
+def test_memory_budget_is_enforced(native):
+    eng = native.Engine(device=0, mem_budget_bytes=4 << 20)
+    g = synth.dblp_like(n_a=3000, n_p=6000, n_v=20, seed=7)
+    hg = native.HeteroGraph.from_synthetic(eng, g)
+    with pytest.raises(native.RmcmError) as e:
+        eng.run_metapath(hg, "0-0-1-3-0")             # 8.5M nnz result does not fit in 4 MB
+    assert e.value.status == native.ENOMEM
+    hg.close()
+    eng.close()
+
+
+def test_cli_output_line(native, tmp_path):
+    g = synth.tiny_dblp()
+    files = g.write_text(str(tmp_path))
+    out = tmp_path / "out.txt"
+    r = subprocess.run([native.CLI_PATH, "4", "1", files["graph"], files["vertex"], files["edge"],
+                        files["metapaths"], str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = out.read_text().splitlines()
+    assert [ln.split()[0] for ln in lines] == g.metapaths
+    assert [int(ln.split()[1]) for ln in lines] == [7, 9, 14, 1, 4]
+    for ln in lines:
+        parts = ln.split()
+        assert len(parts) == 6
+        [float(x) for x in parts[2:]]
