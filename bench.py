@@ -1,0 +1,415 @@
+"""Benchmark: meta-path chains per second on one GB300 (plain drop-in path).
+
+Workload: seeded retail-style heterogeneous graph (U=1,000,000 users,
+I=300,000 items, C=2,000 categories, T=20,000 tags; 20M U-I edges with Zipf
+degrees on both sides, one category per item, 5-15 tags per item) and its
+four meta-path chains I-T-I-C, C-I-U-I-C, T-I-C-I-T, C-I-T-I-U-I-C.  One step
+is one pass of the hot path (RES estimator -> warp DP -> binned Gustavson
+SpGEMM chain) over all four chains, results computed in full and freed.
+
+* value: chains/s with the leaf CSRs resident in HBM when the timed region
+  starts (CUDA events on the engine's stream, barrier + sync on both sides).
+* e2e: the same chains through the C ABI from pinned HOST buffers: per step
+  every leaf CSR is uploaded (rmcm_mat_upload), the chain runs, and every
+  result CSR (rowptr, columns, counts) is copied back to pinned host memory.
+* roofline: the dominant numeric SpGEMM pass (largest event time), its
+  algorithmic bytes (A + touched B rows + C) over its event-timed duration,
+  against the measured HBM copy bandwidth.
+* cpu_baseline: the oracle port of the reference's algorithm (Boolean
+  Gustavson, OpenMP, all host cores) on the same four chains.
+
+--impl reference times that CPU implementation alone, as the reference arm.
+Multi-GPU (torchrun): every rank runs the full workload on its own GPU
+(independent replicas, weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from resmcm_ari_gb300 import synth  # noqa: E402
+
+WORKLOAD = ("retail U=1M I=300k C=2k T=20k, U-I 20M edges (Zipf 1.7 users x Zipf 1.3 items), "
+            "1 category/item (Zipf 1.1), 5-15 tags/item; chains I-T-I-C, C-I-U-I-C, T-I-C-I-T, C-I-T-I-U-I-C")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0, help="shrink the graph (profiling captures)")
+    ap.add_argument("--chains", default="all", help="comma list of chain indices to run")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-clocks", action="store_true")
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--detail", action="store_true", help="per-product stats to stderr")
+    return ap.parse_args()
+
+
+def make_graph(scale: float, seed: int):
+    """Seeded graph, cached on local disk per (scale, seed)."""
+    key = f"retail_s{seed}_x{scale:g}"
+    path = os.path.join(tempfile.gettempdir(), f"resmcm_bench_{key}.npz")
+    if os.path.exists(path):
+        z = np.load(path)
+        g = synth.SyntheticHIN(key, z["type_sizes"].tolist())
+        g._adj = (z["ptr"], z["nbr"], z["et"])
+        g.metapaths = synth.retail_like(n_u=10, n_i=10, n_c=2, n_t=2, ui_edges=10).metapaths
+        return g
+    sc = lambda x: max(2, int(round(x * scale)))  # noqa: E731
+    g = synth.retail_like(n_u=sc(1_000_000), n_i=sc(300_000), n_c=sc(2_000), n_t=sc(20_000),
+                          ui_edges=sc(20_000_000), seed=seed)
+    ptr, nbr, et = g.adjacency()
+    tmp = path + f".{os.getpid()}.tmp.npz"
+    np.savez(tmp, type_sizes=np.array(g.type_sizes), ptr=ptr, nbr=nbr, et=et)
+    os.replace(tmp, path)
+    return g
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profiles():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "dense_numeric_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    out = {}
+    for ln in open(p):
+        if ":" in ln:
+            k, v = ln.split(":", 1)
+            out[k.strip()] = v.strip()
+    try:
+        return {"bytes_per_alg_byte": float(out["dram_bytes_per_algorithmic_byte"]), "source": p}
+    except (KeyError, ValueError):
+        return None
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_reference(g, metapaths, steps, warmup, sample_note):
+    """Oracle port of the reference's algorithm on all host cores: chains/s over full passes."""
+    import oracle
+    oracle.build()
+    og = oracle.OracleGraph.from_synthetic(g)
+    threads = os.cpu_count() or 1
+    times = []
+    for it in range(warmup + steps):
+        t0 = time.perf_counter()
+        for mp in metapaths:
+            og.chain(mp, oracle.MODE_BOOL, threads=threads, export=False)
+        dt = time.perf_counter() - t0
+        if it >= warmup:
+            times.append(dt)
+    per_step = sum(times) / len(times)
+    return {"value": len(metapaths) / per_step, "unit": "chains/s", "cores": threads, "kind": "port",
+            "sample": sample_note, "s_per_pass": per_step}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if ws > 1 and rank != 0:
+        return
+    g = make_graph(args.scale, args.seed)
+    mps = select(g.metapaths, args.chains)
+    steps, warmup = max(1, args.steps), max(0, min(args.warmup, 1))
+    cb = cpu_reference(g, mps, steps, warmup, f"{len(mps)} full chains per step ({WORKLOAD})")
+    line = {"impl": "reference", "metric": "chains/s", "value": cb["value"], "unit": "chains/s", "n_gpus": 0,
+            "steps": steps, "warmup": warmup, "ms_per_step": cb["s_per_pass"] * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bool", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "chains": mps},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": "chains/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "oracle port of efficient/resmcm.cpp (Boolean bitmap Gustavson, OpenMP dynamic schedule); "
+                    "the reference source itself is not present on this host"}
+    print(json.dumps(line), flush=True)
+
+
+def select(mps, spec):
+    if spec == "all":
+        return list(mps)
+    return [mps[int(i)] for i in spec.split(",")]
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    import resmcm_ari_gb300 as rg
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    rg.build()
+    g = make_graph(args.scale, args.seed)
+    mps = select(g.metapaths, args.chains)
+
+    stream = torch.cuda.current_stream()
+    eng = rg.Engine(device=local, valtype=rg.VAL_AUTO, stream=stream.cuda_stream)
+    hg = rg.HeteroGraph.from_synthetic(eng, g)
+    leaves = {mp: hg.leaves(mp, rg.VAL_U32) for mp in mps}
+    # uint64 leaves too (used when a chain escalates on overflow), built untimed
+    for mp in mps:
+        hg.leaves(mp, rg.VAL_U64)
+
+    def step():
+        nnz = 0
+        for mp in mps:
+            C, t, _ = eng.run_metapath(hg, mp, keep=True)
+            nnz += C.nnz
+            C.free()
+        return nnz
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    # warm-up: the first pass collects the algorithmic bytes of every product
+    eng.set_profiling(2)
+    step_nnz = step()
+    bytes_stats = eng.product_stats(reset=True)
+    eng.set_profiling(1)
+    for _ in range(max(0, args.warmup - 1)):
+        step()
+    eng.product_stats(reset=True)
+
+    clocks = rg_clock = ClockSampler(local)
+    if not args.no_clocks:
+        rg_clock.start()
+    launches0 = eng.kernel_launches
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    launches = eng.kernel_launches - launches0
+    clk = rg_clock.stop() if not args.no_clocks else None
+    timed_stats = eng.product_stats(reset=True)
+    eng.set_profiling(0)
+    if ws > 1:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    ms_per_step = elapsed_ms / args.steps
+    value = len(mps) * ws / (ms_per_step / 1e3)
+
+    # roofline of the dominant numeric pass: bytes from the first pass, times from the timed region
+    nprod = len(bytes_stats)
+    per_prod_ms = [[] for _ in range(nprod)]
+    for i, st in enumerate(timed_stats):
+        per_prod_ms[i % nprod].append(st["numeric_ms"])
+    avg_ms = [sum(x) / len(x) if x else 0.0 for x in per_prod_ms]
+    dom = int(np.argmax(avg_ms)) if nprod else 0
+    peak, peak_kind = peak_hbm()
+    roof = None
+    if nprod:
+        b = bytes_stats[dom]
+        alg = b["bytes_a"] + b["bytes_b_touched"] + b["bytes_c"]
+        achieved = alg / (avg_ms[dom] / 1e3) / 1e9
+        tr = traffic_from_profiles()
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_kind": f"of {peak_kind}",
+                "traffic": (alg * tr["bytes_per_alg_byte"]) if tr else None,
+                "kernel": "spgemm numeric pass (all bins) of the dominant product",
+                "product": {k: b[k] for k in ("rows", "inner", "cols", "nnz_a", "nnz_c", "flops", "bin_rows")},
+                "algorithmic_bytes": alg, "launch_ms": avg_ms[dom]}
+        tot_alg = sum(s["bytes_a"] + s["bytes_b_touched"] + s["bytes_c"] for s in bytes_stats)
+        tot_ms = sum(avg_ms)
+        roof["all_numeric_passes"] = {"achieved": tot_alg / (tot_ms / 1e3) / 1e9, "ms_per_step": tot_ms}
+        sym_ms = [0.0] * nprod
+        for i, st in enumerate(timed_stats):
+            sym_ms[i % nprod] += st["symbolic_ms"] / max(1, len(per_prod_ms[i % nprod]))
+        roof["symbolic_ms_per_step"] = sum(sym_ms)
+
+    if args.detail and rank == 0:
+        for i, b in enumerate(bytes_stats):
+            row = {k: b[k] for k in ("rows", "inner", "cols", "nnz_a", "nnz_b", "nnz_c", "flops", "bin_rows",
+                                      "valtype", "touched_rows", "touched_nnz")}
+            reps = [st for j, st in enumerate(timed_stats) if j % nprod == i]
+            for key in ("analyze_ms", "symbolic_ms", "numeric_ms"):
+                row[key] = sum(st[key] for st in reps) / max(1, len(reps))
+            alg = b["bytes_a"] + b["bytes_b_touched"] + b["bytes_c"]
+            row["alg_bytes"] = alg
+            row["numeric_gbs"] = alg / (row["numeric_ms"] / 1e3) / 1e9 if row["numeric_ms"] else None
+            row["gflops_numeric"] = b["flops"] / (row["numeric_ms"] / 1e3) / 1e9 if row["numeric_ms"] else None
+            print("PRODUCT " + json.dumps(row), file=sys.stderr, flush=True)
+
+    # end to end through the C ABI from pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        host = {}
+        h2d = 0
+        for mp in mps:
+            mats = []
+            for L in leaves[mp]:
+                rp, col, val = L.download(values=False)
+                rows, cols = L.shape
+                trp = torch.from_numpy(rp).pin_memory()
+                tcol = torch.from_numpy(col).pin_memory()
+                mats.append((trp, tcol, cols))
+                h2d += rp.nbytes + col.nbytes
+            host[mp] = mats
+        # result buffers (pinned) sized from the device run
+        res_rows = {}
+        for mp in mps:
+            C, _, _ = eng.run_metapath(hg, mp)
+            res_rows[mp] = (C.shape[0], C.nnz, C.valtype)
+            C.free()
+        d2h = 0
+        outbuf = {}
+        for mp, (rows, nnz, vt) in res_rows.items():
+            outbuf[mp] = (torch.empty(rows + 1, dtype=torch.int64, pin_memory=True),
+                          torch.empty(max(nnz, 1), dtype=torch.int32, pin_memory=True),
+                          torch.empty(max(nnz, 1), dtype=torch.int64 if vt == rg.VAL_U64 else torch.int32,
+                                      pin_memory=True))
+            d2h += (rows + 1) * 8 + nnz * 4 + nnz * (8 if vt == rg.VAL_U64 else 4)
+        import ctypes as C_
+
+        def e2e_step():
+            for mp in mps:
+                mats = [eng.upload_ptr(trp.data_ptr(), tcol.data_ptr(), trp.numel() - 1, cols)
+                        for trp, tcol, cols in host[mp]]
+                Cm, _, _ = eng.chain(mats)
+                rp_b, col_b, val_b = outbuf[mp]
+                eng._check(rg.lib().rmcm_mat_download(eng._h, Cm._h, C_.c_void_p(rp_b.data_ptr()),
+                                                      C_.c_void_p(col_b.data_ptr()), C_.c_void_p(val_b.data_ptr())))
+                Cm.free()
+                for m in mats:
+                    m.free()
+
+        for _ in range(max(1, min(args.warmup, 2))):
+            e2e_step()
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier()
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        if ws > 1:
+            t = torch.tensor([e2e_s], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": len(mps) * ws / e2e_s, "unit": "chains/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cpu = cpu_reference(g, mps, 1, 0, f"one full pass over the {len(mps)} chains ({WORKLOAD})")
+        cpu.pop("s_per_pass", None)
+
+    if rank == 0:
+        line = {
+            "metric": "chains/s", "value": value, "unit": "chains/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": WORKLOAD if args.scale == 1.0 else f"{WORKLOAD} (scaled x{args.scale:g})",
+                       "chains": mps, "values": "uint32 path counts, uint64 from the first overflowing product; "
+                                                "estimator and DP in FP64",
+                       "l2": "inputs larger than L2 (leaf CSRs %.0f MB, results %.0f MB per step)" % (
+                           sum(L.nnz * 8 + (L.shape[0] + 1) * 8 for mp in mps for L in leaves[mp]) / 1e6,
+                           step_nnz * 8 / 1e6),
+                       "parallelism": f"replicas x{ws}"},
+            "nnz_per_s": step_nnz * ws / (ms_per_step / 1e3),
+            "result_nnz_per_step": step_nnz,
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+    hg.close()
+    eng.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

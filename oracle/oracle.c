@@ -773,7 +773,7 @@ static int chain_impl(const orc_graph *g, const char *metapath, const int32_t *f
             free(bitmap); free(t_times); free(t_rows); free(res);
             rc = ORC_ENOMEM; goto fail;
         }
-        rowmat *stack[64];
+        rowmat *stack[64] = {0};
         int32_t sp = 0;
         int ovf = 0;
         for (int32_t p = 0; p < len - 1 && !rc; p++) {     /* executor :709-760 */

@@ -335,6 +335,14 @@ class Engine:
                                           None if v is None else _ptr(v), valtype, C.byref(h)))
         return Matrix(self, h.value)
 
+    def upload_ptr(self, rowptr_ptr: int, col_ptr: int, rows: int, cols: int, val_ptr: int = 0,
+                   valtype: int = VAL_U32) -> Matrix:
+        """rmcm_mat_upload from raw host pointers (e.g. pinned buffers); val_ptr 0 = all ones."""
+        h = C.c_void_p()
+        self._check(lib().rmcm_mat_upload(self._h, rows, cols, C.c_void_p(rowptr_ptr), C.c_void_p(col_ptr),
+                                          C.c_void_p(val_ptr) if val_ptr else None, valtype, C.byref(h)))
+        return Matrix(self, h.value)
+
     @staticmethod
     def _chain_ptrs(chain):
         arr = (C.c_void_p * len(chain))(*[m._h.value for m in chain])

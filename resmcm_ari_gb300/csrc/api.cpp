@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -430,8 +431,15 @@ int32_t copy_mat(rmcm_handle *h, const rmcm_mat *src, rmcm_mat **out) {
 }
 
 // SSP_dynamic on device-resident matrices (see file comment).
+//
+// With `widen` set, products run in uint32 and the chain escalates to uint64
+// at the first product whose counts overflow: that product is recomputed in
+// uint64 from widened operands (every earlier intermediate is exact, its
+// counts having fit), and the rest of the chain continues in uint64.  Leaves
+// in uint64 come from `leaf64` when given (the graph's cache), else are
+// widened here.
 int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int32_t *fixed_pairs, rmcm_mat **Cout,
-                   rmcm_timings *t) {
+                   rmcm_timings *t, bool widen, const std::function<int32_t(int, rmcm_mat **)> &leaf64) {
     rmcm_timings tm{};
     *Cout = nullptr;
     if (len < 1 || len > 16) return set_error(h, RMCM_EINVAL, "chain length must be 1..16");
@@ -442,12 +450,14 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
             return set_error(h, RMCM_EINVAL, "consecutive matrices do not chain");
     }
     cudaStream_t s = h->stream;
-    tm.valtype = mats[0]->valtype;
+    int32_t cur = mats[0]->valtype;
+    widen = widen && cur == RMCM_VAL_U32;
     if (len == 1) {
         // efficient/resmcm.cpp:670-677: the leaf itself is the result (no timed work)
         RMCM_TRY(copy_mat(h, mats[0], Cout));
         RMCM_CUDA(h, cudaStreamSynchronize(s));
         tm.nnz = (*Cout)->d.nnz;
+        tm.valtype = cur;
         if (t) *t = tm;
         return RMCM_OK;
     }
@@ -500,31 +510,69 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
     }
     // (c) executor, efficient/resmcm.cpp:709-760
     std::vector<rmcm_mat *> stack;
+    std::vector<rmcm_mat *> wide(len, nullptr);     // uint64 leaves widened here
+    auto leaf = [&](int i, const rmcm_mat **out) -> int32_t {
+        if (cur == mats[i]->valtype) {
+            *out = mats[i];
+            return RMCM_OK;
+        }
+        if (leaf64) {
+            rmcm_mat *m = nullptr;
+            RMCM_TRY(leaf64(i, &m));
+            *out = m;
+            return RMCM_OK;
+        }
+        if (!wide[i]) RMCM_TRY(convert_values(h, mats[i], RMCM_VAL_U64, &wide[i]));
+        *out = wide[i];
+        return RMCM_OK;
+    };
     double spgemm_s = 0;
     for (int p = 0; p < len - 1 && rc == RMCM_OK; p++) {
         const int k = pairs[2 * p], l = pairs[2 * p + 1];
         const int sz = (int)stack.size();
-        const rmcm_mat *A, *B;
-        if (k >= 0 && l >= 0) { A = mats[k]; B = mats[l]; }
-        else if (k == -1 && l >= 0) { A = stack[sz - 1]; B = mats[l]; }
-        else if (k >= 0 && l == -1) { A = mats[k]; B = stack[sz - 1]; }
-        else { A = stack[sz - 2]; B = stack[sz - 1]; }
+        const rmcm_mat *A = nullptr, *B = nullptr;
+        if (k >= 0) rc = leaf(k, &A);
+        else A = (l >= 0) ? stack[sz - 1] : stack[sz - 2];
+        if (rc == RMCM_OK) {
+            if (l >= 0) rc = leaf(l, &B);
+            else B = stack[sz - 1];
+        }
+        if (rc != RMCM_OK) break;
         cudaEventRecord(ev[3], s);
         rmcm_mat *C = nullptr;
         int64_t fl = 0;
         rc = spgemm(h, A, B, &C, &fl);
-        tm.flops += fl;
         cudaEventRecord(ev[4], s);
         if (rc != RMCM_OK) break;
         cudaEventSynchronize(ev[4]);
         spgemm_s += elapsed_s(ev[3], ev[4]);
+        if (widen && cur == RMCM_VAL_U32) {
+            const int32_t st = check_status(h);
+            if (st == RMCM_EOVERFLOW) {
+                // escalate: drop C, widen the live intermediates, redo this product
+                mat_release(h, C);
+                cur = RMCM_VAL_U64;
+                for (auto &m : stack) {
+                    rmcm_mat *w = nullptr;
+                    rc = convert_values(h, m, RMCM_VAL_U64, &w);
+                    if (rc != RMCM_OK) break;
+                    mat_release(h, m);
+                    m = w;
+                }
+                p--;
+                continue;
+            }
+            if (st != RMCM_OK) {
+                mat_release(h, C);
+                rc = st;
+                break;
+            }
+        }
+        tm.flops += fl;
         tm.n_products++;
         if (k >= 0 && l >= 0) {
             stack.push_back(C);
-        } else if (k == -1 && l >= 0) {
-            mat_release(h, stack[sz - 1]);
-            stack[sz - 1] = C;
-        } else if (k >= 0 && l == -1) {
+        } else if (k >= 0 || l >= 0) {
             mat_release(h, stack[sz - 1]);
             stack[sz - 1] = C;
         } else {
@@ -534,6 +582,7 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
             stack[sz - 2] = C;
         }
     }
+    for (auto *m : wide) mat_release(h, m);
     if (rc != RMCM_OK) {
         for (auto *m : stack) mat_release(h, m);
         return rc;
@@ -544,6 +593,7 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
     tm.dp_s = elapsed_s(ev[1], ev[2]);
     tm.spgemm_s = spgemm_s;
     tm.total_s = elapsed_s(ev[0], ev[5]);
+    tm.valtype = cur;
     *Cout = stack[0];
     tm.nnz = stack[0]->d.nnz;
     rc = check_status(h);
@@ -904,7 +954,7 @@ RMCM_API int32_t rmcm_spgemm(rmcm_handle *h, const rmcm_mat *A, const rmcm_mat *
 RMCM_API int32_t rmcm_chain(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, const int32_t *pairs,
                             rmcm_mat **C, rmcm_timings *t) {
     if (!h || !chain || !C) return RMCM_EINVAL;
-    int32_t rc = chain_exec(h, chain, len, pairs, C, t);
+    int32_t rc = chain_exec(h, chain, len, pairs, C, t, h->valtype == RMCM_VAL_AUTO, nullptr);
     if (rc != RMCM_OK && rc != RMCM_EOVERFLOW && *C) {
         mat_release(h, *C);
         *C = nullptr;
@@ -921,25 +971,18 @@ RMCM_API int32_t rmcm_run_metapath(rmcm_handle *h, rmcm_graph *g, const char *me
         return set_error(h, RMCM_EINVAL, std::string("the meta-path is incorrect: ") + metapath);
     const int len = (int)ets.size();
     if (len < 1 || len > 16) return set_error(h, RMCM_EINVAL, "meta-path must have 1..16 edge types");
-    int32_t vt_try[2] = {h->valtype == RMCM_VAL_U64 ? RMCM_VAL_U64 : RMCM_VAL_U32, RMCM_VAL_U64};
-    const int tries = h->valtype == RMCM_VAL_AUTO ? 2 : 1;
-    int32_t rc = RMCM_OK;
-    for (int attempt = 0; attempt < tries; attempt++) {
-        std::vector<rmcm_mat *> mats(len);
-        for (int i = 0; i < len; i++) RMCM_TRY(get_leaf(h, g, vts[i], vts[i + 1], ets[i], vt_try[attempt], &mats[i]));
-        rmcm_mat *res = nullptr;
-        rc = chain_exec(h, mats.data(), len, nullptr, &res, t);
-        if (rc == RMCM_EOVERFLOW && attempt + 1 < tries) {
-            mat_release(h, res);
-            continue;
-        }
-        if (res && (rc == RMCM_OK || rc == RMCM_EOVERFLOW)) {
-            if (C) *C = res;
-            else mat_release(h, res);
-        } else if (res) {
-            mat_release(h, res);
-        }
-        break;
+    const int32_t vt = h->valtype == RMCM_VAL_U64 ? RMCM_VAL_U64 : RMCM_VAL_U32;
+    const bool widen = h->valtype == RMCM_VAL_AUTO;
+    std::vector<rmcm_mat *> mats(len);
+    for (int i = 0; i < len; i++) RMCM_TRY(get_leaf(h, g, vts[i], vts[i + 1], ets[i], vt, &mats[i]));
+    auto leaf64 = [&](int i, rmcm_mat **out) { return get_leaf(h, g, vts[i], vts[i + 1], ets[i], RMCM_VAL_U64, out); };
+    rmcm_mat *res = nullptr;
+    int32_t rc = chain_exec(h, mats.data(), len, nullptr, &res, t, widen, leaf64);
+    if (res && (rc == RMCM_OK || rc == RMCM_EOVERFLOW)) {
+        if (C) *C = res;
+        else mat_release(h, res);
+    } else if (res) {
+        mat_release(h, res);
     }
     return rc;
 }

@@ -137,8 +137,6 @@ inline int64_t val_bytes(int32_t valtype) { return valtype == RMCM_VAL_U64 ? 8 :
 // spgemm.cu
 int32_t spgemm(rmcm_handle *h, const rmcm_mat *A, const rmcm_mat *B, rmcm_mat **C, int64_t *flops_out);
 int32_t fill_ones(rmcm_handle *h, void *val, int64_t nnz, int32_t valtype);
-int32_t sort_rows(rmcm_handle *h, rmcm_mat *m);
-int32_t check_cols(rmcm_handle *h, const rmcm_mat *m);
 int32_t convert_values(rmcm_handle *h, const rmcm_mat *src, int32_t valtype, rmcm_mat **out);
 // estimator.cu: c_dev[len*len] on the device
 int32_t estimate(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, double *c_dev);

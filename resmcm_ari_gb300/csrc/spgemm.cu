@@ -42,9 +42,9 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kEmptyBin = 255;
 
 // Shared-memory windows of the dense bin (columns per window).
-constexpr int32_t kDenseWinU32 = 49152;       // 192 KB counters + 6 KB bitmap
-constexpr int32_t kDenseWinU64 = 24576;       // 192 KB counters + 3 KB bitmap
-constexpr int32_t kDenseWinSym = 1572864;     // bitmap only: 192 KB
+constexpr int32_t kDenseWinU32 = 40960;       // 160 KB counters + 40 KB presence bytes
+constexpr int32_t kDenseWinU64 = 22528;       // 176 KB counters + 22 KB presence bytes
+constexpr int32_t kDenseWinSym = 196608;      // presence bytes only: 192 KB
 constexpr int kDenseThreads = 512;
 
 __device__ __forceinline__ void raise_status(int *st, int word) { atomicOr(st + word, 1); }
@@ -274,6 +274,107 @@ __global__ void __launch_bounds__(256) k_tiny(DevCsr A, DevCsr B, DevCsr C, cons
 }
 
 // ------------------------------------------------------------------------
+// product stream shared by the hash and dense bins
+// ------------------------------------------------------------------------
+//
+// A CTA walks one A row in chunks of kChunk entries.  For a chunk it stages
+// in shared memory, per entry t: pre[t] (first flattened product index),
+// bs[t] (first B position) and va[t] (the A value); then the flattened
+// products pre[0] .. pre[cnt] are split into one contiguous range per warp
+// and lane l of a warp visits products base + l, base + 32 + l, ...  Every
+// lane is busy whatever the B row lengths, consecutive lanes read
+// consecutive B positions (coalesced), and four products are loaded before
+// any is consumed so four loads per lane are in flight.
+
+constexpr int kChunk = 512;
+
+template <typename V>
+struct ChunkStage {
+    int64_t pre[kChunk + 1];
+    int64_t bs[kChunk];
+    V va[kChunk];
+    int64_t warp_tot[32];
+};
+
+// Block-wide exclusive scan of kChunk int64 lengths held kChunk/NT per thread.
+template <int NT>
+__device__ __forceinline__ void stage_scan(int64_t (&len)[kChunk / NT], int64_t *pre, int64_t *warp_tot) {
+    constexpr int IPT = kChunk / NT;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int64_t mine = 0;
+#pragma unroll
+    for (int i = 0; i < IPT; i++) mine += len[i];
+    int64_t incl = mine;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int64_t o = __shfl_up_sync(kFull, incl, d);
+        if (lane >= d) incl += o;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    int64_t base = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < NT / 32; w++) {
+        const int64_t t = warp_tot[w];
+        if (w < warp) base += t;
+        total += t;
+    }
+    int64_t run = base + incl - mine;
+#pragma unroll
+    for (int i = 0; i < IPT; i++) {
+        pre[threadIdx.x * IPT + i] = run;
+        run += len[i];
+    }
+    if (threadIdx.x == 0) pre[kChunk] = total;
+    __syncthreads();
+}
+
+// Visits every staged product of the chunk: visit(col, product value).
+template <int NT, typename V, bool NUMERIC, typename Visit>
+__device__ __forceinline__ void stream_chunk(const ChunkStage<V> &sg, int cnt, const DevCsr B, int *st,
+                                             Visit visit) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int NW = NT / 32;
+    const int64_t total = sg.pre[cnt];
+    if (total == 0) return;
+    const int64_t per = (((total + NW - 1) / NW) + 31) & ~(int64_t)31;
+    const int64_t pbeg = (int64_t)warp * per;
+    const int64_t pend = min(pbeg + per, total);
+    if (pbeg >= pend) return;
+    // k = last staged entry with pre[k] <= p (entries with no products are skipped)
+    int64_t p0 = min(pbeg + lane, pend - 1);
+    int lo = 0, hi = cnt - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sg.pre[mid] <= p0) lo = mid;
+        else hi = mid - 1;
+    }
+    int k = lo;
+    const V *Bval = (const V *)B.val;
+    for (int64_t base = pbeg; base < pend; base += 128) {
+        int32_t c[4];
+        V pv[4];
+        bool ok[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int64_t p = base + u * 32 + lane;
+            ok[u] = p < pend;
+            c[u] = 0;
+            pv[u] = 0;
+            if (ok[u]) {
+                while (sg.pre[k + 1] <= p) k++;
+                const int64_t q = sg.bs[k] + (p - sg.pre[k]);
+                c[u] = B.col[q];
+                if (NUMERIC) pv[u] = mul_chk(sg.va[k], Bval[q], st);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (ok[u]) visit(c[u], pv[u]);
+    }
+}
+
+// ------------------------------------------------------------------------
 // hash bins: one CTA per row, shared-memory linear probing
 // ------------------------------------------------------------------------
 
@@ -329,6 +430,28 @@ __device__ __forceinline__ int block_excl_scan(int v, int *excl, int *s_warp) {
     return total;
 }
 
+// Stages entries [k0, k0 + cnt) of an A row with their whole B rows.
+template <int NT, typename V, bool NUMERIC>
+__device__ __forceinline__ void stage_full_rows(ChunkStage<V> &sg, const DevCsr A, const DevCsr B, int64_t k0,
+                                                int cnt) {
+    constexpr int IPT = kChunk / NT;
+    int64_t len[IPT];
+    const V *Aval = (const V *)A.val;
+#pragma unroll
+    for (int i = 0; i < IPT; i++) {
+        const int t = threadIdx.x * IPT + i;
+        len[i] = 0;
+        if (t < cnt) {
+            const int32_t a = A.col[k0 + t];
+            const int64_t b0 = B.rowptr[a];
+            len[i] = B.rowptr[a + 1] - b0;
+            sg.bs[t] = b0;
+            if (NUMERIC) sg.va[t] = Aval[k0 + t];
+        }
+    }
+    stage_scan<NT>(len, sg.pre, sg.warp_tot);
+}
+
 template <typename V, bool NUMERIC, int S, int NT>
 __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows, int32_t nrows,
                                              int64_t *cnt, int *st) {
@@ -337,10 +460,9 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
     V *vals = (V *)(keys + S);
     int32_t *sk = (int32_t *)(vals + (NUMERIC ? S : 0));
     V *sv = (V *)(sk + S / 2);
+    __shared__ ChunkStage<V> sg;
     __shared__ int s_warp[NT / 32];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const V *Aval = (const V *)A.val;
-    const V *Bval = (const V *)B.val;
+    const int tid = threadIdx.x;
     for (int32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
         const int32_t r = rows[ri];
         const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
@@ -350,17 +472,14 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
         }
         __syncthreads();
         int fresh = 0;
-        for (int64_t k = a0 + warp; k < a1; k += NT / 32) {
-            const int32_t a = A.col[k];
-            const V va = NUMERIC ? Aval[k] : (V)0;
-            const int64_t bs = B.rowptr[a], be = B.rowptr[a + 1];
-            for (int64_t q = bs + lane; q < be; q += 32) {
-                const int32_t c = B.col[q];
-                const V p = NUMERIC ? mul_chk(va, Bval[q], st) : (V)0;
+        for (int64_t k0 = a0; k0 < a1; k0 += kChunk) {
+            const int n = (int)(a1 - k0 < (int64_t)kChunk ? a1 - k0 : (int64_t)kChunk);
+            stage_full_rows<NT, V, NUMERIC>(sg, A, B, k0, n);
+            stream_chunk<NT, V, NUMERIC>(sg, n, B, st, [&](int32_t c, V p) {
                 fresh += hash_insert<V, NUMERIC, S>(keys, vals, c, p, st);
-            }
+            });
+            __syncthreads();
         }
-        __syncthreads();
         if (!NUMERIC) {
             int excl;
             const int total = block_excl_scan<NT>(fresh, &excl, s_warp);
@@ -417,27 +536,37 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
 }
 
 // ------------------------------------------------------------------------
-// dense bin: one CTA per row, windowed bitmap + counters in shared memory
+// dense bin: one CTA per row, windowed presence bytes + counters in shared memory
 // ------------------------------------------------------------------------
+//
+// Presence is a byte per column written with plain stores (no read-modify-
+// write, so lanes hitting neighbouring columns never contend); counters are
+// shared-memory atomics.  Output columns of a window are emitted 32 at a time
+// with a ballot over the presence bytes, so global stores are coalesced.  A
+// row wider than one window is processed window by window: per A entry the
+// staging step finds the part of its (sorted) B row inside the window by a
+// binary search from a per-entry cursor and records where the next window
+// starts; the next window is the one holding the smallest remaining column.
 
 template <typename V, bool NUMERIC>
 __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows,
                                                          int32_t nrows, int64_t *cnt, int32_t *cursors,
                                                          int64_t cur_stride, int32_t W, int *st) {
+    constexpr int NT = kDenseThreads;
+    constexpr int IPT = kChunk / NT;
     extern __shared__ __align__(16) unsigned char smem[];
-    const int nwords = W >> 5;
-    uint32_t *bm = (uint32_t *)smem;
-    V *acc = (V *)(smem + (((size_t)nwords * 4 + 15) & ~(size_t)15));
-    __shared__ int64_t s_warp[32];
+    uint8_t *present = smem;
+    V *acc = (V *)(smem + (((size_t)W + 15) & ~(size_t)15));
+    __shared__ ChunkStage<V> sg;
+    __shared__ int64_t s_warp[NT / 32];
     __shared__ int32_t s_next;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int nwarps = blockDim.x >> 5;
+    constexpr int NW = NT / 32;
     const unsigned lt_mask = (1u << lane) - 1u;
     const V *Aval = (const V *)A.val;
-    const V *Bval = (const V *)B.val;
-    for (int i = tid; i < nwords; i += blockDim.x) bm[i] = 0;
+    for (int i = tid; i < W / 16; i += NT) ((uint4 *)present)[i] = make_uint4(0, 0, 0, 0);
     if (NUMERIC)
-        for (int i = tid; i < W; i += blockDim.x) acc[i] = 0;
+        for (int i = tid; i < W; i += NT) acc[i] = 0;
     const bool multi = B.cols > W;
     int32_t *cur = multi ? cursors + (int64_t)blockIdx.x * cur_stride : nullptr;
     __syncthreads();
@@ -453,78 +582,91 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
         while (true) {
             const int64_t w1 = min(w0 + (int64_t)W, B.cols);
             if (tid == 0) s_next = INT_MAX;
-            __syncthreads();
             int32_t my_next = INT_MAX;
-            for (int64_t k = a0 + warp; k < a1; k += nwarps) {
-                const int32_t a = A.col[k];
-                const V va = NUMERIC ? Aval[k] : (V)0;
-                const int64_t bs = B.rowptr[a], be = B.rowptr[a + 1];
-                int64_t q0 = (multi && !first) ? bs + cur[k - a0] : bs;
-                int64_t stop = be;
-                for (; q0 < be; q0 += 32) {
-                    const int64_t q = q0 + lane;
-                    const bool valid = q < be;
-                    const int32_t c = valid ? B.col[q] : INT_MAX;
-                    if (valid && c < w1) {
-                        const int32_t lc = (int32_t)(c - w0);
-                        atomicOr(bm + (lc >> 5), 1u << (lc & 31));
-                        if (NUMERIC) add_shared_chk(acc + lc, mul_chk(va, Bval[q], st), st);
-                    }
-                    const unsigned beyond = __ballot_sync(kFull, valid && c >= w1);
-                    if (beyond) {
-                        const int src = __ffs(beyond) - 1;
-                        stop = q0 + src;
-                        my_next = min(my_next, __shfl_sync(kFull, c, src));
-                        break;
+            for (int64_t k0 = a0; k0 < a1; k0 += kChunk) {
+                const int n = (int)(a1 - k0 < (int64_t)kChunk ? a1 - k0 : (int64_t)kChunk);
+                int64_t len[IPT];
+#pragma unroll
+                for (int i = 0; i < IPT; i++) {
+                    const int t = tid * IPT + i;
+                    len[i] = 0;
+                    if (t < n) {
+                        const int64_t k = k0 + t;
+                        const int32_t a = A.col[k];
+                        const int64_t bs = B.rowptr[a], be = B.rowptr[a + 1];
+                        int64_t lo = bs, hi = be;
+                        if (multi) {
+                            if (!first) lo = bs + cur[k - a0];
+                            // first position with column >= w1
+                            int64_t L = lo, R = be;
+                            while (L < R) {
+                                const int64_t mid = (L + R) >> 1;
+                                if (B.col[mid] < w1) L = mid + 1;
+                                else R = mid;
+                            }
+                            hi = L;
+                            cur[k - a0] = (int32_t)(hi - bs);
+                            if (hi < be) my_next = min(my_next, B.col[hi]);
+                        }
+                        len[i] = hi - lo;
+                        sg.bs[t] = lo;
+                        if (NUMERIC) sg.va[t] = Aval[k];
                     }
                 }
-                if (multi && lane == 0) cur[k - a0] = (int32_t)(stop - bs);
+                stage_scan<NT>(len, sg.pre, sg.warp_tot);
+                stream_chunk<NT, V, NUMERIC>(sg, n, B, st, [&](int32_t c, V p) {
+                    const int32_t lc = (int32_t)(c - w0);
+                    present[lc] = 1;
+                    if (NUMERIC) add_shared_chk(acc + lc, p, st);
+                });
+                __syncthreads();
             }
             if (multi) {
                 my_next = warp_min(my_next);
                 if (lane == 0 && my_next != INT_MAX) atomicMin(&s_next, my_next);
             }
-            __syncthreads();
-            // count the window, warps own contiguous word ranges
-            const int win_words = (int)((w1 - w0 + 31) >> 5);
-            const int chunk = (win_words + nwarps - 1) / nwarps;
-            const int wb = min(warp * chunk, win_words), we = min(wb + chunk, win_words);
+            // count the window: warps own contiguous ranges of 32-column groups
+            const int groups = (int)((w1 - w0 + 31) >> 5);
+            const int chunk = (groups + NW - 1) / NW;
+            const int gb = min(warp * chunk, groups), ge = min(gb + chunk, groups);
             int64_t c_w = 0;
-            for (int i = wb + lane; i < we; i += 32) {
-                c_w += __popc(bm[i]);
-                if (!NUMERIC) bm[i] = 0;
+            for (int g = gb + lane; g < ge; g += 32) {
+                const uint4 x = ((const uint4 *)present)[2 * g];
+                const uint4 y = ((const uint4 *)present)[2 * g + 1];
+                c_w += __popc(x.x & 0x01010101u) + __popc(x.y & 0x01010101u) + __popc(x.z & 0x01010101u) +
+                       __popc(x.w & 0x01010101u) + __popc(y.x & 0x01010101u) + __popc(y.y & 0x01010101u) +
+                       __popc(y.z & 0x01010101u) + __popc(y.w & 0x01010101u);
+                if (!NUMERIC) {
+                    ((uint4 *)present)[2 * g] = make_uint4(0, 0, 0, 0);
+                    ((uint4 *)present)[2 * g + 1] = make_uint4(0, 0, 0, 0);
+                }
             }
             c_w = warp_sum(c_w);
             if (lane == 0) s_warp[warp] = c_w;
             __syncthreads();
             int64_t base = 0, wtot = 0;
-            for (int w = 0; w < nwarps; w++) {
+#pragma unroll
+            for (int w = 0; w < NW; w++) {
                 const int64_t t = s_warp[w];
                 if (w < warp) base += t;
                 wtot += t;
             }
             if (NUMERIC) {
                 int64_t pos = out + base;
-                for (int i0 = wb; i0 < we; i0 += 32) {
-                    const int i = i0 + lane;
-                    const uint32_t word = i < we ? bm[i] : 0u;
-                    unsigned nz = __ballot_sync(kFull, word != 0);
-                    while (nz) {
-                        const int src = __ffs(nz) - 1;
-                        nz &= nz - 1;
-                        const uint32_t bits = __shfl_sync(kFull, word, src);
-                        if ((bits >> lane) & 1u) {
-                            const int64_t o = pos + __popc(bits & lt_mask);
-                            const int lc = (i0 + src) * 32 + lane;
-                            if (o < row_end) {
-                                C.col[o] = (int32_t)(w0 + lc);
-                                ((V *)C.val)[o] = acc[lc];
-                            }
-                            acc[lc] = 0;
+                for (int g = gb; g < ge; g++) {
+                    const int lc = g * 32 + lane;
+                    const bool here = present[lc] != 0;
+                    const unsigned bits = __ballot_sync(kFull, here);
+                    if (here) {
+                        const int64_t o = pos + __popc(bits & lt_mask);
+                        if (o < row_end) {
+                            C.col[o] = (int32_t)(w0 + lc);
+                            ((V *)C.val)[o] = acc[lc];
                         }
-                        pos += __popc(bits);
+                        acc[lc] = 0;
+                        present[lc] = 0;
                     }
-                    if (i < we) bm[i] = 0;
+                    pos += __popc(bits);
                 }
             }
             out += wtot;
@@ -648,6 +790,11 @@ __global__ void k_sum_touched(DevCsr B, const uint8_t *mark, unsigned long long 
     }
 }
 
+__global__ void k_widen(const uint32_t *src, uint64_t *dst, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
 template <typename V>
 __global__ void k_fill_ones(V *v, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -714,8 +861,8 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
             case kBinDense: {
                 const int64_t wmax = NUMERIC ? (sizeof(V) == 4 ? kDenseWinU32 : kDenseWinU64) : kDenseWinSym;
                 const int64_t W = std::min<int64_t>(wmax, (ncols + 31) / 32 * 32);
-                const int64_t bm_bytes = ((W / 32) * 4 + 15) & ~15LL;
-                const int64_t sm = bm_bytes + (NUMERIC ? W * (int64_t)sizeof(V) : 0);
+                const int64_t pres_bytes = (W + 15) & ~15LL;
+                const int64_t sm = pres_bytes + (NUMERIC ? W * (int64_t)sizeof(V) : 0);
                 auto kern = k_dense<V, NUMERIC>;
                 RMCM_TRY(set_smem(h, kern, sm));
                 int per_sm = (int)std::max<int64_t>(1, std::min<int64_t>(4, (200 * 1024) / std::max<int64_t>(sm, 1)));
@@ -812,43 +959,44 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     memcpy(&flops_total, (int32_t *)h->h_pinned + 32, sizeof(int64_t));
     if (flops_out) *flops_out = flops_total;
 
-    // cursor scratch for multi-window dense rows
-    const int64_t wsym = kDenseWinSym, wnum = sizeof(V) == 4 ? kDenseWinU32 : kDenseWinU64;
+    // Cursor buffer for multi-window dense rows.  It is a separate allocation:
+    // growing the scratch area here would move the row lists built above.
+    const int64_t wnum = sizeof(V) == 4 ? kDenseWinU32 : kDenseWinU64;
     int64_t cursor_cap = 0;
+    int32_t *cursors = nullptr;
     if (counts[kBinDense] > 0 && B.cols > wnum) {
-        const int64_t want = (int64_t)h->sm_count * 4 * std::max<int32_t>(dense_max_alen, 1);
-        cursor_cap = std::min<int64_t>(want, std::max<int64_t>(dense_max_alen, 1) * 1024);
-        need = o_cur + al(4 * cursor_cap);
-        RMCM_TRY(scratch_reserve(h, need));
-        sc = (char *)h->scratch;
-        flops = (int64_t *)(sc + o_flops);
-        cnt = (int64_t *)(sc + o_cnt);
-        tiles = (int64_t *)(sc + o_tiles);
-        lists = (int32_t *)(sc + o_lists);
+        const int64_t stride = std::max<int32_t>(dense_max_alen, 1);
+        cursor_cap = stride * std::min<int64_t>((int64_t)h->sm_count * 4, 1024);
+        RMCM_TRY(dev_alloc(h, (void **)&cursors, 4 * cursor_cap));
     }
-    (void)wsym;
-    int32_t *cursors = (int32_t *)(sc + o_cur);
+    auto drop_cursors = [&]() {
+        if (cursors) dev_free(h, cursors, 4 * cursor_cap);
+        cursors = nullptr;
+    };
 
     // symbolic
     rmcm_mat *C = nullptr;
-    RMCM_TRY(mat_alloc(h, m, B.cols, -1, Am->valtype, &C));
-    if (rec) RMCM_CUDA(h, cudaEventRecord(h->prof[rec_idx].ev[2], s));
-    RMCM_TRY((launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap)));
-    RMCM_TRY(scan_rowptr(h, cnt, m, C->d.rowptr, tiles));
-    if (rec) RMCM_CUDA(h, cudaEventRecord(h->prof[rec_idx].ev[3], s));
-    // nnz and the total flops to the host
-    int64_t *hp = h->h_pinned;
-    RMCM_CUDA(h, cudaMemcpyAsync(hp, C->d.rowptr + m, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    RMCM_CUDA(h, cudaStreamSynchronize(s));
-    const int64_t nnz = hp[0];
-    // allocate the output arrays
-    int32_t rc = mat_alloc(h, m, B.cols, nnz, Am->valtype, &C);
+    int32_t rc = mat_alloc(h, m, B.cols, -1, Am->valtype, &C);
     if (rc != RMCM_OK) {
-        mat_release(h, C);
+        drop_cursors();
         return rc;
     }
-    if (rec) RMCM_CUDA(h, cudaEventRecord(h->prof[rec_idx].ev[4], s));
-    rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap);
+    if (rec) cudaEventRecord(h->prof[rec_idx].ev[2], s);
+    rc = launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap);
+    if (rc == RMCM_OK) rc = scan_rowptr(h, cnt, m, C->d.rowptr, tiles);
+    if (rec) cudaEventRecord(h->prof[rec_idx].ev[3], s);
+    // nnz to the host, then the output arrays
+    int64_t *hp = h->h_pinned;
+    if (rc == RMCM_OK) {
+        cudaError_t e = cudaMemcpyAsync(hp, C->d.rowptr + m, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = cuda_error(h, e, "spgemm nnz download");
+    }
+    const int64_t nnz = hp[0];
+    if (rc == RMCM_OK) rc = mat_alloc(h, m, B.cols, nnz, Am->valtype, &C);
+    if (rec) cudaEventRecord(h->prof[rec_idx].ev[4], s);
+    if (rc == RMCM_OK) rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap);
+    drop_cursors();
     if (rc != RMCM_OK) {
         mat_release(h, C);
         return rc;
@@ -912,6 +1060,29 @@ int32_t spgemm(rmcm_handle *h, const rmcm_mat *A, const rmcm_mat *B, rmcm_mat **
     if (A->valtype != B->valtype) return set_error(h, RMCM_EINVAL, "spgemm: value types differ");
     if (A->valtype == RMCM_VAL_U64) return spgemm_t<uint64_t>(h, A, B, C, flops_out);
     return spgemm_t<uint32_t>(h, A, B, C, flops_out);
+}
+
+int32_t convert_values(rmcm_handle *h, const rmcm_mat *src, int32_t valtype, rmcm_mat **out) {
+    if (src->valtype != RMCM_VAL_U32 || valtype != RMCM_VAL_U64)
+        return set_error(h, RMCM_EINVAL, "convert: only uint32 -> uint64 widening is supported");
+    rmcm_mat *m = nullptr;
+    RMCM_TRY(mat_alloc(h, src->d.rows, src->d.cols, src->d.nnz, valtype, &m));
+    cudaStream_t s = h->stream;
+    cudaError_t e = cudaMemcpyAsync(m->d.rowptr, src->d.rowptr, 8 * (src->d.rows + 1), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && src->d.nnz)
+        e = cudaMemcpyAsync(m->d.col, src->d.col, 4 * src->d.nnz, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && src->d.nnz) {
+        k_widen<<<grid_for(h, src->d.nnz, 256, 8), 256, 0, s>>>((const uint32_t *)src->d.val, (uint64_t *)m->d.val,
+                                                                 src->d.nnz);
+        h->launches++;
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+        mat_release(h, m);
+        return cuda_error(h, e, "convert");
+    }
+    *out = m;
+    return RMCM_OK;
 }
 
 int32_t fill_ones(rmcm_handle *h, void *val, int64_t nnz, int32_t valtype) {
