@@ -32,6 +32,8 @@
 #include <climits>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 
 #include "internal.h"
 
@@ -49,30 +51,25 @@ constexpr int kDenseThreads = 512;
 
 __device__ __forceinline__ void raise_status(int *st, int word) { atomicOr(st + word, 1); }
 
-__device__ __forceinline__ uint32_t mul_chk(uint32_t a, uint32_t b, int *st) {
-    unsigned long long p = (unsigned long long)a * b;
-    if (p > 0xffffffffull) raise_status(st, kOverflow);
+// Overflow of a product or a sum is recorded in a per-thread flag and flushed
+// to the kOverflow status word once per warp or CTA (a global atomic per
+// overflowing add would serialise the whole GPU on one address).
+__device__ __forceinline__ uint32_t mul_chk(uint32_t a, uint32_t b, bool &ovf) {
+    const unsigned long long p = (unsigned long long)a * b;
+    ovf |= p > 0xffffffffull;
     return (uint32_t)p;
 }
-__device__ __forceinline__ uint64_t mul_chk(uint64_t a, uint64_t b, int *st) {
-    if (__umul64hi(a, b) != 0) raise_status(st, kOverflow);
+__device__ __forceinline__ uint64_t mul_chk(uint64_t a, uint64_t b, bool &ovf) {
+    ovf |= __umul64hi(a, b) != 0;
     return a * b;
 }
-__device__ __forceinline__ void add_shared_chk(uint32_t *p, uint32_t v, int *st) {
-    uint32_t old = atomicAdd(p, v);
-    if (old > 0xffffffffu - v) raise_status(st, kOverflow);
+__device__ __forceinline__ void add_shared_chk(uint32_t *p, uint32_t v, bool &ovf) {
+    const uint32_t old = atomicAdd(p, v);
+    ovf |= old > 0xffffffffu - v;
 }
-__device__ __forceinline__ void add_shared_chk(uint64_t *p, uint64_t v, int *st) {
-    unsigned long long old = atomicAdd((unsigned long long *)p, (unsigned long long)v);
-    if (old > ~0ull - v) raise_status(st, kOverflow);
-}
-__device__ __forceinline__ uint32_t add_chk(uint32_t a, uint32_t b, int *st) {
-    if (a > 0xffffffffu - b) raise_status(st, kOverflow);
-    return a + b;
-}
-__device__ __forceinline__ uint64_t add_chk(uint64_t a, uint64_t b, int *st) {
-    if (a > ~0ull - b) raise_status(st, kOverflow);
-    return a + b;
+__device__ __forceinline__ void add_shared_chk(uint64_t *p, uint64_t v, bool &ovf) {
+    const unsigned long long old = atomicAdd((unsigned long long *)p, (unsigned long long)v);
+    ovf |= old > ~0ull - v;
 }
 
 template <typename T>
@@ -171,6 +168,7 @@ __global__ void __launch_bounds__(256) k_tiny(DevCsr A, DevCsr B, DevCsr C, cons
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const V *Aval = (const V *)A.val;
     const V *Bval = (const V *)B.val;
+    bool ovf = false;
     for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nrows; w += nwarps) {
         const int32_t r = rows[w];
         const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
@@ -218,12 +216,8 @@ __global__ void __launch_bounds__(256) k_tiny(DevCsr A, DevCsr B, DevCsr C, cons
                 key = B.col[q];
                 if (NUMERIC) {
                     const unsigned long long vb = Bval[q];
-                    if (sizeof(V) == 4) {
-                        val = sva * vb;
-                    } else {
-                        if (__umul64hi(sva, vb) != 0) raise_status(st, kOverflow);
-                        val = sva * vb;
-                    }
+                    if (sizeof(V) != 4) ovf |= __umul64hi(sva, vb) != 0;
+                    val = sva * vb;
                 }
             }
             filled += tot;
@@ -254,11 +248,11 @@ __global__ void __launch_bounds__(256) k_tiny(DevCsr A, DevCsr B, DevCsr C, cons
                 const unsigned long long o = __shfl_down_sync(kFull, s, d);
                 const int32_t okey = __shfl_down_sync(kFull, key, d);
                 if (lane + d < 32 && okey == key) {
-                    if (s > ~0ull - o) raise_status(st, kOverflow);
+                    ovf |= s > ~0ull - o;
                     s += o;
                 }
             }
-            if (sizeof(V) == 4 && head && s > 0xffffffffull) raise_status(st, kOverflow);
+            if (sizeof(V) == 4 && head) ovf |= s > 0xffffffffull;
             const int64_t base = C.rowptr[r];
             const int64_t rlen = C.rowptr[r + 1] - base;
             if (lane == 0 && rlen != __popc(heads)) raise_status(st, kInvariant);
@@ -271,6 +265,7 @@ __global__ void __launch_bounds__(256) k_tiny(DevCsr A, DevCsr B, DevCsr C, cons
             }
         }
     }
+    if (__any_sync(kFull, ovf) && lane == 0) raise_status(st, kOverflow);
 }
 
 // ------------------------------------------------------------------------
@@ -331,7 +326,7 @@ __device__ __forceinline__ void stage_scan(int64_t (&len)[kChunk / NT], int64_t 
 
 // Visits every staged product of the chunk: visit(col, product value).
 template <int NT, typename V, bool NUMERIC, typename Visit>
-__device__ __forceinline__ void stream_chunk(const ChunkStage<V> &sg, int cnt, const DevCsr B, int *st,
+__device__ __forceinline__ void stream_chunk(const ChunkStage<V> &sg, int cnt, const DevCsr B, bool &ovf,
                                              Visit visit) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     constexpr int NW = NT / 32;
@@ -365,7 +360,7 @@ __device__ __forceinline__ void stream_chunk(const ChunkStage<V> &sg, int cnt, c
                 while (sg.pre[k + 1] <= p) k++;
                 const int64_t q = sg.bs[k] + (p - sg.pre[k]);
                 c[u] = B.col[q];
-                if (NUMERIC) pv[u] = mul_chk(sg.va[k], Bval[q], st);
+                if (NUMERIC) pv[u] = mul_chk(sg.va[k], Bval[q], ovf);
             }
         }
 #pragma unroll
@@ -385,18 +380,18 @@ __device__ __forceinline__ uint32_t hash_slot(int32_t c) {
 }
 
 template <typename V, bool NUMERIC, int S>
-__device__ __forceinline__ int hash_insert(int32_t *keys, V *vals, int32_t c, V p, int *st) {
+__device__ __forceinline__ int hash_insert(int32_t *keys, V *vals, int32_t c, V p, int *st, bool &ovf) {
     uint32_t h = hash_slot<S>(c);
     for (int probe = 0; probe < S; probe++) {
         const int32_t k = ((volatile int32_t *)keys)[h];
         if (k == c) {
-            if (NUMERIC) add_shared_chk(vals + h, p, st);
+            if (NUMERIC) add_shared_chk(vals + h, p, ovf);
             return 0;
         }
         if (k == -1) {
             const int32_t old = atomicCAS(keys + h, -1, c);
             if (old == -1 || old == c) {
-                if (NUMERIC) add_shared_chk(vals + h, p, st);
+                if (NUMERIC) add_shared_chk(vals + h, p, ovf);
                 return old == -1;
             }
         }
@@ -463,6 +458,7 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
     __shared__ ChunkStage<V> sg;
     __shared__ int s_warp[NT / 32];
     const int tid = threadIdx.x;
+    bool ovf = false;
     for (int32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
         const int32_t r = rows[ri];
         const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
@@ -475,8 +471,8 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
         for (int64_t k0 = a0; k0 < a1; k0 += kChunk) {
             const int n = (int)(a1 - k0 < (int64_t)kChunk ? a1 - k0 : (int64_t)kChunk);
             stage_full_rows<NT, V, NUMERIC>(sg, A, B, k0, n);
-            stream_chunk<NT, V, NUMERIC>(sg, n, B, st, [&](int32_t c, V p) {
-                fresh += hash_insert<V, NUMERIC, S>(keys, vals, c, p, st);
+            stream_chunk<NT, V, NUMERIC>(sg, n, B, ovf, [&](int32_t c, V p) {
+                fresh += hash_insert<V, NUMERIC, S>(keys, vals, c, p, st, ovf);
             });
             __syncthreads();
         }
@@ -533,6 +529,7 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
         }
         __syncthreads();
     }
+    if (__syncthreads_or(ovf) && tid == 0) raise_status(st, kOverflow);
 }
 
 // ------------------------------------------------------------------------
@@ -569,6 +566,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
         for (int i = tid; i < W; i += NT) acc[i] = 0;
     const bool multi = B.cols > W;
     int32_t *cur = multi ? cursors + (int64_t)blockIdx.x * cur_stride : nullptr;
+    bool ovf = false;
     __syncthreads();
     for (int32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
         const int32_t r = rows[ri];
@@ -614,10 +612,10 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                     }
                 }
                 stage_scan<NT>(len, sg.pre, sg.warp_tot);
-                stream_chunk<NT, V, NUMERIC>(sg, n, B, st, [&](int32_t c, V p) {
+                stream_chunk<NT, V, NUMERIC>(sg, n, B, ovf, [&](int32_t c, V p) {
                     const int32_t lc = (int32_t)(c - w0);
                     present[lc] = 1;
-                    if (NUMERIC) add_shared_chk(acc + lc, p, st);
+                    if (NUMERIC) add_shared_chk(acc + lc, p, ovf);
                 });
                 __syncthreads();
             }
@@ -682,6 +680,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
             else if (total != row_end - row_base) raise_status(st, kInvariant);
         }
     }
+    if (__syncthreads_or(ovf) && tid == 0) raise_status(st, kOverflow);
 }
 
 // ------------------------------------------------------------------------
@@ -809,9 +808,19 @@ int grid_for(rmcm_handle *h, int64_t work, int threads, int per_sm) {
     return (int)g;
 }
 
+// Opt a kernel in to `bytes` of dynamic shared memory (static shared memory
+// counts against the same 48 KB default, so the attribute is set whenever the
+// request is non-zero and above what this kernel was last given).
 template <typename F>
 int32_t set_smem(rmcm_handle *h, F *kernel, int64_t bytes) {
-    if (bytes > 48 * 1024) RMCM_CUDA(h, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, int64_t> given;
+    std::lock_guard<std::mutex> lock(mu);
+    auto key = std::make_pair(h->device, (const void *)kernel);
+    auto it = given.find(key);
+    if (it != given.end() && it->second >= bytes) return RMCM_OK;
+    RMCM_CUDA(h, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    given[key] = bytes;
     return RMCM_OK;
 }
 
