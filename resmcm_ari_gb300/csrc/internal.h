@@ -48,6 +48,8 @@ struct Tuning {
     int32_t dense_ratio = 16;       // dense when flops * dense_ratio >= cols (and one window covers cols)
     int32_t dense_threads = 256;
     double hash_load = 0.5;         // hash table load factor bound: slots >= min(f, cols) / load
+    bool dense_single_pass = true;  // dense rows in one window: one pass into a padded temporary
+    int64_t dense_temp_max_bytes = 8LL << 30;
 };
 
 // One profiled product: stats plus the six events that bracket its passes

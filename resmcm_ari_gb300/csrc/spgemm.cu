@@ -545,10 +545,15 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
 // binary search from a per-entry cursor and records where the next window
 // starts; the next window is the one holding the smallest remaining column.
 
-template <typename V, bool NUMERIC>
+//
+// TEMP mode (numeric, single window only): row ri of the bin list is written
+// to slot ri of a row-padded temporary (C.col / C.val point at it, slot
+// stride `tstride` entries) and its length goes to cnt[r]; the symbolic pass
+// is skipped for these rows and k_copy_rows compacts the slots into C.
+template <typename V, bool NUMERIC, bool TEMP>
 __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows,
                                                          int32_t nrows, int64_t *cnt, int32_t *cursors,
-                                                         int64_t cur_stride, int32_t W, int *st) {
+                                                         int64_t cur_stride, int32_t W, int *st, int64_t tstride) {
     constexpr int NT = kDenseThreads;
     constexpr int IPT = kChunk / NT;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -571,8 +576,8 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
     for (int32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
         const int32_t r = rows[ri];
         const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
-        const int64_t row_base = NUMERIC ? C.rowptr[r] : 0;
-        const int64_t row_end = NUMERIC ? C.rowptr[r + 1] : 0;
+        const int64_t row_base = TEMP ? (int64_t)ri * tstride : (NUMERIC ? C.rowptr[r] : 0);
+        const int64_t row_end = TEMP ? row_base + tstride : (NUMERIC ? C.rowptr[r + 1] : 0);
         int64_t out = row_base;
         int64_t total = 0;
         int64_t w0 = 0;
@@ -676,11 +681,28 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
             first = false;
         }
         if (tid == 0) {
-            if (!NUMERIC) cnt[r] = total;
+            if (!NUMERIC || TEMP) cnt[r] = total;
             else if (total != row_end - row_base) raise_status(st, kInvariant);
         }
     }
     if (__syncthreads_or(ovf) && tid == 0) raise_status(st, kOverflow);
+}
+
+// Compacts TEMP-mode slots into C: row rows[ri] has cnt = rowptr[r+1]-rowptr[r]
+// entries at slot ri of the temporary.
+template <typename V>
+__global__ void __launch_bounds__(256) k_copy_rows(const int32_t *rows, int32_t nrows, DevCsr C, const int32_t *tcol,
+                                                   const V *tval, int64_t tstride) {
+    for (int32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
+        const int32_t r = rows[ri];
+        const int64_t b = C.rowptr[r], n = C.rowptr[r + 1] - b;
+        const int32_t *sc = tcol + (int64_t)ri * tstride;
+        const V *sv = tval + (int64_t)ri * tstride;
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+            C.col[b + i] = sc[i];
+            ((V *)C.val)[b + i] = sv[i];
+        }
+    }
 }
 
 // ------------------------------------------------------------------------
@@ -824,10 +846,19 @@ int32_t set_smem(rmcm_handle *h, F *kernel, int64_t bytes) {
     return RMCM_OK;
 }
 
+// Row-padded temporary of the single-pass dense rows.
+struct DenseTemp {
+    bool active = false;
+    int32_t *col = nullptr;
+    void *val = nullptr;
+    int64_t stride = 0;
+    int64_t bytes = 0;
+};
+
 template <typename V, bool NUMERIC>
 int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevCsr &C, const int32_t *lists,
                     const int32_t *counts, int32_t dense_max_alen, int64_t *cnt, int32_t *cursor_base,
-                    int64_t cursor_cap) {
+                    int64_t cursor_cap, const DenseTemp *temp) {
     cudaStream_t s = h->stream;
     int *st = h->d_status;
     int32_t off = 0;
@@ -868,11 +899,32 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                 break;
             }
             case kBinDense: {
+                if (temp && temp->active) {
+                    if (!NUMERIC) {
+                        // one pass: columns + counts into the padded slots, lengths to cnt
+                        const int64_t W = (ncols + 31) / 32 * 32;
+                        const int64_t sm = ((W + 15) & ~15LL) + W * (int64_t)sizeof(V);
+                        auto kern = k_dense<V, true, true>;
+                        RMCM_TRY(set_smem(h, kern, sm));
+                        const int per_sm = (int)std::max<int64_t>(1, std::min<int64_t>(4, (200 * 1024) / std::max<int64_t>(sm, 1)));
+                        const int grid = (int)std::min<int64_t>((int64_t)n, (int64_t)h->sm_count * per_sm);
+                        DevCsr T = C;
+                        T.col = temp->col;
+                        T.val = temp->val;
+                        kern<<<grid, kDenseThreads, sm, s>>>(A, B, T, list, n, cnt, nullptr, 0, (int32_t)W, st,
+                                                             temp->stride);
+                    } else {
+                        const int grid = (int)std::min<int64_t>((int64_t)n, (int64_t)h->sm_count * 8);
+                        k_copy_rows<V><<<grid, 256, 0, s>>>(list, n, C, temp->col, (const V *)temp->val,
+                                                             temp->stride);
+                    }
+                    break;
+                }
                 const int64_t wmax = NUMERIC ? (sizeof(V) == 4 ? kDenseWinU32 : kDenseWinU64) : kDenseWinSym;
                 const int64_t W = std::min<int64_t>(wmax, (ncols + 31) / 32 * 32);
                 const int64_t pres_bytes = (W + 15) & ~15LL;
                 const int64_t sm = pres_bytes + (NUMERIC ? W * (int64_t)sizeof(V) : 0);
-                auto kern = k_dense<V, NUMERIC>;
+                auto kern = k_dense<V, NUMERIC, false>;
                 RMCM_TRY(set_smem(h, kern, sm));
                 int per_sm = (int)std::max<int64_t>(1, std::min<int64_t>(4, (200 * 1024) / std::max<int64_t>(sm, 1)));
                 int grid = (int)std::min<int64_t>((int64_t)n, (int64_t)h->sm_count * per_sm);
@@ -881,7 +933,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                 if (multi && (int64_t)grid * stride > cursor_cap) {
                     grid = (int)std::max<int64_t>(1, cursor_cap / stride);
                 }
-                kern<<<grid, kDenseThreads, sm, s>>>(A, B, C, list, n, cnt, cursor_base, stride, (int32_t)W, st);
+                kern<<<grid, kDenseThreads, sm, s>>>(A, B, C, list, n, cnt, cursor_base, stride, (int32_t)W, st, 0);
                 break;
             }
         }
@@ -982,16 +1034,41 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         if (cursors) dev_free(h, cursors, 4 * cursor_cap);
         cursors = nullptr;
     };
+    // Single-pass dense rows: when every dense row fits one numeric window,
+    // compute them once into a row-padded temporary (bounded in size).
+    DenseTemp dtemp;
+    if (counts[kBinDense] > 0 && B.cols <= wnum && h->tune.dense_single_pass) {
+        const int64_t stride = (B.cols + 3) & ~3LL;
+        const int64_t bytes = (int64_t)counts[kBinDense] * stride * (4 + (int64_t)sizeof(V));
+        const int64_t room = h->budget - h->in_use;
+        if (bytes <= h->tune.dense_temp_max_bytes && bytes < room / 2) {
+            void *p = nullptr;
+            if (dev_alloc(h, &p, bytes) == RMCM_OK) {
+                dtemp.active = true;
+                dtemp.col = (int32_t *)p;
+                dtemp.val = (char *)p + (int64_t)counts[kBinDense] * stride * 4;
+                dtemp.stride = stride;
+                dtemp.bytes = bytes;
+            } else {
+                h->last_error.clear();
+            }
+        }
+    }
+    auto drop_temp = [&]() {
+        if (dtemp.active) dev_free(h, dtemp.col, dtemp.bytes);
+        dtemp.active = false;
+    };
 
     // symbolic
     rmcm_mat *C = nullptr;
     int32_t rc = mat_alloc(h, m, B.cols, -1, Am->valtype, &C);
     if (rc != RMCM_OK) {
         drop_cursors();
+        drop_temp();
         return rc;
     }
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[2], s);
-    rc = launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap);
+    rc = launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap, &dtemp);
     if (rc == RMCM_OK) rc = scan_rowptr(h, cnt, m, C->d.rowptr, tiles);
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[3], s);
     // nnz to the host, then the output arrays
@@ -1004,8 +1081,9 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     const int64_t nnz = hp[0];
     if (rc == RMCM_OK) rc = mat_alloc(h, m, B.cols, nnz, Am->valtype, &C);
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[4], s);
-    if (rc == RMCM_OK) rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap);
+    if (rc == RMCM_OK) rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap, &dtemp);
     drop_cursors();
+    drop_temp();
     if (rc != RMCM_OK) {
         mat_release(h, C);
         return rc;
