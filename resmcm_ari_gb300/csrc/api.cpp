@@ -362,6 +362,7 @@ int32_t build_leaf(rmcm_handle *h, rmcm_graph *g, int32_t src, int32_t sink, int
 
 int32_t get_leaf(rmcm_handle *h, rmcm_graph *g, int32_t src, int32_t sink, int32_t et, int32_t valtype,
                  rmcm_mat **out) {
+    if (g->h != h) return set_error(h, RMCM_EINVAL, "graph belongs to another (or a destroyed) handle");
     if (src < 0 || src > g->max_vt || sink < 0 || sink > g->max_vt)
         return set_error(h, RMCM_EINVAL, "meta-path names a vertex type the graph does not have");
     auto key = std::make_tuple(src, sink, et, valtype);
@@ -675,6 +676,13 @@ RMCM_API int32_t rmcm_create(rmcm_handle **out, const rmcm_opts *opts) {
 
 RMCM_API int32_t rmcm_destroy(rmcm_handle *h) {
     if (!h) return RMCM_OK;
+    // graphs outliving their handle keep their host arrays only
+    for (rmcm_graph *g : h->graphs) {
+        for (auto &kv : g->leaves) mat_release(h, kv.second);
+        g->leaves.clear();
+        g->h = nullptr;
+    }
+    h->graphs.clear();
     for (auto &r : h->prof)
         for (auto &e : r.ev)
             if (e) cudaEventDestroy(e);
@@ -749,6 +757,7 @@ RMCM_API int32_t rmcm_graph_load_text(rmcm_handle *h, const char *graph_file, co
         delete g;
         return rc;
     }
+    h->graphs.insert(g);
     *out = g;
     return RMCM_OK;
 }
@@ -779,14 +788,18 @@ RMCM_API int32_t rmcm_graph_from_adjacency(rmcm_handle *h, int64_t n, const int3
         return set_error(h, RMCM_EINVAL, "graph: vertex type, row pointer or neighbour id out of range");
     }
     graph_finish(g);
+    h->graphs.insert(g);
     *out = g;
     return RMCM_OK;
 }
 
 RMCM_API int32_t rmcm_graph_free(rmcm_graph *g) {
     if (!g) return RMCM_OK;
-    for (auto &kv : g->leaves) mat_release(g->h, kv.second);
-    if (g->h && g->h->stream) cudaStreamSynchronize(g->h->stream);
+    if (g->h) {
+        for (auto &kv : g->leaves) mat_release(g->h, kv.second);
+        if (g->h->stream) cudaStreamSynchronize(g->h->stream);
+        g->h->graphs.erase(g);
+    }
     delete g;
     return RMCM_OK;
 }

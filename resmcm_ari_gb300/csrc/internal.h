@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <map>
+#include <set>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -88,6 +89,7 @@ struct rmcm_handle {
     rmcm::Tuning tune;
     int32_t prof_level = 0;
     std::vector<rmcm::ProdRecord> prof;
+    std::set<rmcm_graph *> graphs;   // graphs whose leaves live on this handle
 };
 
 struct rmcm_graph {

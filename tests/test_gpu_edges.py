@@ -207,3 +207,13 @@ def test_cli_output_line(native, tmp_path):
         parts = ln.split()
         assert len(parts) == 6
         [float(x) for x in parts[2:]]
+
+
+def test_graph_outliving_its_handle_is_safe(native):
+    """Destroying a handle first orphans its graphs; freeing them later is host-only."""
+    eng = native.Engine(device=0)
+    hg = native.HeteroGraph.from_synthetic(eng, synth.tiny_dblp())
+    C, _, _ = eng.run_metapath(hg, "1-3-0-0-1")
+    C.free()
+    eng.close()
+    hg.close()
