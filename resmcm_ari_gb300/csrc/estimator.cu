@@ -23,6 +23,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
+#include <mutex>
 #include <vector>
 
 #include "internal.h"
@@ -158,4 +160,115 @@ int32_t estimate(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, double *c_
     return RMCM_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// RES estimator for callers that cannot allocate device memory
+// ---------------------------------------------------------------------------
+//
+// Some callers of this library may not call cudaMalloc (or any allocating
+// routine) at the point where they need an estimate: a host framework that
+// owns every byte of device memory through its own pool and forbids plugins
+// from allocating behind its back, a latency-critical serving loop that
+// allows no allocation after start-up, or code that is recording a CUDA
+// stream into a graph.  rmcm_estimate_noalloc serves them.  The caller passes
+// its chain as plain device CSR arrays it already owns and a host array for
+// the estimates; every temporary the estimator needs (two levels of row
+// sparsities, per-block partial sums and the estimate matrix) lives in the
+// file-scope array below, a fixed 32 MiB that every GPU which loads this
+// library holds until the process exits.  The array's address is looked up
+// once per device, on the first call made with that device current.
+
+namespace {
+
+constexpr int64_t kNoAllocScratchBytes = 32LL << 20;
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+struct NoAllocDevice {
+    bool ready = false;
+    unsigned char *scratch = nullptr;   // device address of g_noalloc_scratch
+    int sm_count = 0;
+};
+std::mutex g_noalloc_mu;
+NoAllocDevice g_noalloc_dev[128];
+
+}  // namespace
 }  // namespace rmcm
+
+extern "C" RMCM_API int32_t rmcm_estimate_noalloc(int32_t len, const int64_t *rows, const int64_t *cols,
+                                                  const int64_t *const *rowptr, const int32_t *const *col,
+                                                  double *c_out, void *stream) {
+    using namespace rmcm;
+    if (len < 1 || len > kMaxLen || !rows || !cols || !rowptr || !col || !c_out) return RMCM_EINVAL;
+    int64_t max_rows = 1;
+    for (int i = 0; i < len; i++) {
+        if (rows[i] < 0 || cols[i] < 0 || cols[i] > INT32_MAX || (rows[i] > 0 && !rowptr[i])) return RMCM_EINVAL;
+        if (i + 1 < len && cols[i] != rows[i + 1]) return RMCM_EINVAL;
+        max_rows = std::max(max_rows, rows[i]);
+    }
+    // set-up, once per device, with that device current
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return RMCM_ECUDA;
+    NoAllocDevice nd;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        NoAllocDevice &d = g_noalloc_dev[dev];
+        if (!d.ready) {
+            void *ptr = nullptr;
+            if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) {
+                cudaGetLastError();
+                return RMCM_ECUDA;
+            }
+            int sm = 0;
+            if (cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sm <= 0) {
+                cudaGetLastError();
+                return RMCM_ECUDA;
+            }
+            d.scratch = (unsigned char *)ptr;
+            d.sm_count = sm;
+            d.ready = true;
+        }
+        nd = d;
+    }
+    // scratch layout: estimates | level r | level r' | block partials
+    const int64_t blocks_cap = (int64_t)nd.sm_count * 8;
+    auto al = [](int64_t x) { return (x + 255) & ~255LL; };
+    const int64_t cbytes = al(8 * kMaxLen * kMaxLen);
+    const int64_t rbytes = al(8 * max_rows * len);
+    const int64_t pbytes = al(8 * blocks_cap * kMaxLen);
+    if (cbytes + 2 * rbytes + pbytes > kNoAllocScratchBytes) return RMCM_EINVAL;   // chain too large
+    cudaStream_t s = (cudaStream_t)stream;
+    double *c_dev = (double *)nd.scratch;
+    double *r_cur = (double *)(nd.scratch + cbytes);
+    double *r_next = (double *)(nd.scratch + cbytes + rbytes);
+    double *part = (double *)(nd.scratch + cbytes + 2 * rbytes);
+    cudaError_t e = cudaMemsetAsync(c_dev, 0, sizeof(double) * len * len, s);
+    for (int i = len - 1; i >= 0 && e == cudaSuccess; i--) {
+        DevCsr M;
+        M.rows = rows[i];
+        M.cols = cols[i];
+        M.rowptr = const_cast<int64_t *>(rowptr[i]);
+        M.col = const_cast<int32_t *>(col[i]);
+        LevelArgs la{};
+        la.len = len;
+        la.i = i;
+        la.nj = len - 1 - i;
+        int jp = 1;
+        while (jp < la.nj) jp <<= 1;
+        la.jp = jp;
+        la.dim_leaf = (double)M.cols;
+        for (int j = 0; j < len; j++) la.dims[j] = (double)cols[j];
+        int64_t blocks = (M.rows * 32 + kEstThreads - 1) / kEstThreads;
+        blocks = std::max<int64_t>(1, std::min(blocks, blocks_cap));
+        k_res_level<<<(unsigned)blocks, kEstThreads, 0, s>>>(M, r_next, r_cur, la, part);
+        if (la.nj > 0) k_res_reduce<<<1, 256, 0, s>>>(part, (int32_t)blocks, la, c_dev);
+        e = cudaGetLastError();
+        std::swap(r_cur, r_next);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c_out, c_dev, sizeof(double) * len * len, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return RMCM_ECUDA;
+    }
+    return RMCM_OK;
+}
