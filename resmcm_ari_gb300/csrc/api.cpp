@@ -115,6 +115,7 @@ int32_t mat_alloc(rmcm_handle *h, int64_t rows, int64_t cols, int64_t nnz, int32
 
 void mat_release(rmcm_handle *h, rmcm_mat *m) {
     if (!m) return;
+    if (m->rowsum) dev_free(h, m->rowsum, 8 * m->d.rows);
     dev_free(h, m->d.rowptr, 8 * (m->d.rows + 1));
     if (m->d.col) dev_free(h, m->d.col, 4 * m->d.nnz);
     if (m->d.val) dev_free(h, m->d.val, val_bytes(m->valtype) * m->d.nnz);
@@ -329,6 +330,8 @@ int32_t upload_csr(rmcm_handle *h, int64_t rows, int64_t cols, const int64_t *ro
             mat_release(h, m);
             return rc;
         }
+        m->ones = true;
+        m->positive = true;
     }
     *out = m;
     return RMCM_OK;
@@ -427,6 +430,8 @@ int32_t copy_mat(rmcm_handle *h, const rmcm_mat *src, rmcm_mat **out) {
         mat_release(h, m);
         return cuda_error(h, e, "copy");
     }
+    m->ones = src->ones;
+    m->positive = src->positive;
     *out = m;
     return RMCM_OK;
 }
@@ -542,8 +547,25 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
         cudaEventRecord(ev[3], s);
         rmcm_mat *C = nullptr;
         int64_t fl = 0;
+        h->abort_on_certain_overflow = widen && cur == RMCM_VAL_U32;
         rc = spgemm(h, A, B, &C, &fl);
+        h->abort_on_certain_overflow = false;
         cudaEventRecord(ev[4], s);
+        if (rc == RMCM_EOVERFLOW && widen && cur == RMCM_VAL_U32 && !C) {
+            // overflow is certain from the row-sum bound: escalate before computing
+            rc = RMCM_OK;
+            cur = RMCM_VAL_U64;
+            for (auto &m : stack) {
+                rmcm_mat *w = nullptr;
+                rc = convert_values(h, m, RMCM_VAL_U64, &w);
+                if (rc != RMCM_OK) break;
+                mat_release(h, m);
+                m = w;
+            }
+            if (rc != RMCM_OK) break;
+            p--;
+            continue;
+        }
         if (rc != RMCM_OK) break;
         cudaEventSynchronize(ev[4]);
         spgemm_s += elapsed_s(ev[3], ev[4]);
@@ -598,6 +620,7 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
     *Cout = stack[0];
     tm.nnz = stack[0]->d.nnz;
     rc = check_status(h);
+    if (rc == RMCM_EOVERFLOW) stack[0]->positive = false;   // wrapped counts may be 0
     if (t) *t = tm;
     return rc;
 }
@@ -864,7 +887,19 @@ RMCM_API int32_t rmcm_mat_upload(rmcm_handle *h, int64_t rows, int64_t cols, con
         }
     }
     if (bad) return set_error(h, RMCM_EINVAL, "upload: row pointer not monotone or column out of range");
-    if (!unsorted) return upload_csr(h, rows, cols, rowptr, col, val, valtype, out);
+    bool positive = true;
+    if (val) {
+        int zero = 0;
+#pragma omp parallel for schedule(static) reduction(| : zero)
+        for (int64_t q = 0; q < nnz; q++)
+            zero |= valtype == RMCM_VAL_U64 ? ((const uint64_t *)val)[q] == 0 : ((const uint32_t *)val)[q] == 0;
+        positive = !zero;
+    }
+    if (!unsorted) {
+        int32_t rc = upload_csr(h, rows, cols, rowptr, col, val, valtype, out);
+        if (rc == RMCM_OK && val) (*out)->positive = positive;
+        return rc;
+    }
     std::vector<int32_t> c2(col, col + nnz);
     std::vector<char> v2;
     const int64_t vb = val_bytes(valtype);
@@ -880,7 +915,9 @@ RMCM_API int32_t rmcm_mat_upload(rmcm_handle *h, int64_t rows, int64_t cols, con
             if (val) memcpy(&v2[(a + q) * vb], (const char *)val + idx[q] * vb, vb);
         }
     }
-    return upload_csr(h, rows, cols, rowptr, c2.data(), val ? v2.data() : nullptr, valtype, out);
+    int32_t rc = upload_csr(h, rows, cols, rowptr, c2.data(), val ? v2.data() : nullptr, valtype, out);
+    if (rc == RMCM_OK && val) (*out)->positive = positive;
+    return rc;
 }
 
 RMCM_API int32_t rmcm_mat_info(const rmcm_mat *m, int64_t *rows, int64_t *cols, int64_t *nnz, int32_t *valtype) {
@@ -957,6 +994,7 @@ RMCM_API int32_t rmcm_spgemm(rmcm_handle *h, const rmcm_mat *A, const rmcm_mat *
     int32_t rc = spgemm(h, A, B, C, nullptr);
     if (rc != RMCM_OK) return rc;
     rc = check_status(h);
+    if (rc == RMCM_EOVERFLOW) (*C)->positive = false;   // wrapped counts may be 0
     if (rc != RMCM_OK && rc != RMCM_EOVERFLOW) {
         mat_release(h, *C);
         *C = nullptr;

@@ -27,6 +27,7 @@ struct DevCsr {
     int64_t *rowptr = nullptr;
     int32_t *col = nullptr;
     void *val = nullptr;
+    const uint64_t *rowsum = nullptr;   // per-row sum of values (saturating); null when every value is 1
 };
 
 // Device-side status words, one int each (set with atomicOr, never cleared by kernels).
@@ -66,6 +67,9 @@ struct rmcm_mat {
     rmcm::DevCsr d;
     int32_t valtype = RMCM_VAL_U32;
     bool graph_owned = false;
+    bool ones = false;                  // every value is 1 (leaves): row sums are row lengths
+    bool positive = false;              // every value is >= 1 (a counter > 0 then marks presence)
+    uint64_t *rowsum = nullptr;         // lazily computed row sums (device), owned
     int64_t bytes = 0;
 };
 
@@ -90,6 +94,7 @@ struct rmcm_handle {
     int32_t prof_level = 0;
     std::vector<rmcm::ProdRecord> prof;
     std::set<rmcm_graph *> graphs;   // graphs whose leaves live on this handle
+    bool abort_on_certain_overflow = false;   // spgemm returns EOVERFLOW before computing when sure
 };
 
 struct rmcm_graph {

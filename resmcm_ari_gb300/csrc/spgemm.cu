@@ -34,6 +34,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <type_traits>
 
 #include "internal.h"
 
@@ -41,7 +42,8 @@ namespace rmcm {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kEmptyBin = 255;
+constexpr int kEmptyBin = 0x7f;   // bin code of rows with no products
+constexpr int kRiskyBit = 0x80;   // bin_of flag: the row's total count may exceed the value type
 
 // Shared-memory windows of the dense bin (columns per window).
 constexpr int32_t kDenseWinU32 = 40960;       // 160 KB counters + 40 KB presence bytes
@@ -107,30 +109,71 @@ __device__ __forceinline__ int classify(int64_t f, int64_t ncols, const BinParam
     return kBinHash8k;
 }
 
+__device__ __forceinline__ unsigned long long sat_add(unsigned long long a, unsigned long long b) {
+    return a > ~0ull - b ? ~0ull : a + b;
+}
+
 // Warp per row of A: flops and bin; per-bin row counts and the longest
-// A row of the dense bin (it sizes the cursor scratch).
+// A row of the dense bin (it sizes the cursor scratch).  It also bounds the
+// row's total count S = sum_k A[r][k] * rowsum(B[k]) (saturating): no entry
+// of the row can exceed S, so a row with S within the value type is marked
+// safe (its kernels skip the overflow checks), and a row with S greater than
+// (its possible distinct columns) x (largest value) is certain to overflow,
+// which raises *certain.
+template <typename V>
 __global__ void k_analyze(DevCsr A, DevCsr B, BinParams bp, int64_t *flops, uint8_t *bin_of,
-                          int32_t *bin_count, int32_t *dense_max_alen, unsigned long long *flops_total) {
+                          int32_t *bin_count, int32_t *dense_max_alen, unsigned long long *flops_total,
+                          int32_t *certain) {
     const int lane = threadIdx.x & 31;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const V *Aval = (const V *)A.val;
     for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < A.rows; r += nwarps) {
         const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
         int64_t f = 0;
+        unsigned long long srow = 0;
         for (int64_t k = a0 + lane; k < a1; k += 32) {
             const int32_t a = A.col[k];
-            f += B.rowptr[a + 1] - B.rowptr[a];
+            const int64_t len = B.rowptr[a + 1] - B.rowptr[a];
+            f += len;
+            const unsigned long long bsum = B.rowsum ? B.rowsum[a] : (unsigned long long)len;
+            const unsigned long long av = Aval[k];
+            const unsigned long long prod = __umul64hi(av, bsum) ? ~0ull : av * bsum;
+            srow = sat_add(srow, prod);
         }
         f = warp_sum(f);
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) srow = sat_add(srow, __shfl_xor_sync(kFull, srow, d));
         if (lane == 0) {
             const int b = classify(f, B.cols, bp);
+            const unsigned long long vmax = sizeof(V) == 4 ? 0xffffffffull : ~0ull;
+            const bool risky = sizeof(V) == 4 ? srow > vmax : srow == ~0ull;
             flops[r] = f;
-            bin_of[r] = (uint8_t)b;
+            bin_of[r] = (uint8_t)(b | (risky ? kRiskyBit : 0));
             if (f) atomicAdd(flops_total, (unsigned long long)f);
+            if (sizeof(V) == 4 && risky) {
+                const unsigned long long distinct = (unsigned long long)min(f, B.cols);
+                if (srow == ~0ull || srow / vmax > distinct) atomicOr(certain, 1);
+            }
             if (b != kEmptyBin) {
                 atomicAdd(bin_count + b, 1);
                 if (b == kBinDense) atomicMax(dense_max_alen, (int32_t)(a1 - a0 < (int64_t)INT_MAX ? a1 - a0 : (int64_t)INT_MAX));
             }
         }
+    }
+}
+
+// Saturating row sums of a matrix's values (warp per row).
+template <typename V>
+__global__ void k_rowsum(DevCsr M, uint64_t *out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const V *v = (const V *)M.val;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < M.rows; r += nwarps) {
+        unsigned long long sum = 0;
+        for (int64_t q = M.rowptr[r] + lane; q < M.rowptr[r + 1]; q += 32) sum = sat_add(sum, (unsigned long long)v[q]);
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) sum = sat_add(sum, __shfl_xor_sync(kFull, sum, d));
+        if (lane == 0) out[r] = sum;
     }
 }
 
@@ -144,7 +187,7 @@ __global__ void k_scatter(int64_t m, const uint8_t *bin_of, const int32_t *bin_c
     }
     __syncthreads();
     for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x) {
-        const int b = bin_of[r];
+        const int b = bin_of[r] & ~kRiskyBit;
         if (b == kEmptyBin) continue;
         const int32_t pos = atomicAdd(bin_cursor + b, 1);
         lists[off[b] + pos] = (int32_t)r;
@@ -153,7 +196,7 @@ __global__ void k_scatter(int64_t m, const uint8_t *bin_of, const int32_t *bin_c
 
 __global__ void k_zero_counts(int64_t m, const uint8_t *bin_of, int64_t *cnt) {
     for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x)
-        if (bin_of[r] == kEmptyBin) cnt[r] = 0;
+        if ((bin_of[r] & ~kRiskyBit) == kEmptyBin) cnt[r] = 0;
 }
 
 // ------------------------------------------------------------------------
@@ -285,11 +328,16 @@ constexpr int kChunk = 512;
 
 template <typename V>
 struct ChunkStage {
-    int64_t pre[kChunk + 1];
-    int64_t bs[kChunk];
-    V va[kChunk];
+    int64_t pre[kChunk + 1];   // first flattened product of each entry (short entries only when split)
+    int64_t bs[kChunk];        // first B position of each entry
+    V va[kChunk];              // A value of each entry
+    int32_t len[kChunk];       // B positions of each entry
     int64_t warp_tot[32];
+    int32_t ctr;               // next entry for the long-row warps
 };
+
+// B rows with at least this many products go to the warp-per-row path.
+constexpr int kLongRow = 32;
 
 // Block-wide exclusive scan of kChunk int64 lengths held kChunk/NT per thread.
 template <int NT>
@@ -326,7 +374,7 @@ __device__ __forceinline__ void stage_scan(int64_t (&len)[kChunk / NT], int64_t 
 
 // Visits every staged product of the chunk: visit(col, product value).
 template <int NT, typename V, bool NUMERIC, typename Visit>
-__device__ __forceinline__ void stream_chunk(const ChunkStage<V> &sg, int cnt, const DevCsr B, bool &ovf,
+__device__ __forceinline__ void stream_chunk(const ChunkStage<V> &sg, int cnt, const DevCsr B, bool checked, bool &ovf,
                                              Visit visit) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     constexpr int NW = NT / 32;
@@ -360,12 +408,46 @@ __device__ __forceinline__ void stream_chunk(const ChunkStage<V> &sg, int cnt, c
                 while (sg.pre[k + 1] <= p) k++;
                 const int64_t q = sg.bs[k] + (p - sg.pre[k]);
                 c[u] = B.col[q];
-                if (NUMERIC) pv[u] = mul_chk(sg.va[k], Bval[q], ovf);
+                if (NUMERIC) pv[u] = checked ? mul_chk(sg.va[k], Bval[q], ovf) : (V)(sg.va[k] * Bval[q]);
             }
         }
 #pragma unroll
         for (int u = 0; u < 4; u++)
             if (ok[u]) visit(c[u], pv[u]);
+    }
+}
+
+// Visits the products of the staged entries whose B segment has at least
+// kLongRow positions: warps take such entries one at a time from a shared
+// counter (sg.ctr, zeroed by the caller before staging) and sweep the segment
+// 128 positions per step, four loads per lane in flight, no per-product search.
+template <typename V, bool NUMERIC, typename Visit>
+__device__ __forceinline__ void stream_long(ChunkStage<V> &sg, int cnt, const DevCsr B, bool checked, bool &ovf,
+                                            Visit visit) {
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(&sg.ctr, 1);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= cnt) break;
+        const int32_t L = sg.len[t];
+        if (L < kLongRow) continue;
+        const int32_t *bc = B.col + sg.bs[t];
+        const V *bv = (const V *)B.val + sg.bs[t];
+        const V a = NUMERIC ? sg.va[t] : (V)0;
+        for (int32_t base = 0; base < L; base += 128) {
+            int32_t c[4];
+            V v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int32_t o = base + u * 32 + lane;
+                c[u] = o < L ? bc[o] : -1;
+                if (NUMERIC) v[u] = o < L ? bv[o] : (V)0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (c[u] >= 0) visit(c[u], NUMERIC ? (checked ? mul_chk(a, v[u], ovf) : (V)(a * v[u])) : (V)0);
+        }
     }
 }
 
@@ -380,18 +462,24 @@ __device__ __forceinline__ uint32_t hash_slot(int32_t c) {
 }
 
 template <typename V, bool NUMERIC, int S>
-__device__ __forceinline__ int hash_insert(int32_t *keys, V *vals, int32_t c, V p, int *st, bool &ovf) {
+__device__ __forceinline__ void hash_add(V *slot, V p, bool checked, bool &ovf) {
+    if (checked) add_shared_chk(slot, p, ovf);
+    else atomicAdd((typename std::conditional<sizeof(V) == 4, unsigned int, unsigned long long>::type *)slot, p);
+}
+
+template <typename V, bool NUMERIC, int S>
+__device__ __forceinline__ int hash_insert(int32_t *keys, V *vals, int32_t c, V p, int *st, bool checked, bool &ovf) {
     uint32_t h = hash_slot<S>(c);
     for (int probe = 0; probe < S; probe++) {
         const int32_t k = ((volatile int32_t *)keys)[h];
         if (k == c) {
-            if (NUMERIC) add_shared_chk(vals + h, p, ovf);
+            if (NUMERIC) hash_add<V, NUMERIC, S>(vals + h, p, checked, ovf);
             return 0;
         }
         if (k == -1) {
             const int32_t old = atomicCAS(keys + h, -1, c);
             if (old == -1 || old == c) {
-                if (NUMERIC) add_shared_chk(vals + h, p, ovf);
+                if (NUMERIC) hash_add<V, NUMERIC, S>(vals + h, p, checked, ovf);
                 return old == -1;
             }
         }
@@ -441,6 +529,7 @@ __device__ __forceinline__ void stage_full_rows(ChunkStage<V> &sg, const DevCsr 
             const int64_t b0 = B.rowptr[a];
             len[i] = B.rowptr[a + 1] - b0;
             sg.bs[t] = b0;
+            sg.len[t] = (int32_t)len[i];
             if (NUMERIC) sg.va[t] = Aval[k0 + t];
         }
     }
@@ -449,7 +538,7 @@ __device__ __forceinline__ void stage_full_rows(ChunkStage<V> &sg, const DevCsr 
 
 template <typename V, bool NUMERIC, int S, int NT>
 __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows, int32_t nrows,
-                                             int64_t *cnt, int *st) {
+                                             int64_t *cnt, int *st, const uint8_t *bin_of) {
     extern __shared__ __align__(16) unsigned char smem[];
     int32_t *keys = (int32_t *)smem;
     V *vals = (V *)(keys + S);
@@ -462,6 +551,7 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
     for (int32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
         const int32_t r = rows[ri];
         const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
+        const bool checked = (bin_of[r] & kRiskyBit) != 0;
         for (int i = tid; i < S; i += NT) {
             keys[i] = -1;
             if (NUMERIC) vals[i] = 0;
@@ -471,8 +561,8 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
         for (int64_t k0 = a0; k0 < a1; k0 += kChunk) {
             const int n = (int)(a1 - k0 < (int64_t)kChunk ? a1 - k0 : (int64_t)kChunk);
             stage_full_rows<NT, V, NUMERIC>(sg, A, B, k0, n);
-            stream_chunk<NT, V, NUMERIC>(sg, n, B, ovf, [&](int32_t c, V p) {
-                fresh += hash_insert<V, NUMERIC, S>(keys, vals, c, p, st, ovf);
+            stream_chunk<NT, V, NUMERIC>(sg, n, B, checked, ovf, [&](int32_t c, V p) {
+                fresh += hash_insert<V, NUMERIC, S>(keys, vals, c, p, st, checked, ovf);
             });
             __syncthreads();
         }
@@ -553,17 +643,19 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
 template <typename V, bool NUMERIC, bool TEMP>
 __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows,
                                                          int32_t nrows, int64_t *cnt, int32_t *cursors,
-                                                         int64_t cur_stride, int32_t W, int *st, int64_t tstride) {
+                                                         int64_t cur_stride, int32_t W, int *st, int64_t tstride,
+                                                         const uint8_t *bin_of, bool positive) {
     constexpr int NT = kDenseThreads;
     constexpr int IPT = kChunk / NT;
+    constexpr int NW = NT / 32;
+    using AtomV = typename std::conditional<sizeof(V) == 4, unsigned int, unsigned long long>::type;
     extern __shared__ __align__(16) unsigned char smem[];
     uint8_t *present = smem;
     V *acc = (V *)(smem + (((size_t)W + 15) & ~(size_t)15));
     __shared__ ChunkStage<V> sg;
-    __shared__ int64_t s_warp[NT / 32];
+    __shared__ int64_t s_warp[NW];
     __shared__ int32_t s_next;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    constexpr int NW = NT / 32;
     const unsigned lt_mask = (1u << lane) - 1u;
     const V *Aval = (const V *)A.val;
     for (int i = tid; i < W / 16; i += NT) ((uint4 *)present)[i] = make_uint4(0, 0, 0, 0);
@@ -576,12 +668,24 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
     for (int32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
         const int32_t r = rows[ri];
         const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
+        // A row that cannot overflow needs no checks, and when every input
+        // value is >= 1 its counters alone mark presence (no count is 0).
+        const bool checked = NUMERIC && (bin_of[r] & kRiskyBit) != 0;
+        const bool track = !NUMERIC || checked || !positive;
         const int64_t row_base = TEMP ? (int64_t)ri * tstride : (NUMERIC ? C.rowptr[r] : 0);
         const int64_t row_end = TEMP ? row_base + tstride : (NUMERIC ? C.rowptr[r + 1] : 0);
         int64_t out = row_base;
         int64_t total = 0;
         int64_t w0 = 0;
         bool first = true;
+        auto visit = [&](int32_t c, V p) {
+            const int32_t lc = (int32_t)(c - w0);
+            if (track) present[lc] = 1;
+            if (NUMERIC) {
+                if (checked) add_shared_chk(acc + lc, p, ovf);
+                else atomicAdd((AtomV *)(acc + lc), (AtomV)p);
+            }
+        };
         while (true) {
             const int64_t w1 = min(w0 + (int64_t)W, B.cols);
             if (tid == 0) s_next = INT_MAX;
@@ -611,17 +715,16 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                             cur[k - a0] = (int32_t)(hi - bs);
                             if (hi < be) my_next = min(my_next, B.col[hi]);
                         }
-                        len[i] = hi - lo;
                         sg.bs[t] = lo;
+                        sg.len[t] = (int32_t)(hi - lo);
                         if (NUMERIC) sg.va[t] = Aval[k];
+                        len[i] = hi - lo < kLongRow ? hi - lo : 0;   // long segments go to stream_long
                     }
                 }
+                if (tid == 0) sg.ctr = 0;
                 stage_scan<NT>(len, sg.pre, sg.warp_tot);
-                stream_chunk<NT, V, NUMERIC>(sg, n, B, ovf, [&](int32_t c, V p) {
-                    const int32_t lc = (int32_t)(c - w0);
-                    present[lc] = 1;
-                    if (NUMERIC) add_shared_chk(acc + lc, p, ovf);
-                });
+                stream_long<V, NUMERIC>(sg, n, B, checked, ovf, visit);
+                stream_chunk<NT, V, NUMERIC>(sg, n, B, checked, ovf, visit);
                 __syncthreads();
             }
             if (multi) {
@@ -630,21 +733,15 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
             }
             // count the window: warps own contiguous ranges of 32-column groups
             const int groups = (int)((w1 - w0 + 31) >> 5);
-            const int chunk = (groups + NW - 1) / NW;
-            const int gb = min(warp * chunk, groups), ge = min(gb + chunk, groups);
+            const int gchunk = (groups + NW - 1) / NW;
+            const int gb = min(warp * gchunk, groups), ge = min(gb + gchunk, groups);
             int64_t c_w = 0;
-            for (int g = gb + lane; g < ge; g += 32) {
-                const uint4 x = ((const uint4 *)present)[2 * g];
-                const uint4 y = ((const uint4 *)present)[2 * g + 1];
-                c_w += __popc(x.x & 0x01010101u) + __popc(x.y & 0x01010101u) + __popc(x.z & 0x01010101u) +
-                       __popc(x.w & 0x01010101u) + __popc(y.x & 0x01010101u) + __popc(y.y & 0x01010101u) +
-                       __popc(y.z & 0x01010101u) + __popc(y.w & 0x01010101u);
-                if (!NUMERIC) {
-                    ((uint4 *)present)[2 * g] = make_uint4(0, 0, 0, 0);
-                    ((uint4 *)present)[2 * g + 1] = make_uint4(0, 0, 0, 0);
-                }
+            for (int g = gb; g < ge; g++) {
+                const int lc = g * 32 + lane;
+                const bool here = track ? present[lc] != 0 : acc[lc] != 0;
+                c_w += __popc(__ballot_sync(kFull, here));
+                if (!NUMERIC && here) present[lc] = 0;
             }
-            c_w = warp_sum(c_w);
             if (lane == 0) s_warp[warp] = c_w;
             __syncthreads();
             int64_t base = 0, wtot = 0;
@@ -658,7 +755,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                 int64_t pos = out + base;
                 for (int g = gb; g < ge; g++) {
                     const int lc = g * 32 + lane;
-                    const bool here = present[lc] != 0;
+                    const bool here = track ? present[lc] != 0 : acc[lc] != 0;
                     const unsigned bits = __ballot_sync(kFull, here);
                     if (here) {
                         const int64_t o = pos + __popc(bits & lt_mask);
@@ -667,7 +764,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                             ((V *)C.val)[o] = acc[lc];
                         }
                         acc[lc] = 0;
-                        present[lc] = 0;
+                        if (track) present[lc] = 0;
                     }
                     pos += __popc(bits);
                 }
@@ -858,7 +955,7 @@ struct DenseTemp {
 template <typename V, bool NUMERIC>
 int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevCsr &C, const int32_t *lists,
                     const int32_t *counts, int32_t dense_max_alen, int64_t *cnt, int32_t *cursor_base,
-                    int64_t cursor_cap, const DenseTemp *temp) {
+                    int64_t cursor_cap, const DenseTemp *temp, const uint8_t *bin_of, bool positive) {
     cudaStream_t s = h->stream;
     int *st = h->d_status;
     int32_t off = 0;
@@ -879,7 +976,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                 const int64_t sm = S * 4 + (NUMERIC ? S * sizeof(V) + (S / 2) * (4 + sizeof(V)) : 0);
                 auto kern = k_hash<V, NUMERIC, S, NT>;
                 RMCM_TRY(set_smem(h, kern, sm));
-                kern<<<grid_for(h, (int64_t)n * NT, NT, 16), NT, sm, s>>>(A, B, C, list, n, cnt, st);
+                kern<<<grid_for(h, (int64_t)n * NT, NT, 16), NT, sm, s>>>(A, B, C, list, n, cnt, st, bin_of);
                 break;
             }
             case kBinHash2k: {
@@ -887,7 +984,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                 const int64_t sm = S * 4 + (NUMERIC ? S * sizeof(V) + (S / 2) * (4 + sizeof(V)) : 0);
                 auto kern = k_hash<V, NUMERIC, S, NT>;
                 RMCM_TRY(set_smem(h, kern, sm));
-                kern<<<grid_for(h, (int64_t)n * NT, NT, 8), NT, sm, s>>>(A, B, C, list, n, cnt, st);
+                kern<<<grid_for(h, (int64_t)n * NT, NT, 8), NT, sm, s>>>(A, B, C, list, n, cnt, st, bin_of);
                 break;
             }
             case kBinHash8k: {
@@ -895,7 +992,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                 const int64_t sm = S * 4 + (NUMERIC ? S * sizeof(V) + (S / 2) * (4 + sizeof(V)) : 0);
                 auto kern = k_hash<V, NUMERIC, S, NT>;
                 RMCM_TRY(set_smem(h, kern, sm));
-                kern<<<grid_for(h, (int64_t)n * NT, NT, 2), NT, sm, s>>>(A, B, C, list, n, cnt, st);
+                kern<<<grid_for(h, (int64_t)n * NT, NT, 2), NT, sm, s>>>(A, B, C, list, n, cnt, st, bin_of);
                 break;
             }
             case kBinDense: {
@@ -912,7 +1009,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                         T.col = temp->col;
                         T.val = temp->val;
                         kern<<<grid, kDenseThreads, sm, s>>>(A, B, T, list, n, cnt, nullptr, 0, (int32_t)W, st,
-                                                             temp->stride);
+                                                             temp->stride, bin_of, positive);
                     } else {
                         const int grid = (int)std::min<int64_t>((int64_t)n, (int64_t)h->sm_count * 8);
                         k_copy_rows<V><<<grid, 256, 0, s>>>(list, n, C, temp->col, (const V *)temp->val,
@@ -933,7 +1030,8 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                 if (multi && (int64_t)grid * stride > cursor_cap) {
                     grid = (int)std::max<int64_t>(1, cursor_cap / stride);
                 }
-                kern<<<grid, kDenseThreads, sm, s>>>(A, B, C, list, n, cnt, cursor_base, stride, (int32_t)W, st, 0);
+                kern<<<grid, kDenseThreads, sm, s>>>(A, B, C, list, n, cnt, cursor_base, stride, (int32_t)W, st, 0, bin_of,
+                                                     positive);
                 break;
             }
         }
@@ -964,9 +1062,20 @@ int32_t scan_rowptr(rmcm_handle *h, const int64_t *cnt, int64_t m, int64_t *rowp
 
 template <typename V>
 int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_mat **Cout, int64_t *flops_out) {
-    const DevCsr A = Am->d, B = Bm->d;
-    const int64_t m = A.rows;
     cudaStream_t s = h->stream;
+    // row sums of B bound the counts of every output row (computed once per matrix)
+    if (!Bm->ones && !Bm->rowsum && Bm->d.rows > 0) {
+        rmcm_mat *Bw = const_cast<rmcm_mat *>(Bm);
+        RMCM_TRY(dev_alloc(h, (void **)&Bw->rowsum, 8 * Bm->d.rows));
+        k_rowsum<V><<<grid_for(h, Bm->d.rows * 32, 256, 8), 256, 0, s>>>(Bm->d, Bw->rowsum);
+        h->launches++;
+        RMCM_CUDA(h, cudaGetLastError());
+    }
+    const DevCsr A = Am->d;
+    DevCsr B = Bm->d;
+    B.rowsum = Bm->ones ? nullptr : Bm->rowsum;
+    const bool positive = Am->positive && Bm->positive;
+    const int64_t m = A.rows;
     // scratch layout: flops[m] i64 | cnt[m] i64 | tile sums | bin_of[m] u8 | lists[m] i32 | small counters | cursors
     const int64_t ntiles = std::max<int64_t>(1, (m + kScanTile - 1) / kScanTile);
     auto al = [](int64_t x) { return (x + 255) & ~255LL; };
@@ -985,7 +1094,9 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     int64_t *tiles = (int64_t *)(sc + o_tiles);
     uint8_t *bin_of = (uint8_t *)(sc + o_bin);
     int32_t *lists = (int32_t *)(sc + o_lists);
-    int32_t *small = (int32_t *)(sc + o_small);   // [0..4] counts, [8..12] cursors, [16] dense max alen
+    // small: [0..4] bin counts, [8..12] bin cursors, [16] longest dense A row,
+    // [32..33] total flops (u64), [40] overflow certain, [48..51] profiling sums
+    int32_t *small = (int32_t *)(sc + o_small);
     RMCM_CUDA(h, cudaMemsetAsync(small, 0, 256, s));
 
     ProdRecord *rec = nullptr;
@@ -1002,8 +1113,8 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     bp.hash_max = h->tune.hash_max_flops;
     bp.dense_ratio = h->tune.dense_ratio;
     if (m > 0) {
-        k_analyze<<<grid_for(h, m * 32, 256, 8), 256, 0, s>>>(A, B, bp, flops, bin_of, small, small + 16,
-                                                               (unsigned long long *)(small + 32));
+        k_analyze<V><<<grid_for(h, m * 32, 256, 8), 256, 0, s>>>(A, B, bp, flops, bin_of, small, small + 16,
+                                                                  (unsigned long long *)(small + 32), small + 40);
         k_scatter<<<grid_for(h, m, 256, 8), 256, 0, s>>>(m, bin_of, small, small + 8, lists);
         k_zero_counts<<<grid_for(h, m, 256, 8), 256, 0, s>>>(m, bin_of, cnt);
         h->launches += 3;
@@ -1011,7 +1122,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     }
     if (rec) RMCM_CUDA(h, cudaEventRecord(h->prof[rec_idx].ev[1], s));
     // bin counts, the longest dense A row and the flops to the host
-    RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned, small, 36 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned, small, 44 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     RMCM_CUDA(h, cudaStreamSynchronize(s));
     int32_t counts[kNumBins];
     memcpy(counts, h->h_pinned, sizeof(counts));
@@ -1019,6 +1130,15 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     int64_t flops_total = 0;
     memcpy(&flops_total, (int32_t *)h->h_pinned + 32, sizeof(int64_t));
     if (flops_out) *flops_out = flops_total;
+    if (((int32_t *)h->h_pinned)[40] && h->abort_on_certain_overflow) {
+        // some row's total count exceeds (its distinct columns) x (largest
+        // value): an overflow is certain, so the caller widens first
+        if (rec) {
+            for (auto &e : h->prof[rec_idx].ev) cudaEventDestroy(e);
+            h->prof.pop_back();
+        }
+        return set_error(h, RMCM_EOVERFLOW, "path counts certainly exceed the value type");
+    }
 
     // Cursor buffer for multi-window dense rows.  It is a separate allocation:
     // growing the scratch area here would move the row lists built above.
@@ -1068,7 +1188,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         return rc;
     }
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[2], s);
-    rc = launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap, &dtemp);
+    rc = launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap, &dtemp, bin_of, positive);
     if (rc == RMCM_OK) rc = scan_rowptr(h, cnt, m, C->d.rowptr, tiles);
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[3], s);
     // nnz to the host, then the output arrays
@@ -1081,7 +1201,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     const int64_t nnz = hp[0];
     if (rc == RMCM_OK) rc = mat_alloc(h, m, B.cols, nnz, Am->valtype, &C);
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[4], s);
-    if (rc == RMCM_OK) rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap, &dtemp);
+    if (rc == RMCM_OK) rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap, &dtemp, bin_of, positive);
     drop_cursors();
     drop_temp();
     if (rc != RMCM_OK) {
@@ -1134,6 +1254,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
             st.bytes_c = (m + 1) * 8 + nnz * (4 + iv);
         }
     }
+    C->positive = positive;
     *Cout = C;
     return RMCM_OK;
 }
@@ -1168,6 +1289,7 @@ int32_t convert_values(rmcm_handle *h, const rmcm_mat *src, int32_t valtype, rmc
         mat_release(h, m);
         return cuda_error(h, e, "convert");
     }
+    m->ones = src->ones;
     *out = m;
     return RMCM_OK;
 }

@@ -217,3 +217,23 @@ def test_graph_outliving_its_handle_is_safe(native):
     C.free()
     eng.close()
     hg.close()
+
+
+def test_explicit_zero_values_keep_the_structure(native, engine):
+    """A stored 0 is still an entry: the structure is the Boolean product's."""
+    rng = np.random.default_rng(12)
+    A = _random_csr(rng, 200, 300, rng.integers(1, 80, 200), vmax=3)
+    B = _random_csr(rng, 300, 3000, rng.integers(1, 200, 300), vmax=3)
+    A.data[::5] = 0                       # explicit zeros, kept in the CSR
+    A.sort_indices(); B.sort_indices()
+    pattern = (sp.csr_matrix((np.ones_like(A.data), A.indices, A.indptr), A.shape)
+               @ sp.csr_matrix((np.ones_like(B.data), B.indices, B.indptr), B.shape)).tocsr()
+    pattern.sort_indices()
+    dense = A.toarray() @ B.toarray()
+    for vt in (native.VAL_U32, native.VAL_U64):
+        Am = engine.upload(A.indptr, A.indices, cols=A.shape[1], val=A.data.astype(np.uint64), valtype=vt)
+        Bm = engine.upload(B.indptr, B.indices, cols=B.shape[1], val=B.data.astype(np.uint64), valtype=vt)
+        rp, col, val = engine.spgemm(Am, Bm).download()
+        assert np.array_equal(rp, pattern.indptr) and np.array_equal(col, pattern.indices)
+        rows = np.repeat(np.arange(A.shape[0]), np.diff(rp))
+        assert np.array_equal(val.astype(np.int64), dense[rows, col].astype(np.int64))
