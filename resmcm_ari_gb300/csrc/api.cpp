@@ -360,7 +360,13 @@ int32_t build_leaf(rmcm_handle *h, rmcm_graph *g, int32_t src, int32_t sink, int
             if (g->adj_et[q] == et && g->vtype[g->adj_nbr[q]] == sink) col[o++] = g->local[g->adj_nbr[q]];
         std::sort(col.begin() + rp[r], col.begin() + rp[r + 1]);
     }
-    return upload_csr(h, rows, cols, rp.data(), col.data(), nullptr, valtype, out);
+    int dup = 0;
+#pragma omp parallel for schedule(dynamic, 4096) reduction(| : dup)
+    for (int64_t r = 0; r < rows; r++)
+        for (int64_t q = rp[r] + 1; q < rp[r + 1]; q++) dup |= col[q] == col[q - 1];
+    int32_t rc = upload_csr(h, rows, cols, rp.data(), col.data(), nullptr, valtype, out);
+    if (rc == RMCM_OK) (*out)->distinct = !dup;
+    return rc;
 }
 
 int32_t get_leaf(rmcm_handle *h, rmcm_graph *g, int32_t src, int32_t sink, int32_t et, int32_t valtype,
@@ -432,6 +438,7 @@ int32_t copy_mat(rmcm_handle *h, const rmcm_mat *src, rmcm_mat **out) {
     }
     m->ones = src->ones;
     m->positive = src->positive;
+    m->distinct = src->distinct;
     *out = m;
     return RMCM_OK;
 }
@@ -876,14 +883,15 @@ RMCM_API int32_t rmcm_mat_upload(rmcm_handle *h, int64_t rows, int64_t cols, con
     const int64_t nnz = rowptr[rows];
     if (rowptr[0] != 0 || nnz < 0 || (nnz > 0 && !col)) return set_error(h, RMCM_EINVAL, "upload: bad row pointer");
     // validate (rows ascending, columns in range); sort rows that are not ascending
-    int bad = 0, unsorted = 0;
-#pragma omp parallel for schedule(dynamic, 4096) reduction(| : bad, unsorted)
+    int bad = 0, unsorted = 0, dup = 0;
+#pragma omp parallel for schedule(dynamic, 4096) reduction(| : bad, unsorted, dup)
     for (int64_t r = 0; r < rows; r++) {
         const int64_t a = rowptr[r], b = rowptr[r + 1];
         if (b < a || b > nnz) { bad = 1; continue; }
         for (int64_t q = a; q < b; q++) {
             if (col[q] < 0 || col[q] >= cols) bad = 1;
             if (q > a && col[q] < col[q - 1]) unsorted = 1;
+            if (q > a && col[q] == col[q - 1]) dup = 1;
         }
     }
     if (bad) return set_error(h, RMCM_EINVAL, "upload: row pointer not monotone or column out of range");
@@ -897,7 +905,10 @@ RMCM_API int32_t rmcm_mat_upload(rmcm_handle *h, int64_t rows, int64_t cols, con
     }
     if (!unsorted) {
         int32_t rc = upload_csr(h, rows, cols, rowptr, col, val, valtype, out);
-        if (rc == RMCM_OK && val) (*out)->positive = positive;
+        if (rc == RMCM_OK) {
+            if (val) (*out)->positive = positive;
+            (*out)->distinct = !dup;
+        }
         return rc;
     }
     std::vector<int32_t> c2(col, col + nnz);
@@ -915,8 +926,15 @@ RMCM_API int32_t rmcm_mat_upload(rmcm_handle *h, int64_t rows, int64_t cols, con
             if (val) memcpy(&v2[(a + q) * vb], (const char *)val + idx[q] * vb, vb);
         }
     }
+    dup = 0;
+#pragma omp parallel for schedule(dynamic, 4096) reduction(| : dup)
+    for (int64_t r = 0; r < rows; r++)
+        for (int64_t q = rowptr[r] + 1; q < rowptr[r + 1]; q++) dup |= c2[q] == c2[q - 1];
     int32_t rc = upload_csr(h, rows, cols, rowptr, c2.data(), val ? v2.data() : nullptr, valtype, out);
-    if (rc == RMCM_OK && val) (*out)->positive = positive;
+    if (rc == RMCM_OK) {
+        if (val) (*out)->positive = positive;
+        (*out)->distinct = !dup;
+    }
     return rc;
 }
 

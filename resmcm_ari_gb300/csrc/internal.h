@@ -69,6 +69,7 @@ struct rmcm_mat {
     bool graph_owned = false;
     bool ones = false;                  // every value is 1 (leaves): row sums are row lengths
     bool positive = false;              // every value is >= 1 (a counter > 0 then marks presence)
+    bool distinct = false;              // no column repeats within a row
     uint64_t *rowsum = nullptr;         // lazily computed row sums (device), owned
     int64_t bytes = 0;
 };

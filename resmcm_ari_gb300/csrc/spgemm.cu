@@ -644,8 +644,10 @@ template <typename V, bool NUMERIC, bool TEMP>
 __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows,
                                                          int32_t nrows, int64_t *cnt, int32_t *cursors,
                                                          int64_t cur_stride, int32_t W, int *st, int64_t tstride,
-                                                         const uint8_t *bin_of, bool positive) {
+                                                         const uint8_t *bin_of, bool positive, bool b_distinct,
+                                                         bool abort_mode) {
     constexpr int NT = kDenseThreads;
+    constexpr int kPull = 4;   // register accumulators per thread: windows of up to 4 * NT columns
     constexpr int IPT = kChunk / NT;
     constexpr int NW = NT / 32;
     using AtomV = typename std::conditional<sizeof(V) == 4, unsigned int, unsigned long long>::type;
@@ -655,9 +657,11 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
     __shared__ ChunkStage<V> sg;
     __shared__ int64_t s_warp[NW];
     __shared__ int32_t s_next;
+    __shared__ int32_t s_abort;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned lt_mask = (1u << lane) - 1u;
     const V *Aval = (const V *)A.val;
+    const V *Bval = (const V *)B.val;
     for (int i = tid; i < W / 16; i += NT) ((uint4 *)present)[i] = make_uint4(0, 0, 0, 0);
     if (NUMERIC)
         for (int i = tid; i < W; i += NT) acc[i] = 0;
@@ -666,6 +670,12 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
     bool ovf = false;
     __syncthreads();
     for (int32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
+        if (abort_mode) {
+            // another CTA saw an overflow: the caller recomputes in uint64
+            if (tid == 0) s_abort = *(volatile int *)(st + kOverflow);
+            __syncthreads();
+            if (s_abort) break;
+        }
         const int32_t r = rows[ri];
         const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
         // A row that cannot overflow needs no checks, and when every input
@@ -690,6 +700,14 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
             const int64_t w1 = min(w0 + (int64_t)W, B.cols);
             if (tid == 0) s_next = INT_MAX;
             int32_t my_next = INT_MAX;
+            // B segments covering every column of a narrow window ("full") are
+            // accumulated in registers by column owner: no atomics, no presence
+            const int32_t wc = (int32_t)(w1 - w0);
+            const bool pull_ok = NUMERIC && b_distinct && wc <= kPull * NT;
+            V preg[kPull];
+#pragma unroll
+            for (int j = 0; j < kPull; j++) preg[j] = 0;
+            bool pulled = false;
             for (int64_t k0 = a0; k0 < a1; k0 += kChunk) {
                 const int n = (int)(a1 - k0 < (int64_t)kChunk ? a1 - k0 : (int64_t)kChunk);
                 int64_t len[IPT];
@@ -716,15 +734,47 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                             if (hi < be) my_next = min(my_next, B.col[hi]);
                         }
                         sg.bs[t] = lo;
-                        sg.len[t] = (int32_t)(hi - lo);
+                        const bool full = pull_ok && hi - lo == wc;
+                        sg.len[t] = full ? -1 : (int32_t)(hi - lo);
                         if (NUMERIC) sg.va[t] = Aval[k];
-                        len[i] = hi - lo < kLongRow ? hi - lo : 0;   // long segments go to stream_long
+                        len[i] = (full || hi - lo >= kLongRow) ? 0 : hi - lo;   // long ones: stream_long
                     }
                 }
                 if (tid == 0) sg.ctr = 0;
                 stage_scan<NT>(len, sg.pre, sg.warp_tot);
                 stream_long<V, NUMERIC>(sg, n, B, checked, ovf, visit);
                 stream_chunk<NT, V, NUMERIC>(sg, n, B, checked, ovf, visit);
+                if (pull_ok) {
+                    for (int t = 0; t < n; t++) {
+                        if (sg.len[t] != -1) continue;   // uniform: every thread reads the same flag
+                        pulled = true;
+                        const V a = sg.va[t];
+                        const V *bv = Bval + sg.bs[t];
+#pragma unroll
+                        for (int j = 0; j < kPull; j++) {
+                            const int c = tid + j * NT;
+                            if (c < wc) {
+                                const V p = checked ? mul_chk(a, bv[c], ovf) : (V)(a * bv[c]);
+                                if (checked) ovf |= preg[j] > (V)~(V)0 - p;
+                                preg[j] += p;
+                            }
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+            if (pulled) {
+                // fold the register sums in: each column has one owner, the
+                // atomics of this window finished at the barrier above
+#pragma unroll
+                for (int j = 0; j < kPull; j++) {
+                    const int c = tid + j * NT;
+                    if (c < wc) {
+                        if (checked) ovf |= acc[c] > (V)~(V)0 - preg[j];
+                        acc[c] += preg[j];
+                        if (track) present[c] = 1;
+                    }
+                }
                 __syncthreads();
             }
             if (multi) {
@@ -781,6 +831,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
             if (!NUMERIC || TEMP) cnt[r] = total;
             else if (total != row_end - row_base) raise_status(st, kInvariant);
         }
+        if (abort_mode && __syncthreads_or(ovf) && tid == 0) raise_status(st, kOverflow);
     }
     if (__syncthreads_or(ovf) && tid == 0) raise_status(st, kOverflow);
 }
@@ -955,7 +1006,8 @@ struct DenseTemp {
 template <typename V, bool NUMERIC>
 int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevCsr &C, const int32_t *lists,
                     const int32_t *counts, int32_t dense_max_alen, int64_t *cnt, int32_t *cursor_base,
-                    int64_t cursor_cap, const DenseTemp *temp, const uint8_t *bin_of, bool positive) {
+                    int64_t cursor_cap, const DenseTemp *temp, const uint8_t *bin_of, bool positive,
+                    bool b_distinct) {
     cudaStream_t s = h->stream;
     int *st = h->d_status;
     int32_t off = 0;
@@ -1009,7 +1061,8 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                         T.col = temp->col;
                         T.val = temp->val;
                         kern<<<grid, kDenseThreads, sm, s>>>(A, B, T, list, n, cnt, nullptr, 0, (int32_t)W, st,
-                                                             temp->stride, bin_of, positive);
+                                                             temp->stride, bin_of, positive, b_distinct,
+                                                             h->abort_on_certain_overflow);
                     } else {
                         const int grid = (int)std::min<int64_t>((int64_t)n, (int64_t)h->sm_count * 8);
                         k_copy_rows<V><<<grid, 256, 0, s>>>(list, n, C, temp->col, (const V *)temp->val,
@@ -1031,7 +1084,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                     grid = (int)std::max<int64_t>(1, cursor_cap / stride);
                 }
                 kern<<<grid, kDenseThreads, sm, s>>>(A, B, C, list, n, cnt, cursor_base, stride, (int32_t)W, st, 0, bin_of,
-                                                     positive);
+                                                     positive, b_distinct, h->abort_on_certain_overflow);
                 break;
             }
         }
@@ -1188,7 +1241,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         return rc;
     }
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[2], s);
-    rc = launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap, &dtemp, bin_of, positive);
+    rc = launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap, &dtemp, bin_of, positive, Bm->distinct);
     if (rc == RMCM_OK) rc = scan_rowptr(h, cnt, m, C->d.rowptr, tiles);
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[3], s);
     // nnz to the host, then the output arrays
@@ -1199,9 +1252,23 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         if (e != cudaSuccess) rc = cuda_error(h, e, "spgemm nnz download");
     }
     const int64_t nnz = hp[0];
+    if (rc == RMCM_OK && h->abort_on_certain_overflow) {
+        // single-pass dense rows already computed their counts: stop early if
+        // any of them overflowed, so the caller can recompute in uint64
+        cudaError_t e = cudaMemcpyAsync(h->h_status, h->d_status, sizeof(int) * kNumStatus, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = cuda_error(h, e, "spgemm status download");
+        else if (h->h_status[kOverflow]) {
+            cudaMemsetAsync(h->d_status + kOverflow, 0, sizeof(int), s);
+            drop_cursors();
+            drop_temp();
+            mat_release(h, C);
+            return set_error(h, RMCM_EOVERFLOW, "path counts exceed the value type");
+        }
+    }
     if (rc == RMCM_OK) rc = mat_alloc(h, m, B.cols, nnz, Am->valtype, &C);
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[4], s);
-    if (rc == RMCM_OK) rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap, &dtemp, bin_of, positive);
+    if (rc == RMCM_OK) rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap, &dtemp, bin_of, positive, Bm->distinct);
     drop_cursors();
     drop_temp();
     if (rc != RMCM_OK) {
@@ -1255,6 +1322,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         }
     }
     C->positive = positive;
+    C->distinct = true;
     *Cout = C;
     return RMCM_OK;
 }
@@ -1290,6 +1358,8 @@ int32_t convert_values(rmcm_handle *h, const rmcm_mat *src, int32_t valtype, rmc
         return cuda_error(h, e, "convert");
     }
     m->ones = src->ones;
+    m->positive = src->positive;
+    m->distinct = src->distinct;
     *out = m;
     return RMCM_OK;
 }

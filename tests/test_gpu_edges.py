@@ -237,3 +237,48 @@ def test_explicit_zero_values_keep_the_structure(native, engine):
         assert np.array_equal(rp, pattern.indptr) and np.array_equal(col, pattern.indices)
         rows = np.repeat(np.arange(A.shape[0]), np.diff(rp))
         assert np.array_equal(val.astype(np.int64), dense[rows, col].astype(np.int64))
+
+
+def test_fully_dense_b_rows_use_the_register_path(native, engine):
+    """B rows covering every column of a narrow window (plus some that do not)."""
+    rng = np.random.default_rng(21)
+    m, k, n = 300, 500, 1500
+    A = _random_csr(rng, m, k, rng.integers(1, 120, m), vmax=5)
+    rows_nnz = np.where(rng.random(k) < 0.6, n, rng.integers(1, n, k))
+    B = _random_csr(rng, k, n, rows_nnz, vmax=5)
+    for vt in (native.VAL_U32, native.VAL_U64):
+        _check_product(native, engine, A, B, vt)
+
+
+def test_full_length_rows_with_repeats_are_not_dense(native, engine):
+    """A row as long as the window but with a repeated column does not cover it."""
+    Bd = np.array([[2, 1, 1, 0]] * 40, np.uint64)          # 4 columns, column 3 empty
+    rp = np.arange(0, 4 * 40 + 1, 4, dtype=np.int64)
+    col = np.tile(np.array([0, 0, 1, 2], np.int32), 40)     # column 0 listed twice
+    val = np.tile(np.array([1, 1, 1, 1], np.uint64), 40)
+    B = engine.upload(rp, col, cols=4, val=val, valtype=native.VAL_U32)
+    arp = np.array([0, 40], np.int64)
+    A = engine.upload(arp, np.arange(40, dtype=np.int32), cols=40, valtype=native.VAL_U32)
+    C = engine.spgemm(A, B)
+    rpc, colc, valc = C.download()
+    assert colc.tolist() == [0, 1, 2] and valc.tolist() == [80, 40, 40]
+
+
+def test_dense_register_path_detects_overflow(native, engine):
+    import ctypes
+    k, n = 64, 1000
+    big = np.uint64(1 << 27)
+    rp = np.arange(0, k * n + 1, n, dtype=np.int64)
+    col = np.tile(np.arange(n, dtype=np.int32), k)
+    B = engine.upload(rp, col, cols=n, val=np.full(k * n, big, np.uint64), valtype=native.VAL_U32)
+    A = engine.upload(np.array([0, k], np.int64), np.arange(k, dtype=np.int32), cols=k,
+                      val=np.full(k, 2, np.uint64), valtype=native.VAL_U32)
+    h = ctypes.c_void_p()
+    rc = native.lib().rmcm_spgemm(engine._h, A._h, B._h, ctypes.byref(h))
+    assert rc == native.EOVERFLOW            # 64 * 2 * 2^27 = 2^34 per column
+    native.lib().rmcm_mat_free(engine._h, h)
+    B64 = engine.upload(rp, col, cols=n, val=np.full(k * n, big, np.uint64), valtype=native.VAL_U64)
+    A64 = engine.upload(np.array([0, k], np.int64), np.arange(k, dtype=np.int32), cols=k,
+                        val=np.full(k, 2, np.uint64), valtype=native.VAL_U64)
+    C = engine.spgemm(A64, B64)
+    assert set(C.download()[2].tolist()) == {1 << 34}
