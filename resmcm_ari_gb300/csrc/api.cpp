@@ -759,9 +759,10 @@ RMCM_API int32_t rmcm_get_product_stats(rmcm_handle *h, rmcm_product_stats *out,
     for (int32_t i = 0; i < n && out && i < cap; i++) {
         rmcm::ProdRecord &r = h->prof[i];
         float a = 0, b = 0, c = 0;
-        cudaEventElapsedTime(&a, r.ev[0], r.ev[1]);
-        cudaEventElapsedTime(&b, r.ev[2], r.ev[3]);
-        cudaEventElapsedTime(&c, r.ev[4], r.ev[5]);
+        if (cudaEventElapsedTime(&a, r.ev[0], r.ev[1]) != cudaSuccess) a = 0;
+        if (cudaEventElapsedTime(&b, r.ev[2], r.ev[3]) != cudaSuccess) b = 0;
+        if (cudaEventElapsedTime(&c, r.ev[4], r.ev[5]) != cudaSuccess) c = 0;
+        cudaGetLastError();   // an unrecorded event must not leak into later launch checks
         r.st.analyze_ms = a;
         r.st.symbolic_ms = b;
         r.st.numeric_ms = c;

@@ -1263,6 +1263,10 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
             drop_cursors();
             drop_temp();
             mat_release(h, C);
+            if (rec) {
+                for (auto &e : h->prof[rec_idx].ev) cudaEventDestroy(e);
+                h->prof.pop_back();
+            }
             return set_error(h, RMCM_EOVERFLOW, "path counts exceed the value type");
         }
     }
