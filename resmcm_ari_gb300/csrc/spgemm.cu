@@ -334,6 +334,10 @@ struct ChunkStage {
     int32_t len[kChunk];       // B positions of each entry
     int64_t warp_tot[32];
     int32_t ctr;               // next entry for the long-row warps
+    int32_t nlong, nfull;      // dense kernel: entries in llist / flist
+    int32_t llist[kChunk];     // dense kernel: entries with long B segments
+    int32_t flist[kChunk];     // dense kernel: entries whose B segment fills the window
+    int32_t wl[32], wf[32];    // per-warp counts while the lists are built
 };
 
 // B rows with at least this many products go to the warp-per-row path.
@@ -426,12 +430,12 @@ __device__ __forceinline__ void stream_long(ChunkStage<V> &sg, int cnt, const De
                                             Visit visit) {
     const int lane = threadIdx.x & 31;
     while (true) {
-        int t = 0;
-        if (lane == 0) t = atomicAdd(&sg.ctr, 1);
-        t = __shfl_sync(kFull, t, 0);
-        if (t >= cnt) break;
+        int i = 0;
+        if (lane == 0) i = atomicAdd(&sg.ctr, 1);
+        i = __shfl_sync(kFull, i, 0);
+        if (i >= cnt) break;
+        const int t = sg.llist[i];
         const int32_t L = sg.len[t];
-        if (L < kLongRow) continue;
         const int32_t *bc = B.col + sg.bs[t];
         const V *bv = (const V *)B.val + sg.bs[t];
         const V a = NUMERIC ? sg.va[t] : (V)0;
@@ -648,6 +652,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                                                          bool abort_mode) {
     constexpr int NT = kDenseThreads;
     constexpr int kPull = 4;   // register accumulators per thread: windows of up to 4 * NT columns
+    static_assert(kChunk == NT, "the dense kernel stages one A entry per thread");
     constexpr int IPT = kChunk / NT;
     constexpr int NW = NT / 32;
     using AtomV = typename std::conditional<sizeof(V) == 4, unsigned int, unsigned long long>::type;
@@ -711,6 +716,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
             for (int64_t k0 = a0; k0 < a1; k0 += kChunk) {
                 const int n = (int)(a1 - k0 < (int64_t)kChunk ? a1 - k0 : (int64_t)kChunk);
                 int64_t len[IPT];
+                bool full = false, lng = false;
 #pragma unroll
                 for (int i = 0; i < IPT; i++) {
                     const int t = tid * IPT + i;
@@ -734,32 +740,68 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                             if (hi < be) my_next = min(my_next, B.col[hi]);
                         }
                         sg.bs[t] = lo;
-                        const bool full = pull_ok && hi - lo == wc;
-                        sg.len[t] = full ? -1 : (int32_t)(hi - lo);
+                        full = pull_ok && hi - lo == wc;
+                        lng = !full && hi - lo >= kLongRow;
+                        sg.len[t] = (int32_t)(hi - lo);
                         if (NUMERIC) sg.va[t] = Aval[k];
-                        len[i] = (full || hi - lo >= kLongRow) ? 0 : hi - lo;   // long ones: stream_long
+                        len[i] = (full || lng) ? 0 : hi - lo;   // short segments: flattened stream
                     }
+                }
+                // lists of long and full entries (one entry per thread: kChunk == NT)
+                const unsigned lb = __ballot_sync(kFull, lng), fb = __ballot_sync(kFull, full);
+                if (lane == 0) {
+                    sg.wl[warp] = __popc(lb);
+                    sg.wf[warp] = __popc(fb);
                 }
                 if (tid == 0) sg.ctr = 0;
                 stage_scan<NT>(len, sg.pre, sg.warp_tot);
-                stream_long<V, NUMERIC>(sg, n, B, checked, ovf, visit);
+                {
+                    int pl = 0, pf = 0, tl = 0, tf = 0;
+#pragma unroll
+                    for (int w = 0; w < NW; w++) {
+                        if (w < warp) {
+                            pl += sg.wl[w];
+                            pf += sg.wf[w];
+                        }
+                        tl += sg.wl[w];
+                        tf += sg.wf[w];
+                    }
+                    if (lng) sg.llist[pl + __popc(lb & lt_mask)] = tid;
+                    if (full) sg.flist[pf + __popc(fb & lt_mask)] = tid;
+                    if (tid == 0) {
+                        sg.nlong = tl;
+                        sg.nfull = tf;
+                    }
+                }
+                __syncthreads();
+                if (sg.nlong) stream_long<V, NUMERIC>(sg, sg.nlong, B, checked, ovf, visit);
                 stream_chunk<NT, V, NUMERIC>(sg, n, B, checked, ovf, visit);
-                if (pull_ok) {
-                    for (int t = 0; t < n; t++) {
-                        if (sg.len[t] != -1) continue;   // uniform: every thread reads the same flag
-                        pulled = true;
-                        const V a = sg.va[t];
+                const int nfull = sg.nfull;
+                for (int i0 = 0; i0 < nfull; i0 += 4) {
+                    // four full entries per step: sixteen independent loads per thread
+                    pulled = true;
+                    V bvals[4][kPull];
+                    V av[4];
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        const bool ok = i0 + e < nfull;
+                        const int t = sg.flist[ok ? i0 + e : i0];
+                        av[e] = ok ? sg.va[t] : (V)0;
                         const V *bv = Bval + sg.bs[t];
 #pragma unroll
                         for (int j = 0; j < kPull; j++) {
                             const int c = tid + j * NT;
-                            if (c < wc) {
-                                const V p = checked ? mul_chk(a, bv[c], ovf) : (V)(a * bv[c]);
-                                if (checked) ovf |= preg[j] > (V)~(V)0 - p;
-                                preg[j] += p;
-                            }
+                            bvals[e][j] = (ok && c < wc) ? bv[c] : (V)0;
                         }
                     }
+#pragma unroll
+                    for (int e = 0; e < 4; e++)
+#pragma unroll
+                        for (int j = 0; j < kPull; j++) {
+                            const V p = checked ? mul_chk(av[e], bvals[e][j], ovf) : (V)(av[e] * bvals[e][j]);
+                            if (checked) ovf |= preg[j] > (V)~(V)0 - p;
+                            preg[j] += p;
+                        }
                 }
                 __syncthreads();
             }
