@@ -96,7 +96,7 @@ typedef struct rmcm_product_stats {
     int64_t bytes_a, bytes_b_touched, bytes_c;   /* level 2 only */
     double analyze_ms, symbolic_ms, numeric_ms;  /* CUDA-event times on the handle's stream */
     int32_t valtype;
-    int32_t bin_rows[5];                /* rows per bin: tiny, hash512, hash2k, hash8k, dense */
+    int32_t bin_rows[6];                /* rows per bin: tiny, hash512, hash2k, hash8k, dense, rank */
 } rmcm_product_stats;
 
 /* ---- handle -------------------------------------------------------------- */

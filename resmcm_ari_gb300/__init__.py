@@ -64,7 +64,7 @@ class ProductStats(C.Structure):
                 ("touched_rows", C.c_int64), ("touched_nnz", C.c_int64),
                 ("bytes_a", C.c_int64), ("bytes_b_touched", C.c_int64), ("bytes_c", C.c_int64),
                 ("analyze_ms", C.c_double), ("symbolic_ms", C.c_double), ("numeric_ms", C.c_double),
-                ("valtype", C.c_int32), ("bin_rows", C.c_int32 * 5)]
+                ("valtype", C.c_int32), ("bin_rows", C.c_int32 * 6)]
 
     def as_dict(self) -> dict:
         d = {f: getattr(self, f) for f, _ in self._fields_ if f != "bin_rows"}

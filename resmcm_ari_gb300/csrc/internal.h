@@ -39,8 +39,9 @@ enum Bin {
     kBinHash512 = 1,   // shared-memory hash tables of 512 / 2048 / 8192 slots
     kBinHash2k = 2,
     kBinHash8k = 3,
-    kBinDense = 4,     // windowed dense accumulator (bitmap + counters) in shared memory
-    kNumBins = 5
+    kBinDense = 4,     // windowed dense accumulator (presence + counters) in shared memory
+    kBinRank = 5,      // whole-row bitmap in shared memory, counts by rank with global atomics
+    kNumBins = 6
 };
 
 // Tunables of the SpGEMM row binning (the autotuner searches these).

@@ -93,15 +93,18 @@ __device__ __forceinline__ int32_t warp_min(int32_t v) {
 
 struct BinParams {
     int64_t dense_win;      // columns one numeric dense window covers
-    int32_t hash_max;       // flops above -> dense
+    int32_t hash_max;       // flops above -> dense or rank
     int32_t dense_ratio;    // dense when flops * ratio >= cols and one window covers cols
 };
+
+// Widest output row the rank bin holds in shared memory (bitmap + prefixes).
+constexpr int64_t kRankCols = 1 << 20;
 
 __device__ __forceinline__ int classify(int64_t f, int64_t ncols, const BinParams &bp) {
     if (f == 0) return kEmptyBin;
     if (f <= 32) return kBinTiny;
     const bool one_window = ncols <= bp.dense_win;
-    if (f > bp.hash_max) return kBinDense;
+    if (f > bp.hash_max) return (!one_window && ncols <= kRankCols) ? kBinRank : kBinDense;
     if (one_window && f * (int64_t)bp.dense_ratio >= ncols) return kBinDense;
     const int64_t need = 2 * min(f, ncols);
     if (need <= 512) return kBinHash512;
@@ -878,6 +881,126 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
     if (__syncthreads_or(ovf) && tid == 0) raise_status(st, kOverflow);
 }
 
+// ------------------------------------------------------------------------
+// rank bin: wide rows (more columns than a dense window, at most kRankCols)
+// ------------------------------------------------------------------------
+//
+// A CTA per row holds a bitmap of the whole output row in shared memory.
+// Symbolic: set the bit of every product's column, count the bits.  Numeric:
+// rebuild the bitmap, turn it into ranks (per 32-word block a prefix of set
+// bits, per word a prefix inside its block), write the sorted columns
+// straight from the bitmap, zero the row's values, then stream the products
+// again and add each one at C.val[row start + rank(column)] with a global
+// atomic.  The cost per row is two or three passes over its products plus one
+// scan of the bitmap, whatever the row's width or product count.
+
+constexpr int kRankThreads = 512;
+
+template <typename V, bool NUMERIC>
+__global__ void __launch_bounds__(kRankThreads) k_rank(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows,
+                                                       int32_t nrows, int64_t *cnt, int *st, const uint8_t *bin_of) {
+    constexpr int NT = kRankThreads;
+    using AtomV = typename std::conditional<sizeof(V) == 4, unsigned int, unsigned long long>::type;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int nblocks = (int)((B.cols + 1023) >> 10);       // 32-word (1024-column) blocks
+    const int nwords = nblocks * 32;
+    uint32_t *bits = (uint32_t *)smem;
+    uint16_t *wpre = (uint16_t *)(bits + nwords);             // NUMERIC only
+    uint32_t *bpre = (uint32_t *)(wpre + nwords);             // NUMERIC only
+    __shared__ ChunkStage<V> sg;
+    __shared__ int s_warp[NT / 32];
+    __shared__ int64_t s_cnt;
+    const int tid = threadIdx.x;
+    bool ovf = false;
+    for (int32_t ri = blockIdx.x; ri < nrows; ri += gridDim.x) {
+        const int32_t r = rows[ri];
+        const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
+        const bool checked = NUMERIC && (bin_of[r] & kRiskyBit) != 0;
+        for (int i = tid; i < nwords / 4; i += NT) ((uint4 *)bits)[i] = make_uint4(0, 0, 0, 0);
+        __syncthreads();
+        auto set_bit = [&](int32_t c, V) { atomicOr(bits + (c >> 5), 1u << (c & 31)); };
+        for (int64_t k0 = a0; k0 < a1; k0 += kChunk) {
+            const int n = (int)(a1 - k0 < (int64_t)kChunk ? a1 - k0 : (int64_t)kChunk);
+            stage_full_rows<NT, V, false>(sg, A, B, k0, n);
+            stream_chunk<NT, V, false>(sg, n, B, false, ovf, set_bit);
+            __syncthreads();
+        }
+        if (!NUMERIC) {
+            int mine = 0;
+            for (int w = tid; w < nwords; w += NT) mine += __popc(bits[w]);
+            int excl;
+            const int total = block_excl_scan<NT>(mine, &excl, s_warp);
+            if (tid == 0) cnt[r] = total;
+            continue;
+        }
+        // ranks: thread t owns a contiguous run of 32-word blocks; per word the
+        // set bits before it inside its block, per block the set bits before it
+        {
+            const int per = (nblocks + NT - 1) / NT;
+            const int b0 = min(tid * per, nblocks), b1 = min(b0 + per, nblocks);
+            int mine = 0;
+            for (int b = b0; b < b1; b++) {
+                int run = 0;
+                for (int j = 0; j < 32; j++) {
+                    wpre[b * 32 + j] = (uint16_t)run;
+                    run += __popc(bits[b * 32 + j]);
+                }
+                bpre[b] = (uint32_t)run;
+                mine += run;
+            }
+            int excl;
+            const int total = block_excl_scan<NT>(mine, &excl, s_warp);
+            for (int b = b0; b < b1; b++) {
+                const uint32_t t = bpre[b];
+                bpre[b] = (uint32_t)excl;
+                excl += (int)t;
+            }
+            if (tid == 0) s_cnt = total;
+            __syncthreads();
+        }
+        const int64_t base = C.rowptr[r];
+        const int64_t rlen = C.rowptr[r + 1] - base;
+        if (tid == 0 && s_cnt != rlen) raise_status(st, kInvariant);
+        // sorted columns straight from the bitmap; zero the row's values
+        for (int w = tid; w < nwords; w += NT) {
+            uint32_t word = bits[w];
+            int64_t pos = (int64_t)bpre[w >> 5] + wpre[w];
+            while (word) {
+                const int b = __ffs(word) - 1;
+                word &= word - 1;
+                if (pos < rlen) {
+                    C.col[base + pos] = w * 32 + b;
+                    ((V *)C.val)[base + pos] = 0;
+                }
+                pos++;
+            }
+        }
+        __syncthreads();
+        // values: every product lands on its column's rank
+        V *vals = (V *)C.val + base;
+        auto add_val = [&](int32_t c, V p) {
+            const int w = c >> 5;
+            const int64_t pos = (int64_t)bpre[w >> 5] + wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u));
+            if (pos < rlen) {
+                if (checked) {
+                    const AtomV old = atomicAdd((AtomV *)(vals + pos), (AtomV)p);
+                    ovf |= old > (AtomV)~(AtomV)0 - (AtomV)p;
+                } else {
+                    atomicAdd((AtomV *)(vals + pos), (AtomV)p);
+                }
+            }
+        };
+        for (int64_t k0 = a0; k0 < a1; k0 += kChunk) {
+            const int n = (int)(a1 - k0 < (int64_t)kChunk ? a1 - k0 : (int64_t)kChunk);
+            stage_full_rows<NT, V, true>(sg, A, B, k0, n);
+            stream_chunk<NT, V, true>(sg, n, B, checked, ovf, add_val);
+            __syncthreads();
+        }
+
+    }
+    if (__syncthreads_or(ovf) && tid == 0) raise_status(st, kOverflow);
+}
+
 // Compacts TEMP-mode slots into C: row rows[ri] has cnt = rowptr[r+1]-rowptr[r]
 // entries at slot ri of the temporary.
 template <typename V>
@@ -1087,6 +1210,16 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                 auto kern = k_hash<V, NUMERIC, S, NT>;
                 RMCM_TRY(set_smem(h, kern, sm));
                 kern<<<grid_for(h, (int64_t)n * NT, NT, 2), NT, sm, s>>>(A, B, C, list, n, cnt, st, bin_of);
+                break;
+            }
+            case kBinRank: {
+                const int64_t nwords = (ncols + 1023) / 1024 * 32;
+                const int64_t sm = NUMERIC ? nwords * 4 + nwords * 2 + (nwords / 32) * 4 : nwords * 4;
+                auto kern = k_rank<V, NUMERIC>;
+                RMCM_TRY(set_smem(h, kern, sm));
+                const int per_sm = (int)std::max<int64_t>(1, std::min<int64_t>(4, (200 * 1024) / std::max<int64_t>(sm, 1)));
+                const int grid = (int)std::min<int64_t>((int64_t)n, (int64_t)h->sm_count * per_sm);
+                kern<<<grid, kRankThreads, sm, s>>>(A, B, C, list, n, cnt, st, bin_of);
                 break;
             }
             case kBinDense: {

@@ -282,3 +282,38 @@ def test_dense_register_path_detects_overflow(native, engine):
                         val=np.full(k, 2, np.uint64), valtype=native.VAL_U64)
     C = engine.spgemm(A64, B64)
     assert set(C.download()[2].tolist()) == {1 << 34}
+
+
+@pytest.mark.parametrize("n", [60_000, 1 << 20])
+def test_rank_bin_for_wide_rows(native, engine, n):
+    """Rows wider than a dense window (up to 2^20 columns) with > 4096 products."""
+    rng = np.random.default_rng(31)
+    m, k = 40, 400
+    A = _random_csr(rng, m, k, rng.integers(100, 300, m), vmax=4)
+    B = _random_csr(rng, k, n, rng.integers(20, 100, k), vmax=4)
+    for vt in (native.VAL_U32, native.VAL_U64):
+        _check_product(native, engine, A, B, vt)
+
+
+def test_rank_bin_detects_overflow(native, engine):
+    import ctypes
+    rng = np.random.default_rng(32)
+    k, n = 200, 300_000
+    B = _random_csr(rng, k, n, np.full(k, 50), vmax=1)
+    B.data[:] = 1 << 26
+    rp = np.array([0, k], np.int64)
+    acol = np.arange(k, dtype=np.int32)
+    for vt, expect in ((native.VAL_U32, native.EOVERFLOW), (native.VAL_U64, native.OK)):
+        Bm = engine.upload(B.indptr, B.indices, cols=n, val=B.data.astype(np.uint64), valtype=vt)
+        Am = engine.upload(rp, acol, cols=k, val=np.full(k, 64, np.uint64), valtype=vt)
+        h = ctypes.c_void_p()
+        rc = native.lib().rmcm_spgemm(engine._h, Am._h, Bm._h, ctypes.byref(h))
+        assert rc == expect
+        if vt == native.VAL_U64:
+            C = native.Matrix(engine, h.value)
+            ref = (sp.csr_matrix((np.full(k, 64, np.int64), acol, rp), shape=(1, k)) @ B.astype(np.int64)).tocsr()
+            ref.sort_indices()
+            got = C.download()
+            assert np.array_equal(got[1], ref.indices) and np.array_equal(got[2].astype(np.int64), ref.data)
+        else:
+            native.lib().rmcm_mat_free(engine._h, h)
