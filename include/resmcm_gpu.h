@@ -56,6 +56,12 @@ typedef enum rmcm_valtype {
     RMCM_VAL_AUTO = 2       /* uint32, re-run in uint64 if a count overflows */
 } rmcm_valtype;
 
+typedef enum rmcm_order_mode {
+    RMCM_ORDER_RES = 0,     /* RES estimates + DP (efficient/resmcm.cpp) */
+    RMCM_ORDER_L2R = 1,     /* left to right, no estimator (efficient/l2r.cpp:725-727) */
+    RMCM_ORDER_DENSE = 2    /* DP over dense dimensions, no estimator (efficient/naive.cpp:506-523) */
+} rmcm_order_mode;
+
 typedef struct rmcm_handle rmcm_handle;
 typedef struct rmcm_graph rmcm_graph;
 typedef struct rmcm_mat rmcm_mat;
@@ -195,6 +201,35 @@ RMCM_API int32_t rmcm_chain(rmcm_handle *h, rmcm_mat *const *chain, int32_t len,
  * which case the result is freed after its nnz is taken. */
 RMCM_API int32_t rmcm_run_metapath(rmcm_handle *h, rmcm_graph *g, const char *metapath, rmcm_mat **C,
                                    rmcm_timings *t);
+
+/* Order used by rmcm_run_metapath / rmcm_chain when no pair list is given.
+ * The ablation orders of the reference's l2r and naive programs skip the
+ * estimator (es time 0), exactly as those programs do. */
+RMCM_API int32_t rmcm_set_order_mode(rmcm_handle *h, int32_t mode);
+/* Left-to-right pair list (0,1), (-1,2), ..., (-1,len-1): efficient/l2r.cpp:725-727. */
+RMCM_API int32_t rmcm_order_l2r(int32_t len, int32_t *pairs);
+/* DP of efficient/naive.cpp:506-523 over dims_vt[len+1] (the vertex counts
+ * of the meta-path's types): cost(i,k,j) = m[i][k] + m[k+1][j] +
+ * d[i]*d[k]*d[j+1], the product taken in 32-bit two's-complement int
+ * arithmetic as the reference's `vertex` (int) operands do, then widened to
+ * double; strict '<' keeps the smallest k.  split/cost may be NULL. */
+RMCM_API int32_t rmcm_order_dense(const int64_t *dims_vt, int32_t len, int32_t *split, double *cost,
+                                  int32_t *pairs);
+
+/* ---- graph cache and result sinks -----------------------------------------
+ * Binary form of a typed graph (vertex types and typed adjacency), so a graph
+ * parsed once from text loads in one read: "RMCMHIN1", n, m, max_vt, then
+ * vtype[n] int32, adj_ptr[n+1] int64, adj_nbr[m] int32, adj_et[m] int32
+ * (little endian). */
+RMCM_API int32_t rmcm_graph_save(const rmcm_graph *g, const char *path);
+RMCM_API int32_t rmcm_graph_load(rmcm_handle *h, const char *path, rmcm_graph **out);
+/* Global vertex ids of the vertices of type vt in local-id order (ascending;
+ * the order of HeteroGraph::bins).  out needs rmcm_graph_dim(g, vt) slots. */
+RMCM_API int32_t rmcm_graph_global_ids(const rmcm_graph *g, int32_t vt, int32_t *out);
+/* A matrix to a binary file: "RMCMCSR1", rows, cols, nnz (int64), valtype
+ * (int32), 4 bytes padding, rowptr[rows+1] int64, col[nnz] int32,
+ * val[nnz] uint32 or uint64. */
+RMCM_API int32_t rmcm_mat_save(rmcm_handle *h, const rmcm_mat *m, const char *path);
 
 /* Estimated nnz of the whole chain, c_[0][len-1]: the estimator-only program
  * accuracy/res.cpp (final_result_estimate :564-600, output :698). */

@@ -23,6 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libref_resmcm.so")
 REF_CLI_PATH = os.path.join(HERE, "_ref", "resmcm")
+REF_NAIVE_LIB_PATH = os.path.join(HERE, "_ref", "libref_naive.so")
 DEFAULT_REF = "/root/reference"
 
 MODE_BOOL, MODE_COUNT = 0, 1
@@ -251,6 +252,20 @@ def ref_lib():
                                 C.POINTER(C.POINTER(C.c_int32))]
         _ref = L
     return _ref
+
+
+def ref_naive_order(dims_by_type, vts):
+    """The reference naive.cpp DP over type dimensions → (split, m, pairs)."""
+    L = C.CDLL(REF_NAIVE_LIB_PATH)
+    L.ref_naive_order.argtypes = [_i32p, C.c_int32, _i32p, C.c_int32, _i32p, _f64p, _i32p]
+    dims = np.ascontiguousarray(dims_by_type, np.int32)
+    v = np.ascontiguousarray(vts, np.int32)
+    n = v.size - 1
+    split = np.zeros(n * n, np.int32)
+    m = np.zeros(n * n, np.float64)
+    pairs = np.zeros(max(2 * (n - 1), 1), np.int32)
+    L.ref_naive_order(dims, dims.size, v, n, split, m, pairs)
+    return split.reshape(n, n), m.reshape(n, n), pairs[:2 * (n - 1)].reshape(-1, 2)
 
 
 class RefGraph:

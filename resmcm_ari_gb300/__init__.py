@@ -35,6 +35,7 @@ CLI_PATH = os.path.join(_PKG, "_build", "resmcm_gpu")
 HEADER_PATH = os.path.join(os.path.dirname(_PKG), "include", "resmcm_gpu.h")
 
 OK, EINVAL, ENOMEM, EOVERFLOW, ETIMEOUT, ECUDA, EIO, EPARSE, EINTERNAL = range(9)
+ORDER_RES, ORDER_L2R, ORDER_DENSE = 0, 1, 2
 VAL_U32, VAL_U64, VAL_AUTO = 0, 1, 2
 _VAL_DTYPE = {VAL_U32: np.uint32, VAL_U64: np.uint64}
 
@@ -119,6 +120,13 @@ def lib():
         "rmcm_chain": ([vp, vp, i32, vp, pp, C.POINTER(Timings)], i32),
         "rmcm_run_metapath": ([vp, vp, C.c_char_p, pp, C.POINTER(Timings)], i32),
         "rmcm_estimate_metapath": ([vp, vp, C.c_char_p, f64p], i32),
+        "rmcm_set_order_mode": ([vp, i32], i32),
+        "rmcm_order_l2r": ([i32, vp], i32),
+        "rmcm_order_dense": ([vp, i32, vp, vp, vp], i32),
+        "rmcm_graph_save": ([vp, C.c_char_p], i32),
+        "rmcm_graph_load": ([vp, C.c_char_p, pp], i32),
+        "rmcm_graph_global_ids": ([vp, i32, vp], i32),
+        "rmcm_mat_save": ([vp, vp, C.c_char_p], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -126,6 +134,41 @@ def lib():
         fn.restype = res
     _lib = L
     return L
+
+
+def order_l2r(length: int) -> np.ndarray:
+    """Pair list of the left-to-right order (efficient/l2r.cpp:725-727)."""
+    out = np.zeros(2 * (length - 1), np.int32)
+    rc = lib().rmcm_order_l2r(length, _ptr(out))
+    if rc != OK:
+        raise RmcmError(rc, "order_l2r")
+    return out.reshape(-1, 2)
+
+
+def order_dense(dims_vt) -> tuple:
+    """Dense-dimension DP of efficient/naive.cpp:506-523 → (split, cost, pairs)."""
+    d = np.ascontiguousarray(dims_vt, np.int64)
+    L = d.size - 1
+    split = np.zeros(L * L, np.int32)
+    cost = np.zeros(L * L, np.float64)
+    pairs = np.zeros(max(2 * (L - 1), 1), np.int32)
+    rc = lib().rmcm_order_dense(_ptr(d), L, _ptr(split), _ptr(cost), _ptr(pairs))
+    if rc != OK:
+        raise RmcmError(rc, "order_dense")
+    return split.reshape(L, L), cost.reshape(L, L), pairs[:2 * (L - 1)].reshape(-1, 2)
+
+
+def read_csr(path: str):
+    """Read a result written by rmcm_mat_save → (rows, cols, rowptr, col, val)."""
+    with open(path, "rb") as f:
+        if f.read(8) != b"RMCMCSR1":
+            raise ValueError(f"not a result file: {path}")
+        rows, cols, nnz = np.frombuffer(f.read(24), np.int64)
+        valtype = int(np.frombuffer(f.read(8), np.int32)[0])
+        rp = np.frombuffer(f.read(8 * (rows + 1)), np.int64)
+        col = np.frombuffer(f.read(4 * nnz), np.int32)
+        val = np.frombuffer(f.read(_VAL_DTYPE[valtype]().itemsize * nnz), _VAL_DTYPE[valtype])
+    return int(rows), int(cols), rp, col, val
 
 
 def header_symbols() -> list:
@@ -200,6 +243,9 @@ class Matrix:
                                                    _ptr(val) if values else None))
         return rp, col[:nnz], (val[:nnz] if values else None)
 
+    def save(self, path: str):
+        self.engine._check(lib().rmcm_mat_save(self.engine._h, self._h, path.encode()))
+
     def free(self):
         if self.owned and self._h:
             lib().rmcm_mat_free(self.engine._h, self._h)
@@ -241,6 +287,23 @@ class HeteroGraph:
     def from_synthetic(cls, engine: "Engine", g) -> "HeteroGraph":
         ptr, nbr, et = g.adjacency()
         return cls.from_adjacency(engine, g.vertex_types(), ptr, nbr, et)
+
+    @classmethod
+    def load(cls, engine: "Engine", path: str) -> "HeteroGraph":
+        """Binary graph cache written by save()."""
+        h = C.c_void_p()
+        engine._check(lib().rmcm_graph_load(engine._h, path.encode(), C.byref(h)))
+        return cls(engine, h.value)
+
+    def save(self, path: str):
+        rc = lib().rmcm_graph_save(self._h, path.encode())
+        if rc != OK:
+            raise RmcmError(rc, f"cannot write graph cache {path}")
+
+    def global_ids(self, vt: int) -> np.ndarray:
+        out = np.zeros(max(self.dim(vt), 1), np.int32)
+        lib().rmcm_graph_global_ids(self._h, vt, _ptr(out))
+        return out[:self.dim(vt)]
 
     def info(self):
         n, m, mv = C.c_int64(), C.c_int64(), C.c_int32()
@@ -315,6 +378,9 @@ class Engine:
     @property
     def kernel_launches(self) -> int:
         return lib().rmcm_kernel_launches(self._h)
+
+    def set_order_mode(self, mode: int):
+        self._check(lib().rmcm_set_order_mode(self._h, mode))
 
     def set_profiling(self, level: int):
         self._check(lib().rmcm_set_profiling(self._h, level))

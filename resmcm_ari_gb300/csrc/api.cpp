@@ -10,6 +10,7 @@
 #include <omp.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -443,6 +444,39 @@ int32_t copy_mat(rmcm_handle *h, const rmcm_mat *src, rmcm_mat **out) {
     return RMCM_OK;
 }
 
+// Post-order (k, l) pair list of a split table (get_optimal_chain_order,
+// efficient/resmcm.cpp:563-573).
+int32_t post_order(const std::vector<int32_t> &split, int32_t len, int32_t i, int32_t j, std::vector<int32_t> &out) {
+    if (i == j) return i;
+    const int32_t k = split[i * len + j];
+    const int32_t a = post_order(split, len, i, k, out);
+    const int32_t b = post_order(split, len, k + 1, j, out);
+    out.push_back(a);
+    out.push_back(b);
+    return -1;
+}
+
+// DP of efficient/naive.cpp:506-523 (dense dimension costs).
+void dense_order(const int64_t *d, int32_t len, std::vector<int32_t> &split, std::vector<double> &m) {
+    split.assign(len * len, 0);
+    m.assign(len * len, 0.0);
+    for (int32_t l = 1; l < len; l++) {
+        for (int32_t i = 0; i < len - l; i++) {
+            const int32_t j = i + l;
+            m[i * len + j] = DBL_MAX;
+            for (int32_t k = i; k < j; k++) {
+                // `vertex` (int) operands: the product wraps in 32 bits
+                const uint32_t p = (uint32_t)d[i] * (uint32_t)d[k] * (uint32_t)d[j + 1];
+                const double cost = m[i * len + k] + m[(k + 1) * len + j] + (double)(int32_t)p;
+                if (cost < m[i * len + j]) {
+                    m[i * len + j] = cost;
+                    split[i * len + j] = k;
+                }
+            }
+        }
+    }
+}
+
 // SSP_dynamic on device-resident matrices (see file comment).
 //
 // With `widen` set, products run in uint32 and the chain escalates to uint64
@@ -476,12 +510,40 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
     }
     cudaEvent_t *ev = h->ev;
     RMCM_CUDA(h, cudaEventRecord(ev[0], s));
+    int32_t pairs[32];
+    int32_t rc = RMCM_OK;
+    double host_dp_s = -1;
+    if (!fixed_pairs && h->order_mode != RMCM_ORDER_RES) {
+        // ablation orders: no estimator, order computed on the host
+        cudaEventRecord(ev[1], s);
+        const auto t0 = std::chrono::steady_clock::now();
+        std::vector<int32_t> pl;
+        if (h->order_mode == RMCM_ORDER_L2R) {
+            pl.resize(2 * (len - 1));
+            rmcm_order_l2r(len, pl.data());
+        } else {
+            std::vector<int64_t> d(len + 1);
+            for (int i = 0; i < len; i++) d[i] = mats[i]->d.rows;
+            d[len] = mats[len - 1]->d.cols;
+            std::vector<int32_t> split;
+            std::vector<double> m;
+            dense_order(d.data(), len, split, m);
+            post_order(split, len, 0, len - 1, pl);
+        }
+        host_dp_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        memcpy(pairs, pl.data(), sizeof(int32_t) * 2 * (len - 1));
+        cudaEventRecord(ev[2], s);
+        fixed_pairs = pairs;
+    }
+    if (fixed_pairs == pairs) {
+        // order already known
+    } else {
     // (a) estimator
     double *c_dev = nullptr;
     char *ord = nullptr;
     const int64_t ord_bytes = 8 * 256 + 4 * 256 + 4 * 64;
     RMCM_TRY(dev_alloc(h, (void **)&c_dev, 8 * 256));
-    int32_t rc = estimate(h, mats, len, c_dev);
+    rc = estimate(h, mats, len, c_dev);
     if (rc == RMCM_OK) rc = dev_alloc(h, (void **)&ord, ord_bytes);
     if (rc != RMCM_OK) {
         dev_free(h, c_dev, 8 * 256);
@@ -492,7 +554,6 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
     int32_t *pairs_dev = (int32_t *)(ord + 8 * 256 + 4 * 256);
     rc = chain_order_dev(h, c_dev, len, (int32_t *)(ord + 8 * 256), (double *)ord, pairs_dev);
     cudaEventRecord(ev[2], s);
-    int32_t pairs[32];
     if (rc == RMCM_OK) {
         if (fixed_pairs) {
             memcpy(pairs, fixed_pairs, sizeof(int32_t) * 2 * (len - 1));
@@ -506,6 +567,7 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
     dev_free(h, ord, ord_bytes);
     dev_free(h, c_dev, 8 * 256);
     if (rc != RMCM_OK) return rc;
+    }
     // validate the pair list against the stack machine before running it
     {
         int depth = 0;
@@ -620,7 +682,7 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
     cudaEventRecord(ev[5], s);
     RMCM_CUDA(h, cudaEventSynchronize(ev[5]));
     tm.es_s = elapsed_s(ev[0], ev[1]);
-    tm.dp_s = elapsed_s(ev[1], ev[2]);
+    tm.dp_s = host_dp_s >= 0 ? host_dp_s : elapsed_s(ev[1], ev[2]);
     tm.spgemm_s = spgemm_s;
     tm.total_s = elapsed_s(ev[0], ev[5]);
     tm.valtype = cur;
@@ -1055,6 +1117,102 @@ RMCM_API int32_t rmcm_run_metapath(rmcm_handle *h, rmcm_graph *g, const char *me
         mat_release(h, res);
     }
     return rc;
+}
+
+RMCM_API int32_t rmcm_set_order_mode(rmcm_handle *h, int32_t mode) {
+    if (!h || mode < RMCM_ORDER_RES || mode > RMCM_ORDER_DENSE) return RMCM_EINVAL;
+    h->order_mode = mode;
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_order_l2r(int32_t len, int32_t *pairs) {
+    if (len < 2 || !pairs) return RMCM_EINVAL;
+    pairs[0] = 0;
+    pairs[1] = 1;
+    for (int32_t i = 2; i < len; i++) {
+        pairs[2 * (i - 1)] = -1;
+        pairs[2 * (i - 1) + 1] = i;
+    }
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_order_dense(const int64_t *dims_vt, int32_t len, int32_t *split, double *cost, int32_t *pairs) {
+    if (!dims_vt || len < 1 || len > 64) return RMCM_EINVAL;
+    std::vector<int32_t> sp;
+    std::vector<double> m;
+    dense_order(dims_vt, len, sp, m);
+    if (split) std::copy(sp.begin(), sp.end(), split);
+    if (cost) std::copy(m.begin(), m.end(), cost);
+    if (pairs && len > 1) {
+        std::vector<int32_t> pl;
+        post_order(sp, len, 0, len - 1, pl);
+        std::copy(pl.begin(), pl.end(), pairs);
+    }
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_graph_save(const rmcm_graph *g, const char *path) {
+    if (!g || !path) return RMCM_EINVAL;
+    FILE *f = fopen(path, "wb");
+    if (!f) return RMCM_EIO;
+    const char magic[8] = {'R', 'M', 'C', 'M', 'H', 'I', 'N', '1'};
+    const int64_t hdr[2] = {g->n, g->m};
+    const int32_t hdr2[2] = {g->max_vt, 0};
+    bool ok = fwrite(magic, 1, 8, f) == 8 && fwrite(hdr, 8, 2, f) == 2 && fwrite(hdr2, 4, 2, f) == 2;
+    ok = ok && (g->n == 0 || fwrite(g->vtype.data(), 4, g->n, f) == (size_t)g->n);
+    ok = ok && fwrite(g->adj_ptr.data(), 8, g->n + 1, f) == (size_t)(g->n + 1);
+    ok = ok && (g->m == 0 || fwrite(g->adj_nbr.data(), 4, g->m, f) == (size_t)g->m);
+    ok = ok && (g->m == 0 || fwrite(g->adj_et.data(), 4, g->m, f) == (size_t)g->m);
+    ok = (fclose(f) == 0) && ok;
+    return ok ? RMCM_OK : RMCM_EIO;
+}
+
+RMCM_API int32_t rmcm_graph_load(rmcm_handle *h, const char *path, rmcm_graph **out) {
+    if (!h || !path || !out) return RMCM_EINVAL;
+    *out = nullptr;
+    FILE *f = fopen(path, "rb");
+    if (!f) return set_error(h, RMCM_EIO, std::string("cannot open ") + path);
+    char magic[8];
+    int64_t hdr[2];
+    int32_t hdr2[2];
+    if (fread(magic, 1, 8, f) != 8 || memcmp(magic, "RMCMHIN1", 8) != 0 || fread(hdr, 8, 2, f) != 2 ||
+        fread(hdr2, 4, 2, f) != 2 || hdr[0] < 0 || hdr[1] < 0) {
+        fclose(f);
+        return set_error(h, RMCM_EPARSE, std::string("not a graph cache file: ") + path);
+    }
+    const int64_t n = hdr[0], m = hdr[1];
+    std::vector<int32_t> vt(n), nbr(m), et(m);
+    std::vector<int64_t> ptr(n + 1);
+    bool ok = (n == 0 || fread(vt.data(), 4, n, f) == (size_t)n) && fread(ptr.data(), 8, n + 1, f) == (size_t)(n + 1) &&
+              (m == 0 || fread(nbr.data(), 4, m, f) == (size_t)m) && (m == 0 || fread(et.data(), 4, m, f) == (size_t)m);
+    fclose(f);
+    if (!ok || ptr[n] != m) return set_error(h, RMCM_EPARSE, std::string("truncated graph cache file: ") + path);
+    return rmcm_graph_from_adjacency(h, n, vt.data(), ptr.data(), nbr.data(), et.data(), out);
+}
+
+RMCM_API int32_t rmcm_graph_global_ids(const rmcm_graph *g, int32_t vt, int32_t *out) {
+    if (!g || !out || vt < 0 || vt > g->max_vt) return RMCM_EINVAL;
+    std::copy(g->bin_ids.begin() + g->bin_ptr[vt], g->bin_ids.begin() + g->bin_ptr[vt + 1], out);
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_mat_save(rmcm_handle *h, const rmcm_mat *m, const char *path) {
+    if (!h || !m || !path) return RMCM_EINVAL;
+    std::vector<int64_t> rp(m->d.rows + 1);
+    std::vector<int32_t> col(std::max<int64_t>(m->d.nnz, 1));
+    std::vector<char> val(std::max<int64_t>(m->d.nnz * val_bytes(m->valtype), 1));
+    RMCM_TRY(rmcm_mat_download(h, m, rp.data(), col.data(), val.data()));
+    FILE *f = fopen(path, "wb");
+    if (!f) return set_error(h, RMCM_EIO, std::string("cannot write ") + path);
+    const char magic[8] = {'R', 'M', 'C', 'M', 'C', 'S', 'R', '1'};
+    const int64_t hdr[3] = {m->d.rows, m->d.cols, m->d.nnz};
+    const int32_t hdr2[2] = {m->valtype, 0};
+    bool ok = fwrite(magic, 1, 8, f) == 8 && fwrite(hdr, 8, 3, f) == 3 && fwrite(hdr2, 4, 2, f) == 2 &&
+              fwrite(rp.data(), 8, rp.size(), f) == rp.size();
+    ok = ok && (m->d.nnz == 0 || (fwrite(col.data(), 4, m->d.nnz, f) == (size_t)m->d.nnz &&
+                                  fwrite(val.data(), val_bytes(m->valtype), m->d.nnz, f) == (size_t)m->d.nnz));
+    ok = (fclose(f) == 0) && ok;
+    return ok ? RMCM_OK : set_error(h, RMCM_EIO, std::string("short write to ") + path);
 }
 
 RMCM_API int32_t rmcm_estimate_metapath(rmcm_handle *h, rmcm_graph *g, const char *metapath, double *est_nnz) {

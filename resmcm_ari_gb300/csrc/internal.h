@@ -97,6 +97,7 @@ struct rmcm_handle {
     std::vector<rmcm::ProdRecord> prof;
     std::set<rmcm_graph *> graphs;   // graphs whose leaves live on this handle
     bool abort_on_certain_overflow = false;   // spgemm returns EOVERFLOW before computing when sure
+    int32_t order_mode = RMCM_ORDER_RES;
 };
 
 struct rmcm_graph {

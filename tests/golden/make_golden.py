@@ -110,6 +110,11 @@ def main():
                 if L >= 2:
                     c, m, s, pairs = rg.estimate(mp, threads=1)
                     rec.update({"c": c.tolist(), "m": m.tolist(), "split": s.tolist(), "pairs": pairs.tolist()})
+                    # dense-dimension order of efficient/naive.cpp (no estimator)
+                    vts = oracle.parse_metapath(mp)[0]
+                    dims = [g.type_sizes[t] if t < len(g.type_sizes) else 0 for t in range(max(vts) + 1)]
+                    ds, dm, dp = oracle.ref_naive_order(dims, vts)
+                    rec.update({"dense_split": ds.tolist(), "dense_m": dm.tolist(), "dense_pairs": dp.tolist()})
                 rowptr, col, nnz, _ = rg.chain(mp, threads=8)
                 rec["nnz"] = int(nnz)
                 rec["rows"] = int(rowptr.size - 1)

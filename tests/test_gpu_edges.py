@@ -317,3 +317,69 @@ def test_rank_bin_detects_overflow(native, engine):
             assert np.array_equal(got[1], ref.indices) and np.array_equal(got[2].astype(np.int64), ref.data)
         else:
             native.lib().rmcm_mat_free(engine._h, h)
+
+
+@pytest.mark.parametrize("mode", ["l2r", "dense"])
+def test_ablation_orders_give_the_same_result(native, mode):
+    from helpers import load_fixture, make_graph
+    fx = load_fixture("dblp_small")
+    eng = native.Engine(device=0)
+    hg = native.HeteroGraph.from_synthetic(eng, make_graph(fx))
+    refs = {}
+    for rec in fx["paths"][:5]:
+        C, t, _ = eng.run_metapath(hg, rec["metapath"])
+        refs[rec["metapath"]] = C.download()
+        C.free()
+    eng.set_order_mode(native.ORDER_L2R if mode == "l2r" else native.ORDER_DENSE)
+    for rec in fx["paths"][:5]:
+        C, t, _ = eng.run_metapath(hg, rec["metapath"])
+        got = C.download()
+        C.free()
+        for a, b in zip(refs[rec["metapath"]], got):
+            assert np.array_equal(a, b), rec["metapath"]
+        if rec["len"] >= 2:
+            assert t["es_s"] == 0.0
+    hg.close()
+    eng.close()
+
+
+def test_graph_cache_roundtrip(native, engine, tmp_path):
+    g = synth.dblp_like(n_a=3000, n_p=6000, n_v=20, seed=7)
+    hg = native.HeteroGraph.from_synthetic(engine, g)
+    path = str(tmp_path / "g.bin")
+    hg.save(path)
+    hg2 = native.HeteroGraph.load(engine, path)
+    assert hg2.info() == hg.info()
+    a, _, _ = engine.run_metapath(hg, "1-3-0-1-2-4-0-0-1")
+    b, _, _ = engine.run_metapath(hg2, "1-3-0-1-2-4-0-0-1")
+    for x, y in zip(a.download(), b.download()):
+        assert np.array_equal(x, y)
+    assert np.array_equal(hg2.global_ids(1), np.arange(6000, 9000))
+
+
+def test_cli_flags(native, tmp_path):
+    g = synth.tiny_dblp()
+    files = g.write_text(str(tmp_path))
+    run = lambda *extra: subprocess.run([native.CLI_PATH, "4", "1", files["graph"], files["vertex"], files["edge"],
+                                         files["metapaths"], *extra], capture_output=True, text=True, timeout=300)
+    # estimator only: accuracy/res line format
+    est = tmp_path / "est.txt"
+    r = run(str(est), "--estimate-only")
+    assert r.returncode == 0, r.stderr
+    lines = est.read_text().splitlines()
+    assert [ln.split()[0] for ln in lines] == g.metapaths and all(len(ln.split()) == 2 for ln in lines)
+    # cache + result sinks
+    cache = tmp_path / "g.bin"
+    res_dir = tmp_path / "res"
+    cnt_dir = tmp_path / "cnt"
+    res_dir.mkdir()
+    cnt_dir.mkdir()
+    for _ in range(2):   # second run reads the cache
+        out = tmp_path / "out.txt"
+        r = run(str(out), f"--cache={cache}", f"--save-result={res_dir}", f"--row-counts={cnt_dir}", "--order=l2r")
+        assert r.returncode == 0, r.stderr
+        assert cache.exists()
+    rows, cols, rp, col, val = native.read_csr(str(res_dir / "1-3-0-0-1.csr"))
+    assert (rows, cols) == (3, 3) and int(rp[-1]) == 7 and set(val.tolist()) <= {1, 2}
+    cnt = (cnt_dir / "1-3-0-0-1.cnt").read_text().split()
+    assert cnt == ["4", "3", "5", "2", "6", "2"]        # global author ids 4..6 and their row sizes
