@@ -681,7 +681,8 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
     }
     cudaEventRecord(ev[5], s);
     RMCM_CUDA(h, cudaEventSynchronize(ev[5]));
-    tm.es_s = elapsed_s(ev[0], ev[1]);
+    // the ablation orders run no estimator, as efficient/l2r.cpp and naive.cpp
+    tm.es_s = host_dp_s >= 0 ? 0.0 : elapsed_s(ev[0], ev[1]);
     tm.dp_s = host_dp_s >= 0 ? host_dp_s : elapsed_s(ev[1], ev[2]);
     tm.spgemm_s = spgemm_s;
     tm.total_s = elapsed_s(ev[0], ev[5]);
