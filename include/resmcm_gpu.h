@@ -65,6 +65,7 @@ typedef enum rmcm_order_mode {
 typedef struct rmcm_handle rmcm_handle;
 typedef struct rmcm_graph rmcm_graph;
 typedef struct rmcm_mat rmcm_mat;
+typedef struct rmcm_batch rmcm_batch;
 
 typedef struct rmcm_opts {
     int32_t device;            /* CUDA device ordinal */
@@ -235,6 +236,36 @@ RMCM_API int32_t rmcm_mat_save(rmcm_handle *h, const rmcm_mat *m, const char *pa
  * accuracy/res.cpp (final_result_estimate :564-600, output :698). */
 RMCM_API int32_t rmcm_estimate_metapath(rmcm_handle *h, rmcm_graph *g, const char *metapath,
                                         double *est_nnz);
+
+/* ---- batches ---------------------------------------------------------------
+ * Many meta-paths over one graph, each computed exactly as rmcm_run_metapath
+ * computes it (RES estimate, DP order, SpGEMM chain, uint32 with escalation
+ * in AUTO mode).  The reference runs its meta-paths one after another in
+ * main() (efficient/resmcm.cpp:839-889); a batch runs them all at once.
+ * rmcm_batch_create runs every path once through the ordinary executor and
+ * records each device step with the sizes it read back, then captures the
+ * whole set into one CUDA graph over `lanes` concurrent streams (<= 0: 8),
+ * longest chains first onto the least-loaded lane.  rmcm_batch_run launches
+ * that graph: every estimate, order and product is computed again on the
+ * device with no host round trip, and per path the result nnz and an
+ * order-free digest of the result (rmcm_mat_digest) come back.  The result
+ * matrices themselves are freed inside the graph.  A product whose replayed
+ * size differs from its record returns RMCM_EINTERNAL.  The graph's leaves
+ * must stay loaded: rmcm_graph_free fails while a batch uses the graph, and
+ * rmcm_destroy frees the handle's batches.  Only RMCM_ORDER_RES is batched. */
+RMCM_API int32_t rmcm_batch_create(rmcm_handle *h, rmcm_graph *g, const char *const *metapaths,
+                                   int32_t count, int32_t lanes, rmcm_batch **out);
+/* nnz_out[count], digest_out[count] may be NULL; seconds = device time of
+ * the graph launch (CUDA events on the handle's stream). */
+RMCM_API int32_t rmcm_batch_run(rmcm_handle *h, rmcm_batch *b, int64_t *nnz_out, uint64_t *digest_out,
+                                double *seconds);
+RMCM_API int32_t rmcm_batch_info(const rmcm_batch *b, int32_t *count, int32_t *lanes,
+                                 int64_t *launches_per_run, int64_t *graph_nodes);
+RMCM_API int32_t rmcm_batch_free(rmcm_handle *h, rmcm_batch *b);
+/* nnz and an entry-order-free 64-bit digest of a matrix: the sum mod 2^64
+ * over entries (r, c, v) of f(f(r * 2^32 + c) + v), f the splitmix64 output
+ * function.  Equal matrices give equal digests.  Synchronises the stream. */
+RMCM_API int32_t rmcm_mat_digest(rmcm_handle *h, const rmcm_mat *m, uint64_t *nnz, uint64_t *digest);
 
 /* ---- RES estimator that allocates nothing --------------------------------
  * No counterpart in the reference.  For callers that may not allocate device

@@ -127,6 +127,11 @@ def lib():
         "rmcm_graph_load": ([vp, C.c_char_p, pp], i32),
         "rmcm_graph_global_ids": ([vp, i32, vp], i32),
         "rmcm_mat_save": ([vp, vp, C.c_char_p], i32),
+        "rmcm_batch_create": ([vp, vp, vp, i32, i32, pp], i32),
+        "rmcm_batch_run": ([vp, vp, vp, vp, f64p], i32),
+        "rmcm_batch_info": ([vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)], i32),
+        "rmcm_batch_free": ([vp, vp], i32),
+        "rmcm_mat_digest": ([vp, vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -326,12 +331,73 @@ class HeteroGraph:
 
     def close(self):
         if self._h:
-            lib().rmcm_graph_free(self._h)
+            rc = lib().rmcm_graph_free(self._h)
+            if rc != OK:
+                raise RmcmError(rc, "graph_free: a batch still replays this graph's leaves")
             self._h = C.c_void_p()
 
     def __del__(self):
         try:
             self.close()
+        except Exception:
+            pass
+
+
+def _mix64(x: np.ndarray) -> np.ndarray:
+    """splitmix64 output function (Steele, Lea and Flood, OOPSLA 2014)."""
+    x = x ^ (x >> np.uint64(30))
+    x = x * np.uint64(0xBF58476D1CE4E5B9)
+    x = x ^ (x >> np.uint64(27))
+    x = x * np.uint64(0x94D049BB133111EB)
+    return x ^ (x >> np.uint64(31))
+
+
+def csr_digest(rowptr, col, val=None) -> tuple:
+    """(nnz, digest) of a host CSR, the same function as rmcm_mat_digest:
+    the sum mod 2^64 over entries (r, c, v) of mix(mix(r * 2^32 + c) + v)."""
+    rowptr = np.asarray(rowptr, np.int64)
+    col = np.asarray(col)
+    nnz = int(rowptr[-1]) if rowptr.size else 0
+    rows = np.repeat(np.arange(rowptr.size - 1, dtype=np.uint64), np.diff(rowptr))
+    key = (rows << np.uint64(32)) | col[:nnz].astype(np.uint32).astype(np.uint64)
+    v = np.ones(nnz, np.uint64) if val is None else np.asarray(val)[:nnz].astype(np.uint64)
+    with np.errstate(over="ignore"):
+        h = _mix64(_mix64(key) + v)
+        return nnz, int(h.sum(dtype=np.uint64)) if nnz else 0
+
+
+class Batch:
+    """Meta-paths recorded once and replayed as one CUDA graph (rmcm_batch_*)."""
+
+    def __init__(self, engine: "Engine", graph: "HeteroGraph", paths: list, lanes: int = 8):
+        self.engine, self.graph, self.paths = engine, graph, list(paths)
+        arr = (C.c_char_p * len(self.paths))(*[p.encode() for p in self.paths])
+        h = C.c_void_p()
+        engine._check(lib().rmcm_batch_create(engine._h, graph._h, arr, len(self.paths), lanes, C.byref(h)))
+        self._h = h
+
+    def run(self):
+        """Returns (nnz int64[count], digest uint64[count], device seconds)."""
+        n = len(self.paths)
+        nnz = np.zeros(n, np.int64)
+        dig = np.zeros(n, np.uint64)
+        sec = C.c_double()
+        self.engine._check(lib().rmcm_batch_run(self.engine._h, self._h, _ptr(nnz), _ptr(dig), C.byref(sec)))
+        return nnz, dig, sec.value
+
+    def info(self) -> dict:
+        c, ln, la, nd = C.c_int32(), C.c_int32(), C.c_int64(), C.c_int64()
+        lib().rmcm_batch_info(self._h, C.byref(c), C.byref(ln), C.byref(la), C.byref(nd))
+        return {"count": c.value, "lanes": ln.value, "launches_per_run": la.value, "graph_nodes": nd.value}
+
+    def free(self):
+        if getattr(self, "_h", None) and getattr(self.engine, "_h", None):
+            lib().rmcm_batch_free(self.engine._h, self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
         except Exception:
             pass
 
@@ -452,6 +518,15 @@ class Engine:
                                                  C.byref(h) if keep else None, C.byref(t)),
                          allow=(OK, EOVERFLOW))
         return (Matrix(self, h.value) if keep else None), t.as_dict(), rc
+
+    def batch(self, graph: HeteroGraph, paths: list, lanes: int = 8) -> Batch:
+        return Batch(self, graph, paths, lanes)
+
+    def digest(self, m: Matrix) -> tuple:
+        """(nnz, digest) of a device matrix (rmcm_mat_digest)."""
+        n, d = C.c_uint64(), C.c_uint64()
+        self._check(lib().rmcm_mat_digest(self._h, m._h, C.byref(n), C.byref(d)))
+        return n.value, d.value
 
     def estimate_metapath(self, graph: HeteroGraph, metapath: str) -> float:
         est = C.c_double()

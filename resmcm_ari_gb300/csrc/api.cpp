@@ -17,6 +17,7 @@
 #include <cstring>
 #include <fstream>
 #include <functional>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -444,6 +445,25 @@ int32_t copy_mat(rmcm_handle *h, const rmcm_mat *src, rmcm_mat **out) {
     return RMCM_OK;
 }
 
+// Device operations of one chain as the executor issued them, with every
+// size the executor read back from the device.  Replaying the log issues the
+// same work with no host round trip, so it can be captured into a CUDA graph.
+struct LogOp {
+    enum Kind { kEst, kDp, kBind, kSpgemm, kWiden, kFree } kind;
+    int a = -1, b = -1, c = -1;          // matrix slots
+    rmcm_mat *ext = nullptr;             // kBind: a graph-owned leaf
+    ProductPlan plan;                    // kSpgemm
+};
+struct ChainLog {
+    int32_t len = 0;
+    std::vector<rmcm_mat *> leaves;      // slots 0 .. len-1
+    std::vector<LogOp> ops;
+    int32_t nslots = 0;
+    int32_t result = -1;
+    int64_t nnz = 0;
+    int32_t valtype = RMCM_VAL_U32;
+};
+
 // Post-order (k, l) pair list of a split table (get_optimal_chain_order,
 // efficient/resmcm.cpp:563-573).
 int32_t post_order(const std::vector<int32_t> &split, int32_t len, int32_t i, int32_t j, std::vector<int32_t> &out) {
@@ -486,9 +506,38 @@ void dense_order(const int64_t *d, int32_t len, std::vector<int32_t> &split, std
 // in uint64 come from `leaf64` when given (the graph's cache), else are
 // widened here.
 int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int32_t *fixed_pairs, rmcm_mat **Cout,
-                   rmcm_timings *t, bool widen, const std::function<int32_t(int, rmcm_mat **)> &leaf64) {
+                   rmcm_timings *t, bool widen, const std::function<int32_t(int, rmcm_mat **)> &leaf64,
+                   ChainLog *log = nullptr) {
     rmcm_timings tm{};
     *Cout = nullptr;
+    // slot bookkeeping of the optional log
+    std::map<const rmcm_mat *, int> slot_of;
+    auto slot = [&](const rmcm_mat *m) -> int {
+        auto it = slot_of.find(m);
+        if (it != slot_of.end()) return it->second;
+        const int id = log->nslots++;
+        slot_of[m] = id;
+        return id;
+    };
+    auto log_op = [&](LogOp op) {
+        if (log) log->ops.push_back(op);
+    };
+    auto release = [&](rmcm_mat *m) {
+        if (log && m) {
+            LogOp op;
+            op.kind = LogOp::kFree;
+            op.a = slot(m);
+            log_op(op);
+            slot_of.erase(m);
+        }
+        mat_release(h, m);
+    };
+    if (log) {
+        log->len = len;
+        log->leaves.assign(mats, mats + len);
+        log->nslots = len;
+        for (int i = 0; i < len; i++) slot_of[mats[i]] = i;
+    }
     if (len < 1 || len > 16) return set_error(h, RMCM_EINVAL, "chain length must be 1..16");
     for (int i = 0; i < len; i++) {
         if (!mats[i]) return set_error(h, RMCM_EINVAL, "null matrix in chain");
@@ -506,6 +555,11 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
         tm.nnz = (*Cout)->d.nnz;
         tm.valtype = cur;
         if (t) *t = tm;
+        if (log) {
+            log->result = 0;
+            log->nnz = tm.nnz;
+            log->valtype = cur;
+        }
         return RMCM_OK;
     }
     cudaEvent_t *ev = h->ev;
@@ -538,6 +592,14 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
     if (fixed_pairs == pairs) {
         // order already known
     } else {
+    if (log) {
+        LogOp e;
+        e.kind = LogOp::kEst;
+        log_op(e);
+        LogOp d;
+        d.kind = LogOp::kDp;
+        log_op(d);
+    }
     // (a) estimator
     double *c_dev = nullptr;
     char *ord = nullptr;
@@ -594,10 +656,26 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
         if (leaf64) {
             rmcm_mat *m = nullptr;
             RMCM_TRY(leaf64(i, &m));
+            if (log && !slot_of.count(m)) {
+                LogOp op;
+                op.kind = LogOp::kBind;
+                op.c = slot(m);
+                op.ext = m;
+                log_op(op);
+            }
             *out = m;
             return RMCM_OK;
         }
-        if (!wide[i]) RMCM_TRY(convert_values(h, mats[i], RMCM_VAL_U64, &wide[i]));
+        if (!wide[i]) {
+            RMCM_TRY(convert_values(h, mats[i], RMCM_VAL_U64, &wide[i]));
+            if (log) {
+                LogOp op;
+                op.kind = LogOp::kWiden;
+                op.a = i;
+                op.c = slot(wide[i]);
+                log_op(op);
+            }
+        }
         *out = wide[i];
         return RMCM_OK;
     };
@@ -617,7 +695,9 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
         rmcm_mat *C = nullptr;
         int64_t fl = 0;
         h->abort_on_certain_overflow = widen && cur == RMCM_VAL_U32;
-        rc = spgemm(h, A, B, &C, &fl);
+        ProductPlan plan;
+        plan.mode = log ? 1 : 0;
+        rc = spgemm(h, A, B, &C, &fl, log ? &plan : nullptr);
         h->abort_on_certain_overflow = false;
         cudaEventRecord(ev[4], s);
         if (rc == RMCM_EOVERFLOW && widen && cur == RMCM_VAL_U32 && !C) {
@@ -628,7 +708,14 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
                 rmcm_mat *w = nullptr;
                 rc = convert_values(h, m, RMCM_VAL_U64, &w);
                 if (rc != RMCM_OK) break;
-                mat_release(h, m);
+                if (log) {
+                    LogOp op;
+                    op.kind = LogOp::kWiden;
+                    op.a = slot(m);
+                    op.c = slot(w);
+                    log_op(op);
+                }
+                release(m);
                 m = w;
             }
             if (rc != RMCM_OK) break;
@@ -648,7 +735,14 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
                     rmcm_mat *w = nullptr;
                     rc = convert_values(h, m, RMCM_VAL_U64, &w);
                     if (rc != RMCM_OK) break;
-                    mat_release(h, m);
+                    if (log) {
+                        LogOp op;
+                        op.kind = LogOp::kWiden;
+                        op.a = slot(m);
+                        op.c = slot(w);
+                        log_op(op);
+                    }
+                    release(m);
                     m = w;
                 }
                 p--;
@@ -662,19 +756,28 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
         }
         tm.flops += fl;
         tm.n_products++;
+        if (log) {
+            LogOp op;
+            op.kind = LogOp::kSpgemm;
+            op.a = slot(A);
+            op.b = slot(B);
+            op.c = slot(C);
+            op.plan = plan;
+            log_op(op);
+        }
         if (k >= 0 && l >= 0) {
             stack.push_back(C);
         } else if (k >= 0 || l >= 0) {
-            mat_release(h, stack[sz - 1]);
+            release(stack[sz - 1]);
             stack[sz - 1] = C;
         } else {
-            mat_release(h, stack[sz - 1]);
-            mat_release(h, stack[sz - 2]);
+            release(stack[sz - 1]);
+            release(stack[sz - 2]);
             stack.pop_back();
             stack[sz - 2] = C;
         }
     }
-    for (auto *m : wide) mat_release(h, m);
+    for (auto *m : wide) release(m);
     if (rc != RMCM_OK) {
         for (auto *m : stack) mat_release(h, m);
         return rc;
@@ -689,10 +792,80 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
     tm.valtype = cur;
     *Cout = stack[0];
     tm.nnz = stack[0]->d.nnz;
+    if (log) {
+        log->result = slot(stack[0]);
+        log->nnz = stack[0]->d.nnz;
+        log->valtype = cur;
+    }
     rc = check_status(h);
     if (rc == RMCM_EOVERFLOW) stack[0]->positive = false;   // wrapped counts may be 0
     if (t) *t = tm;
     return rc;
+}
+
+// Issues a chain's logged device work again, reading nothing back.  The
+// result's digest goes to digest_dev (when given); the result is freed unless
+// `keep`.
+int32_t chain_replay(rmcm_handle *h, const ChainLog &log, uint64_t *digest_dev, bool keep, rmcm_mat **out) {
+    std::vector<rmcm_mat *> slot(log.nslots, nullptr);
+    for (int i = 0; i < log.len; i++) slot[i] = log.leaves[i];
+    std::vector<bool> owned(log.nslots, false);
+    double *c_dev = nullptr;
+    int32_t rc = RMCM_OK;
+    for (const LogOp &op : log.ops) {
+        switch (op.kind) {
+            case LogOp::kEst:
+                rc = dev_alloc(h, (void **)&c_dev, 8 * 256);
+                if (rc == RMCM_OK) rc = estimate(h, log.leaves.data(), log.len, c_dev);
+                break;
+            case LogOp::kDp: {
+                char *buf = nullptr;
+                const int64_t bytes = 8 * 256 + 4 * 256 + 8 * 256 + 4 * 64;
+                rc = dev_alloc(h, (void **)&buf, bytes);
+                if (rc == RMCM_OK)
+                    rc = chain_order_launch(h, c_dev, log.len, (double *)buf, (int32_t *)(buf + 8 * 256),
+                                            (double *)(buf + 8 * 256 + 4 * 256), (int32_t *)(buf + 8 * 256 + 4 * 256 + 8 * 256));
+                dev_free(h, buf, bytes);
+                dev_free(h, c_dev, 8 * 256);
+                c_dev = nullptr;
+                break;
+            }
+            case LogOp::kBind:
+                slot[op.c] = op.ext;
+                break;
+            case LogOp::kSpgemm: {
+                ProductPlan p = op.plan;
+                p.mode = 2;
+                rmcm_mat *C = nullptr;
+                rc = spgemm(h, slot[op.a], slot[op.b], &C, nullptr, &p);
+                slot[op.c] = C;
+                owned[op.c] = true;
+                break;
+            }
+            case LogOp::kWiden:
+                rc = convert_values(h, slot[op.a], RMCM_VAL_U64, &slot[op.c]);
+                owned[op.c] = true;
+                break;
+            case LogOp::kFree:
+                if (owned[op.a]) mat_release(h, slot[op.a]);
+                slot[op.a] = nullptr;
+                owned[op.a] = false;
+                break;
+        }
+        if (rc != RMCM_OK) break;
+    }
+    if (c_dev) dev_free(h, c_dev, 8 * 256);
+    rmcm_mat *res = log.result >= 0 ? slot[log.result] : nullptr;
+    if (rc == RMCM_OK && res && digest_dev) rc = mat_digest_launch(h, res, digest_dev);
+    for (int i = 0; i < log.nslots; i++)
+        if (owned[i] && slot[i] && slot[i] != res) mat_release(h, slot[i]);
+    if (rc != RMCM_OK) {
+        if (res && owned[log.result]) mat_release(h, res);
+        return rc;
+    }
+    if (keep && out) *out = res;
+    else if (res && owned[log.result]) mat_release(h, res);
+    return RMCM_OK;
 }
 
 }  // namespace
@@ -769,6 +942,7 @@ RMCM_API int32_t rmcm_create(rmcm_handle **out, const rmcm_opts *opts) {
 
 RMCM_API int32_t rmcm_destroy(rmcm_handle *h) {
     if (!h) return RMCM_OK;
+    while (!h->batches.empty()) rmcm_batch_free(h, *h->batches.begin());
     // graphs outliving their handle keep their host arrays only
     for (rmcm_graph *g : h->graphs) {
         for (auto &kv : g->leaves) mat_release(h, kv.second);
@@ -889,6 +1063,10 @@ RMCM_API int32_t rmcm_graph_from_adjacency(rmcm_handle *h, int64_t n, const int3
 
 RMCM_API int32_t rmcm_graph_free(rmcm_graph *g) {
     if (!g) return RMCM_OK;
+    if (g->batches > 0) {
+        if (g->h) set_error(g->h, RMCM_EINVAL, "graph_free: free the batches recorded on this graph first");
+        return RMCM_EINVAL;
+    }
     if (g->h) {
         for (auto &kv : g->leaves) mat_release(g->h, kv.second);
         if (g->h->stream) cudaStreamSynchronize(g->h->stream);
@@ -1232,3 +1410,276 @@ RMCM_API int32_t rmcm_estimate_metapath(rmcm_handle *h, rmcm_graph *g, const cha
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Batches: many meta-paths over one graph, recorded once and replayed as one
+// CUDA graph over concurrent lanes.
+// ===========================================================================
+
+struct rmcm_batch {
+    rmcm_handle *h = nullptr;
+    rmcm_graph *g = nullptr;
+    std::vector<std::string> paths;
+    std::vector<ChainLog> logs;
+    std::vector<int32_t> lane_of;
+    std::vector<rmcm_handle *> lanes;
+    std::vector<int64_t> scratch_need;      // per lane
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<cudaEvent_t> fork_join;     // 1 fork + one join per lane
+    uint64_t *d_digest = nullptr;           // 2 per chain
+    uint64_t *h_digest = nullptr;           // pinned mirror
+    int64_t launches_per_run = 0;
+    int64_t nodes = 0;
+    int64_t runs = 0;
+};
+
+namespace {
+
+void batch_release(rmcm_batch *b) {
+    rmcm_handle *h = b->h;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (auto e : b->fork_join)
+        if (e) cudaEventDestroy(e);
+    for (rmcm_handle *l : b->lanes) rmcm_destroy(l);
+    if (b->d_digest) {
+        dev_free(h, b->d_digest, 16 * (int64_t)b->paths.size());
+        cudaStreamSynchronize(h->stream);
+    }
+    if (b->h_digest) cudaFreeHost(b->h_digest);
+    if (b->g) b->g->batches--;
+    h->batches.erase(b);
+    delete b;
+}
+
+// Captures every lane's chains into one CUDA graph: a fork event on the
+// handle's stream, each lane replaying its chains in order on its own
+// stream, a join back, then one copy of all digests to pinned host memory.
+int32_t batch_capture(rmcm_batch *b) {
+    rmcm_handle *h = b->h;
+    const int K = (int)b->lanes.size();
+    // scratch is grown outside the capture: a replay never allocates it
+    for (int k = 0; k < K; k++) {
+        RMCM_TRY(scratch_reserve(b->lanes[k], b->scratch_need[k]));
+        RMCM_CUDA(h, cudaStreamSynchronize(b->lanes[k]->stream));
+    }
+    const int64_t launches0 = [&] {
+        int64_t x = 0;
+        for (auto *l : b->lanes) x += l->launches;
+        return x;
+    }();
+    RMCM_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int32_t rc = RMCM_OK;
+    cudaError_t e = cudaEventRecord(b->fork_join[0], h->stream);
+    std::vector<bool> forked(K, false);
+    for (int k = 0; k < K && e == cudaSuccess; k++) {
+        e = cudaStreamWaitEvent(b->lanes[k]->stream, b->fork_join[0], 0);
+        forked[k] = e == cudaSuccess;
+    }
+    if (e != cudaSuccess) rc = cuda_error(h, e, "batch fork");
+    for (size_t i = 0; i < b->logs.size() && rc == RMCM_OK; i++) {
+        rmcm_handle *l = b->lanes[b->lane_of[i]];
+        rc = chain_replay(l, b->logs[i], b->d_digest + 2 * i, false, nullptr);
+        if (rc != RMCM_OK) set_error(h, rc, "batch capture: " + b->paths[i] + ": " + l->last_error);
+    }
+    for (int k = 0; k < K; k++) {
+        if (!forked[k]) continue;
+        cudaEventRecord(b->fork_join[1 + k], b->lanes[k]->stream);
+        cudaStreamWaitEvent(h->stream, b->fork_join[1 + k], 0);
+    }
+    if (rc == RMCM_OK) {
+        e = cudaMemcpyAsync(b->h_digest, b->d_digest, 16 * b->paths.size(), cudaMemcpyDeviceToHost, h->stream);
+        if (e != cudaSuccess) rc = cuda_error(h, e, "batch digest copy");
+    }
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(h->stream, &graph);
+    if (rc == RMCM_OK && e != cudaSuccess) rc = cuda_error(h, e, "cudaStreamEndCapture");
+    if (rc != RMCM_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return rc;
+    }
+    b->graph = graph;
+    e = cudaGraphInstantiate(&b->exec, graph, 0);
+    if (e != cudaSuccess) {
+        b->exec = nullptr;
+        return cuda_error(h, e, "cudaGraphInstantiate");
+    }
+    size_t nodes = 0;
+    cudaGraphGetNodes(graph, nullptr, &nodes);
+    b->nodes = (int64_t)nodes;
+    int64_t launches1 = 0;
+    for (auto *l : b->lanes) launches1 += l->launches;
+    b->launches_per_run = launches1 - launches0;
+    return RMCM_OK;
+}
+
+}  // namespace
+
+RMCM_API int32_t rmcm_batch_create(rmcm_handle *h, rmcm_graph *g, const char *const *metapaths, int32_t count,
+                                   int32_t lanes, rmcm_batch **out) {
+    if (!h || !g || !metapaths || count < 1 || !out) return RMCM_EINVAL;
+    *out = nullptr;
+    if (g->h != h) return set_error(h, RMCM_EINVAL, "batch: the graph belongs to another handle");
+    if (h->order_mode != RMCM_ORDER_RES) return set_error(h, RMCM_EINVAL, "batch: only the RES order is batched");
+    if (lanes < 1) lanes = 8;
+    lanes = std::min(lanes, std::min<int32_t>(count, 64));
+    rmcm_batch *b = new rmcm_batch();
+    b->h = h;
+    b->g = g;
+    g->batches++;
+    h->batches.insert(b);
+    const int32_t vt = h->valtype == RMCM_VAL_U64 ? RMCM_VAL_U64 : RMCM_VAL_U32;
+    const bool widen = h->valtype == RMCM_VAL_AUTO;
+    const int32_t prof = h->prof_level;
+    h->prof_level = 0;
+    int32_t rc = RMCM_OK;
+    // record pass: every chain once through the ordinary executor
+    std::vector<double> cost(count, 0.0);
+    for (int32_t i = 0; i < count && rc == RMCM_OK; i++) {
+        const char *mp = metapaths[i];
+        std::vector<int32_t> vts, ets;
+        if (!mp || parse_path(mp, vts, ets) != RMCM_OK) {
+            rc = set_error(h, RMCM_EINVAL, std::string("the meta-path is incorrect: ") + (mp ? mp : "(null)"));
+            break;
+        }
+        const int len = (int)ets.size();
+        if (len < 1 || len > 16) {
+            rc = set_error(h, RMCM_EINVAL, "meta-path must have 1..16 edge types");
+            break;
+        }
+        std::vector<rmcm_mat *> mats(len);
+        for (int j = 0; j < len && rc == RMCM_OK; j++) rc = get_leaf(h, g, vts[j], vts[j + 1], ets[j], vt, &mats[j]);
+        if (rc != RMCM_OK) break;
+        auto leaf64 = [&](int j, rmcm_mat **o) { return get_leaf(h, g, vts[j], vts[j + 1], ets[j], RMCM_VAL_U64, o); };
+        b->paths.emplace_back(mp);
+        b->logs.emplace_back();
+        rmcm_mat *res = nullptr;
+        rc = chain_exec(h, mats.data(), len, nullptr, &res, nullptr, widen, leaf64, &b->logs.back());
+        if (res) mat_release(h, res);
+        if (rc != RMCM_OK) {
+            const std::string why = h->last_error;
+            rc = set_error(h, rc, "batch record: " + std::string(mp) + ": " + why);
+            break;
+        }
+        for (const LogOp &op : b->logs.back().ops)
+            cost[i] += op.kind == LogOp::kSpgemm ? 2e6 + (double)op.plan.flops + 4.0 * (double)op.plan.nnz : 2e5;
+    }
+    h->prof_level = prof;
+    // lanes: longest chains first onto the least-loaded lane
+    if (rc == RMCM_OK) {
+        rmcm_opts o{};
+        o.device = h->device;
+        o.valtype = h->valtype;
+        o.mem_budget_bytes = h->budget;
+        for (int k = 0; k < lanes && rc == RMCM_OK; k++) {
+            rmcm_handle *l = nullptr;
+            rc = rmcm_create(&l, &o);
+            if (rc != RMCM_OK) {
+                set_error(h, rc, "batch: could not create a lane");
+                break;
+            }
+            l->tune = h->tune;
+            b->lanes.push_back(l);
+        }
+    }
+    if (rc == RMCM_OK) {
+        std::vector<int32_t> idx(count);
+        for (int32_t i = 0; i < count; i++) idx[i] = i;
+        std::stable_sort(idx.begin(), idx.end(), [&](int32_t x, int32_t y) { return cost[x] > cost[y]; });
+        std::vector<double> load(lanes, 0.0);
+        b->lane_of.assign(count, 0);
+        b->scratch_need.assign(lanes, 256);
+        for (int32_t i : idx) {
+            const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            b->lane_of[i] = k;
+            load[k] += cost[i];
+            for (const LogOp &op : b->logs[i].ops)
+                if (op.kind == LogOp::kSpgemm) b->scratch_need[k] = std::max(b->scratch_need[k], op.plan.scratch_bytes);
+        }
+        b->fork_join.assign(1 + lanes, nullptr);
+        for (auto &e : b->fork_join)
+            if (rc == RMCM_OK && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+                rc = set_error(h, RMCM_ECUDA, "batch: event creation failed");
+    }
+    if (rc == RMCM_OK) rc = dev_alloc(h, (void **)&b->d_digest, 16 * (int64_t)count);
+    if (rc == RMCM_OK && cudaMallocHost((void **)&b->h_digest, 16 * (size_t)count) != cudaSuccess) {
+        b->h_digest = nullptr;
+        rc = set_error(h, RMCM_ECUDA, "batch: pinned digest buffer");
+    }
+    if (rc == RMCM_OK) {
+        RMCM_CUDA(h, cudaStreamSynchronize(h->stream));
+        rc = batch_capture(b);
+    }
+    if (rc != RMCM_OK) {
+        const std::string why = h->last_error;
+        batch_release(b);
+        h->last_error = why;
+        return rc;
+    }
+    *out = b;
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_batch_run(rmcm_handle *h, rmcm_batch *b, int64_t *nnz_out, uint64_t *digest_out,
+                                double *seconds) {
+    if (!h || !b || b->h != h || !b->exec) return RMCM_EINVAL;
+    cudaEvent_t *ev = h->ev;
+    RMCM_CUDA(h, cudaEventRecord(ev[6], h->stream));
+    RMCM_CUDA(h, cudaGraphLaunch(b->exec, h->stream));
+    RMCM_CUDA(h, cudaEventRecord(ev[7], h->stream));
+    RMCM_CUDA(h, cudaStreamSynchronize(h->stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev[6], ev[7]);
+    if (seconds) *seconds = ms * 1e-3;
+    h->launches += b->launches_per_run;
+    b->runs++;
+    for (size_t k = 0; k < b->lanes.size(); k++) {
+        const int32_t st = check_status(b->lanes[k]);
+        if (st != RMCM_OK) return set_error(h, st, "batch run: lane " + std::to_string(k) + ": " + b->lanes[k]->last_error);
+    }
+    const size_t n = b->paths.size();
+    for (size_t i = 0; i < n; i++) {
+        if ((int64_t)b->h_digest[2 * i] != b->logs[i].nnz)
+            return set_error(h, RMCM_EINTERNAL, "batch run: result size of " + b->paths[i] + " differs from its record");
+        if (nnz_out) nnz_out[i] = (int64_t)b->h_digest[2 * i];
+        if (digest_out) digest_out[i] = b->h_digest[2 * i + 1];
+    }
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_batch_info(const rmcm_batch *b, int32_t *count, int32_t *lanes, int64_t *launches_per_run,
+                                 int64_t *graph_nodes) {
+    if (!b) return RMCM_EINVAL;
+    if (count) *count = (int32_t)b->paths.size();
+    if (lanes) *lanes = (int32_t)b->lanes.size();
+    if (launches_per_run) *launches_per_run = b->launches_per_run;
+    if (graph_nodes) *graph_nodes = b->nodes;
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_batch_free(rmcm_handle *h, rmcm_batch *b) {
+    if (!b) return RMCM_OK;
+    if (!h || b->h != h) return RMCM_EINVAL;
+    cudaStreamSynchronize(h->stream);
+    batch_release(b);
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_mat_digest(rmcm_handle *h, const rmcm_mat *m, uint64_t *nnz, uint64_t *digest) {
+    if (!h || !m) return RMCM_EINVAL;
+    uint64_t *d = nullptr;
+    RMCM_TRY(dev_alloc(h, (void **)&d, 16));
+    int32_t rc = mat_digest_launch(h, m, d);
+    if (rc == RMCM_OK) {
+        cudaError_t e = cudaMemcpyAsync(h->h_pinned, d, 16, cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) rc = cuda_error(h, e, "digest download");
+    }
+    dev_free(h, d, 16);
+    if (rc != RMCM_OK) return rc;
+    if (nnz) *nnz = (uint64_t)h->h_pinned[0];
+    if (digest) *digest = (uint64_t)h->h_pinned[1];
+    return RMCM_OK;
+}

@@ -12,8 +12,11 @@
 // post-order with an explicit stack and emits the (k, l) pair list, -1
 // standing for "the top of the temporary stack".
 // One warp per chain: `nchains` chains are ordered by one launch.
+// The file also holds the result digest used to compare chain results
+// computed by different routes without copying them to the host.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cfloat>
 
 #include "internal.h"
@@ -24,11 +27,12 @@ namespace {
 constexpr int kMaxLen = 16;
 
 __global__ void __launch_bounds__(32) k_chain_dp(const double *c_all, const int32_t *lens, int32_t nchains,
-                                                 int32_t *split_all, double *cost_all, int32_t *pairs_all) {
+                                                 int32_t *split_all, double *cost_all, int32_t *pairs_all,
+                                                 int32_t one_len) {
     const int chain = blockIdx.x;
     if (chain >= nchains) return;
     const int lane = threadIdx.x;
-    const int len = lens[chain];
+    const int len = lens ? lens[chain] : one_len;
     const double *c = c_all + (int64_t)chain * kMaxLen * kMaxLen;
     __shared__ double sc[kMaxLen * kMaxLen];
     __shared__ double sm[kMaxLen * kMaxLen];
@@ -97,6 +101,57 @@ __global__ void __launch_bounds__(32) k_chain_dp(const double *c_all, const int3
 
 }  // namespace
 
+namespace {
+
+// splitmix64 output function (Steele, Lea and Flood, "Fast splittable
+// pseudorandom number generators", OOPSLA 2014)
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ULL;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebULL;
+    x ^= x >> 31;
+    return x;
+}
+
+// out[0] = nnz (rowptr[rows]); out[1] += sum over entries (r, c, v) of
+// mix64(mix64(r * 2^32 + c) + v), mod 2^64.  The sum does not depend on the
+// entry order, so equal matrices give equal digests whatever the launch shape.
+template <typename V>
+__global__ void __launch_bounds__(256) k_digest(DevCsr C, unsigned long long *out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    uint64_t acc = 0;
+    const V *val = (const V *)C.val;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < C.rows; r += warps) {
+        const int64_t e1 = C.rowptr[r + 1];
+        for (int64_t e = C.rowptr[r] + lane; e < e1; e += 32) {
+            const uint64_t key = ((uint64_t)r << 32) | (uint32_t)C.col[e];
+            const uint64_t v = val ? (uint64_t)val[e] : 1ULL;
+            acc += mix64(mix64(key) + v);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0 && acc) atomicAdd(out + 1, (unsigned long long)acc);
+    if (blockIdx.x == 0 && threadIdx.x == 0) out[0] = (unsigned long long)C.rowptr[C.rows];
+}
+
+}  // namespace
+
+int32_t mat_digest_launch(rmcm_handle *h, const rmcm_mat *m, uint64_t *out_dev) {
+    cudaStream_t s = h->stream;
+    RMCM_CUDA(h, cudaMemsetAsync(out_dev, 0, 2 * sizeof(uint64_t), s));
+    const int64_t want = (m->d.rows * 32 + 255) / 256;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)h->sm_count * 8));
+    if (m->valtype == RMCM_VAL_U64)
+        k_digest<uint64_t><<<grid, 256, 0, s>>>(m->d, (unsigned long long *)out_dev);
+    else
+        k_digest<uint32_t><<<grid, 256, 0, s>>>(m->d, (unsigned long long *)out_dev);
+    h->launches++;
+    RMCM_CUDA(h, cudaGetLastError());
+    return RMCM_OK;
+}
+
 int32_t chain_order_dev(rmcm_handle *h, const double *c_dev, int32_t len, int32_t *split_dev, double *cost_dev,
                         int32_t *pairs_dev) {
     // single-chain form: c_dev is len*len; stage it into the 16x16 batched layout
@@ -117,7 +172,7 @@ int32_t chain_order_dev(rmcm_handle *h, const double *c_dev, int32_t len, int32_
         e = cudaMemcpyAsync(lens, &L, sizeof(int32_t), cudaMemcpyHostToDevice, s);
     }
     if (e == cudaSuccess) {
-        k_chain_dp<<<1, 32, 0, s>>>(c16, lens, 1, sp16, cost16, pairs16);
+        k_chain_dp<<<1, 32, 0, s>>>(c16, lens, 1, sp16, cost16, pairs16, 0);
         h->launches++;
         e = cudaGetLastError();
     }
@@ -130,6 +185,17 @@ int32_t chain_order_dev(rmcm_handle *h, const double *c_dev, int32_t len, int32_
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);   // host value of L must outlive the copy
     dev_free(h, buf, total + 1024);
     if (e != cudaSuccess) return cuda_error(h, e, "chain order");
+    return RMCM_OK;
+}
+
+int32_t chain_order_launch(rmcm_handle *h, const double *c_dev, int32_t len, double *c16, int32_t *split16,
+                           double *cost16, int32_t *pairs32) {
+    if (len < 1 || len > kMaxLen) return set_error(h, RMCM_EINVAL, "order: chain length must be 1..16");
+    cudaStream_t s = h->stream;
+    RMCM_CUDA(h, cudaMemcpyAsync(c16, c_dev, sizeof(double) * len * len, cudaMemcpyDeviceToDevice, s));
+    k_chain_dp<<<1, 32, 0, s>>>(c16, nullptr, 1, split16, cost16, pairs32, len);
+    h->launches++;
+    RMCM_CUDA(h, cudaGetLastError());
     return RMCM_OK;
 }
 

@@ -15,6 +15,7 @@
 struct rmcm_handle;
 struct rmcm_graph;
 struct rmcm_mat;
+struct rmcm_batch;
 
 namespace rmcm {
 
@@ -62,6 +63,18 @@ struct ProdRecord {
     cudaEvent_t ev[6] = {};
 };
 
+// Sizes one SpGEMM read back from the device, kept so that the same product
+// can be replayed (under CUDA stream capture) without any host round trip.
+struct ProductPlan {
+    int mode = 0;                    // 0 normal, 1 record, 2 replay
+    int32_t counts[kNumBins] = {};
+    int32_t dense_max_alen = 0;
+    int64_t flops = 0;
+    int64_t nnz = 0;
+    bool dense_temp = false;
+    int64_t scratch_bytes = 0;
+};
+
 }  // namespace rmcm
 
 struct rmcm_mat {
@@ -96,12 +109,14 @@ struct rmcm_handle {
     int32_t prof_level = 0;
     std::vector<rmcm::ProdRecord> prof;
     std::set<rmcm_graph *> graphs;   // graphs whose leaves live on this handle
+    std::set<rmcm_batch *> batches;  // batches recorded on this handle
     bool abort_on_certain_overflow = false;   // spgemm returns EOVERFLOW before computing when sure
     int32_t order_mode = RMCM_ORDER_RES;
 };
 
 struct rmcm_graph {
     rmcm_handle *h = nullptr;
+    int32_t batches = 0;             // live batches that replay this graph's leaves
     int64_t n = 0, m = 0;
     int32_t max_vt = 0;
     std::vector<int32_t> vtype;
@@ -147,7 +162,8 @@ inline int64_t val_bytes(int32_t valtype) { return valtype == RMCM_VAL_U64 ? 8 :
 
 // ---- kernels (host launchers) --------------------------------------------
 // spgemm.cu
-int32_t spgemm(rmcm_handle *h, const rmcm_mat *A, const rmcm_mat *B, rmcm_mat **C, int64_t *flops_out);
+int32_t spgemm(rmcm_handle *h, const rmcm_mat *A, const rmcm_mat *B, rmcm_mat **C, int64_t *flops_out,
+               ProductPlan *plan = nullptr);
 int32_t fill_ones(rmcm_handle *h, void *val, int64_t nnz, int32_t valtype);
 int32_t convert_values(rmcm_handle *h, const rmcm_mat *src, int32_t valtype, rmcm_mat **out);
 // estimator.cu: c_dev[len*len] on the device
@@ -155,5 +171,12 @@ int32_t estimate(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, double *c_
 // chain_dp.cu: split/cost/pairs on the device
 int32_t chain_order_dev(rmcm_handle *h, const double *c_dev, int32_t len, int32_t *split_dev, double *cost_dev,
                         int32_t *pairs_dev);
+// Launch-only form (no host round trip; usable under stream capture):
+// c16/split16/cost16 are 16x16 arrays, pairs32 holds 32 ints.
+// Launches a digest of m into out_dev[0..1] (nnz, order-free entry hash);
+// capture-safe.
+int32_t mat_digest_launch(rmcm_handle *h, const rmcm_mat *m, uint64_t *out_dev);
+int32_t chain_order_launch(rmcm_handle *h, const double *c_dev, int32_t len, double *c16, int32_t *split16,
+                           double *cost16, int32_t *pairs32);
 
 }  // namespace rmcm

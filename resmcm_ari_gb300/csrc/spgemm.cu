@@ -1288,9 +1288,16 @@ int32_t scan_rowptr(rmcm_handle *h, const int64_t *cnt, int64_t m, int64_t *rowp
     return RMCM_OK;
 }
 
+__global__ void k_check_nnz(const int64_t *nnz_dev, int64_t expect, int *st) {
+    if (threadIdx.x == 0 && *nnz_dev != expect) raise_status(st, kInvariant);
+}
+
 template <typename V>
-int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_mat **Cout, int64_t *flops_out) {
+int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_mat **Cout, int64_t *flops_out,
+                 ProductPlan *plan) {
     cudaStream_t s = h->stream;
+    const bool replay = plan && plan->mode == 2;
+    const bool record = plan && plan->mode == 1;
     // row sums of B bound the counts of every output row (computed once per matrix)
     if (!Bm->ones && !Bm->rowsum && Bm->d.rows > 0) {
         rmcm_mat *Bw = const_cast<rmcm_mat *>(Bm);
@@ -1315,6 +1322,9 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     const int64_t o_small = o_lists + al(4 * m);
     const int64_t o_cur = o_small + 256;
     int64_t need = o_cur;
+    if (record) plan->scratch_bytes = need;
+    if (replay && need > h->scratch_bytes)
+        return set_error(h, RMCM_EINTERNAL, "replay: scratch not reserved before capture");
     RMCM_TRY(scratch_reserve(h, need));
     char *sc = (char *)h->scratch;
     int64_t *flops = (int64_t *)(sc + o_flops);
@@ -1329,7 +1339,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
 
     ProdRecord *rec = nullptr;
     size_t rec_idx = 0;
-    if (h->prof_level > 0) {
+    if (h->prof_level > 0 && !replay) {
         h->prof.emplace_back();
         rec_idx = h->prof.size() - 1;
         rec = &h->prof[rec_idx];
@@ -1349,16 +1359,31 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         RMCM_CUDA(h, cudaGetLastError());
     }
     if (rec) RMCM_CUDA(h, cudaEventRecord(h->prof[rec_idx].ev[1], s));
-    // bin counts, the longest dense A row and the flops to the host
-    RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned, small, 44 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-    RMCM_CUDA(h, cudaStreamSynchronize(s));
+    // bin counts, the longest dense A row and the flops to the host (a replay
+    // takes them from the recorded plan)
     int32_t counts[kNumBins];
-    memcpy(counts, h->h_pinned, sizeof(counts));
-    const int32_t dense_max_alen = ((int32_t *)h->h_pinned)[16];
+    int32_t dense_max_alen = 0;
     int64_t flops_total = 0;
-    memcpy(&flops_total, (int32_t *)h->h_pinned + 32, sizeof(int64_t));
+    bool certain = false;
+    if (replay) {
+        memcpy(counts, plan->counts, sizeof(counts));
+        dense_max_alen = plan->dense_max_alen;
+        flops_total = plan->flops;
+    } else {
+        RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned, small, 44 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        RMCM_CUDA(h, cudaStreamSynchronize(s));
+        memcpy(counts, h->h_pinned, sizeof(counts));
+        dense_max_alen = ((int32_t *)h->h_pinned)[16];
+        memcpy(&flops_total, (int32_t *)h->h_pinned + 32, sizeof(int64_t));
+        certain = ((int32_t *)h->h_pinned)[40] != 0;
+    }
+    if (record) {
+        memcpy(plan->counts, counts, sizeof(counts));
+        plan->dense_max_alen = dense_max_alen;
+        plan->flops = flops_total;
+    }
     if (flops_out) *flops_out = flops_total;
-    if (((int32_t *)h->h_pinned)[40] && h->abort_on_certain_overflow) {
+    if (certain && h->abort_on_certain_overflow) {
         // some row's total count exceeds (its distinct columns) x (largest
         // value): an overflow is certain, so the caller widens first
         if (rec) {
@@ -1385,11 +1410,11 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     // Single-pass dense rows: when every dense row fits one numeric window,
     // compute them once into a row-padded temporary (bounded in size).
     DenseTemp dtemp;
-    if (counts[kBinDense] > 0 && B.cols <= wnum && h->tune.dense_single_pass) {
+    if (counts[kBinDense] > 0 && B.cols <= wnum && h->tune.dense_single_pass && (!replay || plan->dense_temp)) {
         const int64_t stride = (B.cols + 3) & ~3LL;
         const int64_t bytes = (int64_t)counts[kBinDense] * stride * (4 + (int64_t)sizeof(V));
         const int64_t room = h->budget - h->in_use;
-        if (bytes <= h->tune.dense_temp_max_bytes && bytes < room / 2) {
+        if (replay || (bytes <= h->tune.dense_temp_max_bytes && bytes < room / 2)) {
             void *p = nullptr;
             if (dev_alloc(h, &p, bytes) == RMCM_OK) {
                 dtemp.active = true;
@@ -1402,6 +1427,9 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
             }
         }
     }
+    if (replay && plan->dense_temp && !dtemp.active)
+        return set_error(h, RMCM_ENOMEM, "replay: dense temporary could not be allocated");
+    if (record) plan->dense_temp = dtemp.active;
     auto drop_temp = [&]() {
         if (dtemp.active) dev_free(h, dtemp.col, dtemp.bytes);
         dtemp.active = false;
@@ -1421,13 +1449,20 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[3], s);
     // nnz to the host, then the output arrays
     int64_t *hp = h->h_pinned;
-    if (rc == RMCM_OK) {
+    if (rc == RMCM_OK && !replay) {
         cudaError_t e = cudaMemcpyAsync(hp, C->d.rowptr + m, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) rc = cuda_error(h, e, "spgemm nnz download");
     }
-    const int64_t nnz = hp[0];
-    if (rc == RMCM_OK && h->abort_on_certain_overflow) {
+    if (rc == RMCM_OK && replay) {
+        // the replayed symbolic pass must find the recorded size
+        k_check_nnz<<<1, 32, 0, s>>>(C->d.rowptr + m, plan->nnz, h->d_status);
+        h->launches++;
+        if (cudaGetLastError() != cudaSuccess) rc = set_error(h, RMCM_ECUDA, "replay nnz check launch");
+    }
+    const int64_t nnz = replay ? plan->nnz : hp[0];
+    if (record) plan->nnz = nnz;
+    if (rc == RMCM_OK && h->abort_on_certain_overflow && !replay) {
         // single-pass dense rows already computed their counts: stop early if
         // any of them overflowed, so the caller can recompute in uint64
         cudaError_t e = cudaMemcpyAsync(h->h_status, h->d_status, sizeof(int) * kNumStatus, cudaMemcpyDeviceToHost, s);
@@ -1508,13 +1543,14 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
 
 }  // namespace
 
-int32_t spgemm(rmcm_handle *h, const rmcm_mat *A, const rmcm_mat *B, rmcm_mat **C, int64_t *flops_out) {
+int32_t spgemm(rmcm_handle *h, const rmcm_mat *A, const rmcm_mat *B, rmcm_mat **C, int64_t *flops_out,
+               ProductPlan *plan) {
     if (!A || !B || !C) return set_error(h, RMCM_EINVAL, "spgemm: null matrix");
     if (A->d.cols != B->d.rows)
         return set_error(h, RMCM_EINVAL, "spgemm: shape mismatch (A.cols != B.rows)");
     if (A->valtype != B->valtype) return set_error(h, RMCM_EINVAL, "spgemm: value types differ");
-    if (A->valtype == RMCM_VAL_U64) return spgemm_t<uint64_t>(h, A, B, C, flops_out);
-    return spgemm_t<uint32_t>(h, A, B, C, flops_out);
+    if (A->valtype == RMCM_VAL_U64) return spgemm_t<uint64_t>(h, A, B, C, flops_out, plan);
+    return spgemm_t<uint32_t>(h, A, B, C, flops_out, plan);
 }
 
 int32_t convert_values(rmcm_handle *h, const rmcm_mat *src, int32_t valtype, rmcm_mat **out) {
