@@ -103,7 +103,7 @@ typedef struct rmcm_product_stats {
     int64_t bytes_a, bytes_b_touched, bytes_c;   /* level 2 only */
     double analyze_ms, symbolic_ms, numeric_ms;  /* CUDA-event times on the handle's stream */
     int32_t valtype;
-    int32_t bin_rows[6];                /* rows per bin: tiny, hash512, hash2k, hash8k, dense, rank */
+    int32_t bin_rows[7];                /* rows per bin: tiny, hash512, hash2k, hash8k, dense, rank, micro */
 } rmcm_product_stats;
 
 /* ---- handle -------------------------------------------------------------- */
@@ -236,6 +236,29 @@ RMCM_API int32_t rmcm_mat_save(rmcm_handle *h, const rmcm_mat *m, const char *pa
  * accuracy/res.cpp (final_result_estimate :564-600, output :698). */
 RMCM_API int32_t rmcm_estimate_metapath(rmcm_handle *h, rmcm_graph *g, const char *metapath,
                                         double *est_nnz);
+
+/* ---- SpGEMM tunables --------------------------------------------------------
+ * Row binning of every product on this handle (none changes a result):
+ *   threads_per_row  rows of at most 32 products: 32 = a warp per row;
+ *                    1, 2, 4, 8 or 16 = that many lanes per row for rows of at
+ *                    most that many products (the others a warp each);
+ *                    128 = a 128-thread CTA per row (512-slot hash bin)
+ *   hash_max_flops   rows with more products leave the hash bins for the
+ *                    dense / rank bins (32 .. 1048576)
+ *   dense_ratio      a row whose products x dense_ratio reach the output
+ *                    width goes to the dense bin (>= 1)
+ *   hash_load        hash tables get at least min(products, width) / load
+ *                    slots (0.1 .. 0.75)
+ * Defaults: 32, 4096, 16, 0.5.  A batch keeps the values it was created with. */
+typedef struct rmcm_tuning {
+    int32_t threads_per_row;
+    int32_t hash_max_flops;
+    int32_t dense_ratio;
+    int32_t reserved;
+    double hash_load;
+} rmcm_tuning;
+RMCM_API int32_t rmcm_set_tuning(rmcm_handle *h, const rmcm_tuning *t);
+RMCM_API int32_t rmcm_get_tuning(const rmcm_handle *h, rmcm_tuning *t);
 
 /* ---- batches ---------------------------------------------------------------
  * Many meta-paths over one graph, each computed exactly as rmcm_run_metapath

@@ -59,13 +59,21 @@ class Timings(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class Tuning(C.Structure):
+    _fields_ = [("threads_per_row", C.c_int32), ("hash_max_flops", C.c_int32), ("dense_ratio", C.c_int32),
+                ("reserved", C.c_int32), ("hash_load", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
 class ProductStats(C.Structure):
     _fields_ = [("rows", C.c_int64), ("inner", C.c_int64), ("cols", C.c_int64),
                 ("nnz_a", C.c_int64), ("nnz_b", C.c_int64), ("nnz_c", C.c_int64), ("flops", C.c_int64),
                 ("touched_rows", C.c_int64), ("touched_nnz", C.c_int64),
                 ("bytes_a", C.c_int64), ("bytes_b_touched", C.c_int64), ("bytes_c", C.c_int64),
                 ("analyze_ms", C.c_double), ("symbolic_ms", C.c_double), ("numeric_ms", C.c_double),
-                ("valtype", C.c_int32), ("bin_rows", C.c_int32 * 6)]
+                ("valtype", C.c_int32), ("bin_rows", C.c_int32 * 7)]
 
     def as_dict(self) -> dict:
         d = {f: getattr(self, f) for f, _ in self._fields_ if f != "bin_rows"}
@@ -132,6 +140,8 @@ def lib():
         "rmcm_batch_info": ([vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)], i32),
         "rmcm_batch_free": ([vp, vp], i32),
         "rmcm_mat_digest": ([vp, vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], i32),
+        "rmcm_set_tuning": ([vp, C.POINTER(Tuning)], i32),
+        "rmcm_get_tuning": ([vp, C.POINTER(Tuning)], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -518,6 +528,22 @@ class Engine:
                                                  C.byref(h) if keep else None, C.byref(t)),
                          allow=(OK, EOVERFLOW))
         return (Matrix(self, h.value) if keep else None), t.as_dict(), rc
+
+    def get_tuning(self) -> dict:
+        t = Tuning()
+        self._check(lib().rmcm_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, **kw):
+        """Change some of threads_per_row, hash_max_flops, dense_ratio, hash_load."""
+        cur = self.get_tuning()
+        bad = set(kw) - set(cur)
+        if bad:
+            raise ValueError(f"unknown tunables {sorted(bad)}")
+        cur.update(kw)
+        t = Tuning(int(cur["threads_per_row"]), int(cur["hash_max_flops"]), int(cur["dense_ratio"]), 0,
+                   float(cur["hash_load"]))
+        self._check(lib().rmcm_set_tuning(self._h, C.byref(t)))
 
     def batch(self, graph: HeteroGraph, paths: list, lanes: int = 8) -> Batch:
         return Batch(self, graph, paths, lanes)

@@ -1517,6 +1517,33 @@ int32_t batch_capture(rmcm_batch *b) {
 
 }  // namespace
 
+RMCM_API int32_t rmcm_set_tuning(rmcm_handle *h, const rmcm_tuning *t) {
+    if (!h || !t) return RMCM_EINVAL;
+    const int32_t g = t->threads_per_row;
+    if (g != 1 && g != 2 && g != 4 && g != 8 && g != 16 && g != 32 && g != 128)
+        return set_error(h, RMCM_EINVAL, "tuning: threads_per_row must be 1, 2, 4, 8, 16, 32 or 128");
+    if (t->hash_max_flops < 32 || t->hash_max_flops > (1 << 20))
+        return set_error(h, RMCM_EINVAL, "tuning: hash_max_flops must be in 32 .. 1048576");
+    if (t->dense_ratio < 1) return set_error(h, RMCM_EINVAL, "tuning: dense_ratio must be >= 1");
+    if (!(t->hash_load >= 0.1 && t->hash_load <= 0.75))
+        return set_error(h, RMCM_EINVAL, "tuning: hash_load must be in 0.1 .. 0.75");
+    h->tune.threads_per_row = g;
+    h->tune.hash_max_flops = t->hash_max_flops;
+    h->tune.dense_ratio = t->dense_ratio;
+    h->tune.hash_load = t->hash_load;
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_get_tuning(const rmcm_handle *h, rmcm_tuning *t) {
+    if (!h || !t) return RMCM_EINVAL;
+    t->threads_per_row = h->tune.threads_per_row;
+    t->hash_max_flops = h->tune.hash_max_flops;
+    t->dense_ratio = h->tune.dense_ratio;
+    t->reserved = 0;
+    t->hash_load = h->tune.hash_load;
+    return RMCM_OK;
+}
+
 RMCM_API int32_t rmcm_batch_create(rmcm_handle *h, rmcm_graph *g, const char *const *metapaths, int32_t count,
                                    int32_t lanes, rmcm_batch **out) {
     if (!h || !g || !metapaths || count < 1 || !out) return RMCM_EINVAL;

@@ -42,16 +42,20 @@ enum Bin {
     kBinHash8k = 3,
     kBinDense = 4,     // windowed dense accumulator (presence + counters) in shared memory
     kBinRank = 5,      // whole-row bitmap in shared memory, counts by rank with global atomics
-    kNumBins = 6
+    kBinMicro = 6,     // flops <= G (1, 2, 4, 8 or 16): G lanes per row, one product per lane
+    kNumBins = 7
 };
 
 // Tunables of the SpGEMM row binning (the autotuner searches these).
 struct Tuning {
-    int32_t tiny_max = 32;          // flops threshold of the warp-per-row bin (fixed by the kernel)
-    int32_t hash_max_flops = 4096;  // rows above go to the dense bin
+    // threads per short row (flops <= 32): 32 = a warp per row (k_tiny);
+    // 1..16 = that many lanes per row for rows of at most that many products
+    // (k_micro), the rest of the short rows a warp each; 128 = no short-row
+    // bins, short rows go to the 128-thread CTAs of the 512-slot hash bin
+    int32_t threads_per_row = 32;
+    int32_t hash_max_flops = 4096;  // rows above go to the dense / rank bins
     int32_t dense_ratio = 16;       // dense when flops * dense_ratio >= cols (and one window covers cols)
-    int32_t dense_threads = 256;
-    double hash_load = 0.5;         // hash table load factor bound: slots >= min(f, cols) / load
+    double hash_load = 0.5;         // hash table load factor bound: slots >= min(f, cols) / load, load <= 0.75
     bool dense_single_pass = true;  // dense rows in one window: one pass into a padded temporary
     int64_t dense_temp_max_bytes = 8LL << 30;
 };

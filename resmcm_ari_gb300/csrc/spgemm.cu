@@ -13,12 +13,15 @@
 //   3. symbolic     exact |C[u]| per bin kernel (same kernels, NUMERIC=false).
 //   4. scan         device exclusive scan of |C[u]| into C.rowptr (int64).
 //   5. numeric      columns + counts per bin kernel (NUMERIC=true).
-// Bins (see classify):
+// Bins (see classify; the thresholds are the handle's tunables):
+//   micro   flops <= G      G lanes per row (G = 1..16), one product per lane,
+//                           G-wide bitonic sort (only when G is tuned below 32).
 //   tiny    flops <= 32     one warp per row; products in registers, bitonic
 //                           sort across the warp, segmented sum, ballot compaction.
 //   hash*   flops <= 4096   one CTA per row; linear-probing hash table in shared
-//                           memory sized 2*min(flops, n) (512/2048/8192 slots),
-//                           then compaction and a shared-memory bitonic sort.
+//                           memory of at least min(flops, n) / load slots
+//                           (512/2048/8192; load 0.5 by default, at most 0.75),
+//                           then in-place compaction and a bitonic sort.
 //   dense   otherwise       one CTA per row; bitmap + counters over a window of
 //                           W columns in shared memory; rows wider than W are
 //                           processed window by window with per-entry cursors
@@ -30,6 +33,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -95,6 +99,9 @@ struct BinParams {
     int64_t dense_win;      // columns one numeric dense window covers
     int32_t hash_max;       // flops above -> dense or rank
     int32_t dense_ratio;    // dense when flops * ratio >= cols and one window covers cols
+    int32_t micro_max;      // flops <= micro_max -> micro bin (0: none)
+    int32_t tiny_max;       // flops <= tiny_max -> tiny bin (32, or 0: none)
+    int32_t inv_load_q8;    // 256 / hash load factor, rounded up
 };
 
 // Widest output row the rank bin holds in shared memory (bitmap + prefixes).
@@ -102,11 +109,13 @@ constexpr int64_t kRankCols = 1 << 20;
 
 __device__ __forceinline__ int classify(int64_t f, int64_t ncols, const BinParams &bp) {
     if (f == 0) return kEmptyBin;
-    if (f <= 32) return kBinTiny;
+    if (f <= bp.micro_max) return kBinMicro;
+    if (f <= bp.tiny_max) return kBinTiny;
     const bool one_window = ncols <= bp.dense_win;
     if (f > bp.hash_max) return (!one_window && ncols <= kRankCols) ? kBinRank : kBinDense;
     if (one_window && f * (int64_t)bp.dense_ratio >= ncols) return kBinDense;
-    const int64_t need = 2 * min(f, ncols);
+    const int64_t need = (min(f, ncols) * bp.inv_load_q8 + 255) >> 8;
+    if (need > 8192) return (!one_window && ncols <= kRankCols) ? kBinRank : kBinDense;
     if (need <= 512) return kBinHash512;
     if (need <= 2048) return kBinHash2k;
     return kBinHash8k;
@@ -314,6 +323,97 @@ __global__ void __launch_bounds__(256) k_tiny(DevCsr A, DevCsr B, DevCsr C, cons
     if (__any_sync(kFull, ovf) && lane == 0) raise_status(st, kOverflow);
 }
 
+// Micro bin: G lanes per row (G = 1, 2, 4, 8 or 16) for rows of at most G
+// products, 32/G rows per warp.  Lane g of a group takes the row's g-th
+// product (walking the A row until the B lengths pass g), the group sorts
+// its keys with a G-wide bitonic network (xor partners stay inside the
+// aligned group) and merges equal columns with segmented suffix sums, as
+// the warp-per-row bin does for up to 32 products.
+template <typename V, bool NUMERIC, int G>
+__global__ void __launch_bounds__(256) k_micro(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows, int32_t nrows,
+                                               int64_t *cnt, int *st) {
+    static_assert(G >= 1 && G <= 16 && (G & (G - 1)) == 0, "G must be a power of two up to 16");
+    constexpr int RPW = 32 / G;                       // rows per warp
+    const int lane = threadIdx.x & 31;
+    const int g = lane & (G - 1);
+    const int gbase = lane & ~(G - 1);
+    const unsigned gmask = G == 32 ? kFull : (((1u << G) - 1u) << gbase);
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const V *Aval = (const V *)A.val;
+    const V *Bval = (const V *)B.val;
+    bool ovf = false;
+    for (int64_t w0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * RPW; w0 < nrows; w0 += nwarps * RPW) {
+        const int64_t w = w0 + lane / G;
+        const bool active = w < nrows;
+        int32_t r = 0;
+        int32_t key = INT_MAX;
+        unsigned long long val = 0;
+        if (active) {
+            r = rows[w];
+            const int64_t a1 = A.rowptr[r + 1];
+            int64_t acc = 0;
+            for (int64_t k = A.rowptr[r]; k < a1 && acc <= g; k++) {
+                const int32_t a = A.col[k];
+                const int64_t bs = B.rowptr[a];
+                const int64_t len = B.rowptr[a + 1] - bs;
+                if (g < acc + len) {
+                    const int64_t q = bs + (g - acc);
+                    key = B.col[q];
+                    if (NUMERIC) {
+                        const unsigned long long va = Aval[k], vb = Bval[q];
+                        if (sizeof(V) != 4) ovf |= __umul64hi(va, vb) != 0;
+                        val = va * vb;
+                    }
+                }
+                acc += len;
+            }
+        }
+#pragma unroll
+        for (int kk = 2; kk <= G; kk <<= 1) {
+#pragma unroll
+            for (int j = kk >> 1; j > 0; j >>= 1) {
+                const int32_t ok = __shfl_xor_sync(kFull, key, j);
+                const unsigned long long ov = NUMERIC ? __shfl_xor_sync(kFull, val, j) : 0ull;
+                const bool up = (g & kk) == 0;
+                const bool lower = (g & j) == 0;
+                const bool take = (lower == up) ? (ok < key) : (ok > key);
+                if (take) { key = ok; if (NUMERIC) val = ov; }
+            }
+        }
+        const int32_t prev = __shfl_up_sync(kFull, key, 1, G);
+        const bool head = active && key != INT_MAX && (g == 0 || prev != key);
+        const unsigned heads = (__ballot_sync(kFull, head) & gmask) >> gbase;
+        if (!NUMERIC) {
+            if (active && g == 0) cnt[r] = __popc(heads);
+        } else {
+            unsigned long long sum = val;
+#pragma unroll
+            for (int d = 1; d < G; d <<= 1) {
+                const unsigned long long o = __shfl_down_sync(kFull, sum, d, G);
+                const int32_t okey = __shfl_down_sync(kFull, key, d, G);
+                if (g + d < G && okey == key) {
+                    ovf |= sum > ~0ull - o;
+                    sum += o;
+                }
+            }
+            if (sizeof(V) == 4 && head) ovf |= sum > 0xffffffffull;
+            if (active) {
+                const int64_t base = C.rowptr[r];
+                const int64_t rlen = C.rowptr[r + 1] - base;
+                if (g == 0 && rlen != __popc(heads)) raise_status(st, kInvariant);
+                if (head) {
+                    const int pos = __popc(heads & ((1u << g) - 1u));
+                    if (pos < rlen) {
+                        C.col[base + pos] = key;
+                        ((V *)C.val)[base + pos] = (V)sum;
+                    }
+                }
+            }
+        }
+    }
+    if (__any_sync(kFull, ovf) && lane == 0) raise_status(st, kOverflow);
+}
+
 // ------------------------------------------------------------------------
 // product stream shared by the hash and dense bins
 // ------------------------------------------------------------------------
@@ -492,7 +592,7 @@ __device__ __forceinline__ int hash_insert(int32_t *keys, V *vals, int32_t c, V 
         }
         h = (h + 1) & (S - 1);
     }
-    raise_status(st, kInvariant);   // table full: cannot happen with slots >= 2 * nnz
+    raise_status(st, kInvariant);   // table full: cannot happen, the bin keeps nnz <= 0.75 * slots
     return 0;
 }
 
@@ -549,8 +649,6 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
     extern __shared__ __align__(16) unsigned char smem[];
     int32_t *keys = (int32_t *)smem;
     V *vals = (V *)(keys + S);
-    int32_t *sk = (int32_t *)(vals + (NUMERIC ? S : 0));
-    V *sv = (V *)(sk + S / 2);
     __shared__ ChunkStage<V> sg;
     __shared__ int s_warp[NT / 32];
     const int tid = threadIdx.x;
@@ -578,23 +676,34 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
             const int total = block_excl_scan<NT>(fresh, &excl, s_warp);
             if (tid == 0) cnt[r] = total;
         } else {
+            // compact the occupied slots to the front of the table itself
+            // (each thread holds its slots in registers across the scan's
+            // barriers), then sort them there
             constexpr int PER = S / NT;
+            int32_t kr[PER];
+            V vr[PER];
             int mine = 0;
-#pragma unroll 4
-            for (int i = 0; i < PER; i++) mine += keys[tid * PER + i] != -1;
+#pragma unroll
+            for (int i = 0; i < PER; i++) {
+                kr[i] = keys[tid * PER + i];
+                vr[i] = vals[tid * PER + i];
+                mine += kr[i] != -1;
+            }
             int off;
             const int n = block_excl_scan<NT>(mine, &off, s_warp);
+#pragma unroll
             for (int i = 0; i < PER; i++) {
-                const int slot = tid * PER + i;
-                if (keys[slot] != -1) {
-                    sk[off] = keys[slot];
-                    sv[off] = vals[slot];
+                if (kr[i] != -1) {
+                    keys[off] = kr[i];
+                    vals[off] = vr[i];
                     off++;
                 }
             }
             int P = 1;
             while (P < n) P <<= 1;
-            for (int i = n + tid; i < P; i += NT) sk[i] = INT_MAX;
+            for (int i = n + tid; i < P; i += NT) keys[i] = INT_MAX;
+            int32_t *sk = keys;
+            V *sv = vals;
             __syncthreads();
             for (int kk = 2; kk <= P; kk <<= 1) {
                 for (int j = kk >> 1; j > 0; j >>= 1) {
@@ -1177,6 +1286,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
     int *st = h->d_status;
     int32_t off = 0;
     const int64_t ncols = B.cols;
+    const int micro_g = h->tune.threads_per_row;
     for (int b = 0; b < kNumBins; b++) {
         const int32_t n = counts[b];
         const int32_t *list = lists + off;
@@ -1188,9 +1298,20 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                 k_tiny<V, NUMERIC><<<grid, 256, 0, s>>>(A, B, C, list, n, cnt, st);
                 break;
             }
+            case kBinMicro: {
+                const int grid = grid_for(h, ((int64_t)n * micro_g + 31) / 32 * 32, 256, 8);
+                switch (micro_g) {
+                    case 1: k_micro<V, NUMERIC, 1><<<grid, 256, 0, s>>>(A, B, C, list, n, cnt, st); break;
+                    case 2: k_micro<V, NUMERIC, 2><<<grid, 256, 0, s>>>(A, B, C, list, n, cnt, st); break;
+                    case 4: k_micro<V, NUMERIC, 4><<<grid, 256, 0, s>>>(A, B, C, list, n, cnt, st); break;
+                    case 8: k_micro<V, NUMERIC, 8><<<grid, 256, 0, s>>>(A, B, C, list, n, cnt, st); break;
+                    default: k_micro<V, NUMERIC, 16><<<grid, 256, 0, s>>>(A, B, C, list, n, cnt, st); break;
+                }
+                break;
+            }
             case kBinHash512: {
                 constexpr int S = 512, NT = 128;
-                const int64_t sm = S * 4 + (NUMERIC ? S * sizeof(V) + (S / 2) * (4 + sizeof(V)) : 0);
+                const int64_t sm = S * 4 + (NUMERIC ? S * sizeof(V) : 0);
                 auto kern = k_hash<V, NUMERIC, S, NT>;
                 RMCM_TRY(set_smem(h, kern, sm));
                 kern<<<grid_for(h, (int64_t)n * NT, NT, 16), NT, sm, s>>>(A, B, C, list, n, cnt, st, bin_of);
@@ -1198,7 +1319,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
             }
             case kBinHash2k: {
                 constexpr int S = 2048, NT = 256;
-                const int64_t sm = S * 4 + (NUMERIC ? S * sizeof(V) + (S / 2) * (4 + sizeof(V)) : 0);
+                const int64_t sm = S * 4 + (NUMERIC ? S * sizeof(V) : 0);
                 auto kern = k_hash<V, NUMERIC, S, NT>;
                 RMCM_TRY(set_smem(h, kern, sm));
                 kern<<<grid_for(h, (int64_t)n * NT, NT, 8), NT, sm, s>>>(A, B, C, list, n, cnt, st, bin_of);
@@ -1206,7 +1327,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
             }
             case kBinHash8k: {
                 constexpr int S = 8192, NT = 512;
-                const int64_t sm = S * 4 + (NUMERIC ? S * sizeof(V) + (S / 2) * (4 + sizeof(V)) : 0);
+                const int64_t sm = S * 4 + (NUMERIC ? S * sizeof(V) : 0);
                 auto kern = k_hash<V, NUMERIC, S, NT>;
                 RMCM_TRY(set_smem(h, kern, sm));
                 kern<<<grid_for(h, (int64_t)n * NT, NT, 2), NT, sm, s>>>(A, B, C, list, n, cnt, st, bin_of);
@@ -1350,6 +1471,12 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     bp.dense_win = sizeof(V) == 4 ? kDenseWinU32 : kDenseWinU64;
     bp.hash_max = h->tune.hash_max_flops;
     bp.dense_ratio = h->tune.dense_ratio;
+    {
+        const int tpr = h->tune.threads_per_row;
+        bp.micro_max = tpr < 32 ? tpr : 0;
+        bp.tiny_max = tpr <= 32 ? 32 : 0;
+        bp.inv_load_q8 = (int32_t)std::ceil(256.0 / h->tune.hash_load);
+    }
     if (m > 0) {
         k_analyze<V><<<grid_for(h, m * 32, 256, 8), 256, 0, s>>>(A, B, bp, flops, bin_of, small, small + 16,
                                                                   (unsigned long long *)(small + 32), small + 40);

@@ -98,3 +98,61 @@ def test_bad_batch_arguments(native, engine):
         engine.batch(hg, ["0-0-1"])
     engine.set_order_mode(native.ORDER_RES)
     hg.close()
+
+
+@pytest.mark.parametrize("tpr", [1, 2, 4, 8, 16, 32, 128])
+def test_every_threads_per_row_gives_the_same_products(native, tpr):
+    """Short rows through the micro bin (1..16 lanes), a warp, or a CTA."""
+    fx = load_fixture("hin4_small")
+    g = make_graph(fx)
+    paths = [r["metapath"] for r in fx["paths"]]
+    eng = native.Engine(device=0)
+    hg = native.HeteroGraph.from_synthetic(eng, g)
+    ref = _plain_digests(native, eng, hg, paths)
+    eng.set_tuning(threads_per_row=tpr)
+    assert _plain_digests(native, eng, hg, paths) == ref
+    hg.close()
+    eng.close()
+
+
+@pytest.mark.parametrize("hash_max,load", [(32, 0.5), (128, 0.7), (512, 0.7), (8192, 0.5), (8192, 0.75)])
+def test_bin_thresholds_and_load_factors_give_the_same_products(native, hash_max, load):
+    rng = np.random.default_rng(hash_max)
+    import scipy.sparse as sp
+    A = sp.random(300, 4000, density=0.01, random_state=rng, format="csr", dtype=np.float64)
+    B = sp.random(4000, 9000, density=0.004, random_state=rng, format="csr", dtype=np.float64)
+    A.data[:] = rng.integers(1, 4, A.nnz)
+    B.data[:] = rng.integers(1, 4, B.nnz)
+    want = (A @ B).tocsr()
+    want.sort_indices()
+    eng = native.Engine(device=0)
+    eng.set_tuning(hash_max_flops=hash_max, hash_load=load, threads_per_row=4)
+    dA = eng.upload(A.indptr, A.indices, cols=A.shape[1], val=A.data.astype(np.uint64))
+    dB = eng.upload(B.indptr, B.indices, cols=B.shape[1], val=B.data.astype(np.uint64))
+    C = eng.spgemm(dA, dB)
+    rp, col, val = C.download()
+    assert np.array_equal(rp, want.indptr) and np.array_equal(col, want.indices)
+    assert np.array_equal(val, want.data.astype(np.uint64))
+    eng.close()
+
+
+def test_autotuner_keeps_results_and_picks_a_measured_best(native):
+    from resmcm_ari_gb300 import autotune, workloads
+    g = workloads.batch_graph(seed=2, scale=1 / 400)
+    paths = workloads.batch_walks(7, g, 32, lengths=(2, 6))
+    eng = native.Engine(device=0)
+    hg = native.HeteroGraph.from_synthetic(eng, g)
+    res = autotune.tune(eng, hg, paths, lanes=4, reps=2, mode="coordinate")
+    assert len(res["table"]) >= 8
+    assert res["best_s"] == min(t for _, t, _ in res["table"])
+    assert eng.get_tuning()["threads_per_row"] == res["best"]["threads_per_row"]
+    hg.close()
+    eng.close()
+
+
+def test_bad_tuning_is_rejected(native, engine):
+    for kw in ({"threads_per_row": 3}, {"hash_max_flops": 8}, {"hash_load": 0.9}, {"dense_ratio": 0}):
+        with pytest.raises(native.RmcmError):
+            engine.set_tuning(**kw)
+    assert engine.get_tuning() == {"threads_per_row": 32, "hash_max_flops": 4096, "dense_ratio": 16,
+                                   "hash_load": 0.5}
