@@ -66,6 +66,7 @@ typedef struct rmcm_handle rmcm_handle;
 typedef struct rmcm_graph rmcm_graph;
 typedef struct rmcm_mat rmcm_mat;
 typedef struct rmcm_batch rmcm_batch;
+typedef struct rmcm_server rmcm_server;
 
 typedef struct rmcm_opts {
     int32_t device;            /* CUDA device ordinal */
@@ -289,6 +290,61 @@ RMCM_API int32_t rmcm_batch_free(rmcm_handle *h, rmcm_batch *b);
  * over entries (r, c, v) of f(f(r * 2^32 + c) + v), f the splitmix64 output
  * function.  Equal matrices give equal digests.  Synchronises the stream. */
 RMCM_API int32_t rmcm_mat_digest(rmcm_handle *h, const rmcm_mat *m, uint64_t *nnz, uint64_t *digest);
+
+/* ---- query server ------------------------------------------------------------
+ * A request loop over resident graphs: the reference's per-meta-path steps
+ * (main(), efficient/resmcm.cpp:839-889: estimate, order, multiply) run for
+ * many queries at once on `lanes` worker threads, each with its own stream.
+ * A query is admitted when the device bytes its RES estimates predict (12
+ * bytes per estimated entry of every intermediate and of the result, plus
+ * row pointers and scratch) fit the budget left; one predicted above the
+ * whole budget completes with RMCM_ENOMEM; one that does not fit yet waits
+ * and is retried oldest first as bytes come back, while younger queries that
+ * fit go ahead.  Every query's result equals rmcm_run_metapath's in AUTO
+ * mode; a completed query reports its nnz and rmcm_mat_digest, and its
+ * result is freed.  Graphs are added before their queries are submitted and
+ * cannot be freed while the server lives; the owning handle must not be
+ * used by another thread meanwhile.  Times are seconds on the server clock
+ * (rmcm_server_now). */
+typedef struct rmcm_server_opts {
+    int32_t lanes;                  /* worker lanes (<= 0: 8) */
+    int32_t reserved;
+    int64_t mem_budget_bytes;       /* admission budget (<= 0: the handle's) */
+} rmcm_server_opts;
+typedef struct rmcm_query_result {
+    int64_t tag;                    /* the caller's tag from rmcm_server_submit */
+    int32_t status;                 /* RMCM_OK or the error */
+    int32_t graph;
+    int64_t nnz;
+    uint64_t digest;
+    double t_submit, t_admit, t_done;
+    double est_bytes;               /* predicted device bytes used for admission */
+    double es_s, dp_s;              /* estimator and DP device time */
+    int32_t valtype;                /* value type of the result */
+    int32_t lane;
+    char error[128];
+} rmcm_query_result;
+typedef struct rmcm_server_stats {
+    int64_t submitted, completed, rejected, pending, waiting;
+    int32_t running, max_running;
+    int32_t lanes, reserved_;
+    int64_t budget, reserved, peak_reserved, kernel_launches;
+} rmcm_server_counters;
+RMCM_API int32_t rmcm_server_create(rmcm_handle *h, const rmcm_server_opts *opts, rmcm_server **out);
+/* Builds the graph's uint32 leaves of every edge kind; *index names it in submit. */
+RMCM_API int32_t rmcm_server_add_graph(rmcm_server *s, rmcm_graph *g, int32_t *index);
+RMCM_API double rmcm_server_now(const rmcm_server *s);
+/* Queues a query; t_arrival >= 0 stamps its arrival (server clock) instead of now. */
+RMCM_API int32_t rmcm_server_submit(rmcm_server *s, int32_t graph, const char *metapath, int64_t tag,
+                                    double t_arrival);
+/* Completed queries, oldest first; waits up to wait_s for the first. */
+RMCM_API int32_t rmcm_server_poll(rmcm_server *s, rmcm_query_result *out, int32_t cap, int32_t *count,
+                                  double wait_s);
+/* Waits until no query is queued, waiting or running (timeout_s <= 0: no limit). */
+RMCM_API int32_t rmcm_server_drain(rmcm_server *s, double timeout_s);
+RMCM_API int32_t rmcm_server_stats(const rmcm_server *s, rmcm_server_counters *st);
+/* Drains, stops the workers and frees the lanes. */
+RMCM_API int32_t rmcm_server_destroy(rmcm_server *s);
 
 /* ---- RES estimator that allocates nothing --------------------------------
  * No counterpart in the reference.  For callers that may not allocate device

@@ -67,6 +67,32 @@ class Tuning(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
 
 
+class ServerOpts(C.Structure):
+    _fields_ = [("lanes", C.c_int32), ("reserved", C.c_int32), ("mem_budget_bytes", C.c_int64)]
+
+
+class QueryResult(C.Structure):
+    _fields_ = [("tag", C.c_int64), ("status", C.c_int32), ("graph", C.c_int32), ("nnz", C.c_int64),
+                ("digest", C.c_uint64), ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double),
+                ("est_bytes", C.c_double), ("es_s", C.c_double), ("dp_s", C.c_double), ("valtype", C.c_int32),
+                ("lane", C.c_int32), ("error", C.c_char * 128)]
+
+    def as_dict(self) -> dict:
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f != "error"}
+        d["error"] = self.error.decode(errors="replace")
+        return d
+
+
+class ServerCounters(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("rejected", C.c_int64),
+                ("pending", C.c_int64), ("waiting", C.c_int64), ("running", C.c_int32), ("max_running", C.c_int32),
+                ("lanes", C.c_int32), ("reserved_", C.c_int32), ("budget", C.c_int64), ("reserved", C.c_int64),
+                ("peak_reserved", C.c_int64), ("kernel_launches", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved_"}
+
+
 class ProductStats(C.Structure):
     _fields_ = [("rows", C.c_int64), ("inner", C.c_int64), ("cols", C.c_int64),
                 ("nnz_a", C.c_int64), ("nnz_b", C.c_int64), ("nnz_c", C.c_int64), ("flops", C.c_int64),
@@ -142,6 +168,14 @@ def lib():
         "rmcm_mat_digest": ([vp, vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], i32),
         "rmcm_set_tuning": ([vp, C.POINTER(Tuning)], i32),
         "rmcm_get_tuning": ([vp, C.POINTER(Tuning)], i32),
+        "rmcm_server_create": ([vp, C.POINTER(ServerOpts), pp], i32),
+        "rmcm_server_add_graph": ([vp, vp, C.POINTER(i32)], i32),
+        "rmcm_server_now": ([vp], C.c_double),
+        "rmcm_server_submit": ([vp, i32, C.c_char_p, i64, C.c_double], i32),
+        "rmcm_server_poll": ([vp, C.POINTER(QueryResult), i32, C.POINTER(i32), C.c_double], i32),
+        "rmcm_server_drain": ([vp, C.c_double], i32),
+        "rmcm_server_stats": ([vp, C.POINTER(ServerCounters)], i32),
+        "rmcm_server_destroy": ([vp], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -408,6 +442,56 @@ class Batch:
     def __del__(self):
         try:
             self.free()
+        except Exception:
+            pass
+
+
+class Server:
+    """Query server over resident graphs (rmcm_server_*): admission by
+    RES-predicted bytes, queries overlapping on ``lanes`` worker lanes."""
+
+    def __init__(self, engine: "Engine", lanes: int = 8, mem_budget_bytes: int = 0):
+        self.engine = engine
+        self.graphs = []
+        h = C.c_void_p()
+        o = ServerOpts(lanes, 0, mem_budget_bytes)
+        engine._check(lib().rmcm_server_create(engine._h, C.byref(o), C.byref(h)))
+        self._h = h
+
+    def add_graph(self, graph: "HeteroGraph") -> int:
+        idx = C.c_int32()
+        self.engine._check(lib().rmcm_server_add_graph(self._h, graph._h, C.byref(idx)))
+        self.graphs.append(graph)
+        return idx.value
+
+    def now(self) -> float:
+        return lib().rmcm_server_now(self._h)
+
+    def submit(self, graph: int, metapath: str, tag: int, t_arrival: float = -1.0):
+        self.engine._check(lib().rmcm_server_submit(self._h, graph, metapath.encode(), tag, t_arrival))
+
+    def poll(self, wait_s: float = 0.0, cap: int = 1024) -> list:
+        buf = (QueryResult * cap)()
+        n = C.c_int32()
+        self.engine._check(lib().rmcm_server_poll(self._h, buf, cap, C.byref(n), wait_s))
+        return [buf[i].as_dict() for i in range(n.value)]
+
+    def drain(self, timeout_s: float = 0.0):
+        self.engine._check(lib().rmcm_server_drain(self._h, timeout_s))
+
+    def stats(self) -> dict:
+        st = ServerCounters()
+        self.engine._check(lib().rmcm_server_stats(self._h, C.byref(st)))
+        return st.as_dict()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().rmcm_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass
 

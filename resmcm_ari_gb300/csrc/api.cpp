@@ -507,7 +507,7 @@ void dense_order(const int64_t *d, int32_t len, std::vector<int32_t> &split, std
 // widened here.
 int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int32_t *fixed_pairs, rmcm_mat **Cout,
                    rmcm_timings *t, bool widen, const std::function<int32_t(int, rmcm_mat **)> &leaf64,
-                   ChainLog *log = nullptr) {
+                   ChainLog *log = nullptr, bool order_given = false) {
     rmcm_timings tm{};
     *Cout = nullptr;
     // slot bookkeeping of the optional log
@@ -587,6 +587,14 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
         host_dp_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         memcpy(pairs, pl.data(), sizeof(int32_t) * 2 * (len - 1));
         cudaEventRecord(ev[2], s);
+        fixed_pairs = pairs;
+    }
+    if (order_given && fixed_pairs) {
+        // the caller ordered the chain already: no estimator, no DP
+        memcpy(pairs, fixed_pairs, sizeof(int32_t) * 2 * (len - 1));
+        cudaEventRecord(ev[1], s);
+        cudaEventRecord(ev[2], s);
+        host_dp_s = 0;
         fixed_pairs = pairs;
     }
     if (fixed_pairs == pairs) {
@@ -869,6 +877,56 @@ int32_t chain_replay(rmcm_handle *h, const ChainLog &log, uint64_t *digest_dev, 
 }
 
 }  // namespace
+
+namespace rmcm {
+
+int32_t leaf_of(rmcm_handle *h, rmcm_graph *g, int32_t src, int32_t sink, int32_t et, int32_t valtype,
+                rmcm_mat **out) {
+    return get_leaf(h, g, src, sink, et, valtype, out);
+}
+
+int32_t path_parse(const char *s, std::vector<int32_t> &vts, std::vector<int32_t> &ets) {
+    return parse_path(s, vts, ets);
+}
+
+int32_t chain_run_ordered(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int32_t *pairs, rmcm_mat **out,
+                          rmcm_timings *t, bool widen, const std::function<int32_t(int, rmcm_mat **)> &leaf64) {
+    return chain_exec(h, mats, len, pairs, out, t, widen, leaf64, nullptr, true);
+}
+
+int32_t chain_plan(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, double *c, int32_t *split, int32_t *pairs,
+                   double *es_s, double *dp_s) {
+    if (len < 2 || len > 16) return set_error(h, RMCM_EINVAL, "chain_plan: length must be 2..16");
+    cudaStream_t s = h->stream;
+    char *buf = nullptr;
+    const int64_t bytes = 8 * 256 + 8 * 256 + 4 * 256 + 4 * 64;
+    RMCM_TRY(dev_alloc(h, (void **)&buf, bytes));
+    double *c_dev = (double *)buf;
+    double *cost_dev = (double *)(buf + 8 * 256);
+    int32_t *split_dev = (int32_t *)(buf + 16 * 256);
+    int32_t *pairs_dev = (int32_t *)(buf + 16 * 256 + 4 * 256);
+    cudaEventRecord(h->ev[0], s);
+    int32_t rc = estimate(h, mats, len, c_dev);
+    cudaEventRecord(h->ev[1], s);
+    if (rc == RMCM_OK) rc = chain_order_dev(h, c_dev, len, split_dev, cost_dev, pairs_dev);
+    cudaEventRecord(h->ev[2], s);
+    std::vector<char> host(bytes);
+    if (rc == RMCM_OK) {
+        cudaError_t e = cudaMemcpyAsync(host.data(), buf, bytes, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = cuda_error(h, e, "chain plan download");
+    }
+    dev_free(h, buf, bytes);
+    if (rc != RMCM_OK) return rc;
+    if (c) memcpy(c, host.data(), sizeof(double) * len * len);
+    if (split) memcpy(split, host.data() + 16 * 256, sizeof(int32_t) * len * len);
+    if (pairs) memcpy(pairs, host.data() + 16 * 256 + 4 * 256, sizeof(int32_t) * 2 * (len - 1));
+    if (es_s) *es_s = elapsed_s(h->ev[0], h->ev[1]);
+    if (dp_s) *dp_s = elapsed_s(h->ev[1], h->ev[2]);
+    return RMCM_OK;
+}
+
+}  // namespace rmcm
 
 // ===========================================================================
 // C ABI

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <map>
 #include <set>
 #include <string>
@@ -177,6 +178,21 @@ int32_t chain_order_dev(rmcm_handle *h, const double *c_dev, int32_t len, int32_
                         int32_t *pairs_dev);
 // Launch-only form (no host round trip; usable under stream capture):
 // c16/split16/cost16 are 16x16 arrays, pairs32 holds 32 ints.
+// ---- executor entry points shared with the server -----------------------
+// Leaf CSR of (src, sink, et) in valtype, built on first use (owned by g).
+int32_t leaf_of(rmcm_handle *h, rmcm_graph *g, int32_t src, int32_t sink, int32_t et, int32_t valtype,
+                rmcm_mat **out);
+// Meta-path string -> vertex types (len+1) and edge types (len).
+int32_t path_parse(const char *s, std::vector<int32_t> &vts, std::vector<int32_t> &ets);
+// Runs a chain in the given post-order pair list (no estimator, no DP);
+// widen = uint32 with escalation to uint64 (leaf64 supplies uint64 leaves).
+int32_t chain_run_ordered(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int32_t *pairs, rmcm_mat **out,
+                          rmcm_timings *t, bool widen, const std::function<int32_t(int, rmcm_mat **)> &leaf64);
+// Estimates + DP of a chain: c (len*len), split (len*len) and the pair list
+// (2*(len-1)) on the host.
+int32_t chain_plan(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, double *c, int32_t *split, int32_t *pairs,
+                   double *es_s, double *dp_s);
+
 // Launches a digest of m into out_dev[0..1] (nnz, order-free entry hash);
 // capture-safe.
 int32_t mat_digest_launch(rmcm_handle *h, const rmcm_mat *m, uint64_t *out_dev);
