@@ -17,6 +17,14 @@ SpGEMM chain) over all four chains, results computed in full and freed.
   against the measured HBM copy bandwidth.
 * cpu_baseline: the oracle port of the reference's algorithm (Boolean
   Gustavson, OpenMP, all host cores) on the same four chains.
+* batched: 512 seeded random-walk meta-paths (2-10 matrices) over a five-type
+  schema graph, one at a time through rmcm_run_metapath versus one batch
+  recorded once and replayed as a CUDA graph (after the autotuner's sweep of
+  the row-binning tunables); chains/s of both and whether every nnz matches.
+* served: Poisson query streams over two resident graphs (the A/P/V graph and
+  the retail graph) at two offered rates, the plain one-query-at-a-time path
+  versus the query server; queries/s, p50 and p99 latency of both and
+  whether every result (nnz + digest) matches.
 
 --impl reference times that CPU implementation alone, as the reference arm.
 Multi-GPU (torchrun): every rank runs the full workload on its own GPU
@@ -58,6 +66,8 @@ def parse():
     ap.add_argument("--no-clocks", action="store_true")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--detail", action="store_true", help="per-product stats to stderr")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched (CUDA graph) section")
+    ap.add_argument("--no-served", action="store_true", help="skip the served (query server) section")
     return ap.parse_args()
 
 
@@ -203,6 +213,83 @@ def run_reference(args):
             "note": "oracle port of efficient/resmcm.cpp (Boolean bitmap Gustavson, OpenMP dynamic schedule); "
                     "the reference source itself is not present on this host"}
     print(json.dumps(line), flush=True)
+
+
+def batched_section(rg, device, seed=2, scale=1 / 200, count=512, lanes=8, reps=5, tune=True):
+    """512 seeded random-walk meta-paths of 2-10 matrices over the five-type
+    schema graph (vertex counts x``scale``): one chain at a time through
+    rmcm_run_metapath, then as one batch replayed as a CUDA graph."""
+    from resmcm_ari_gb300 import autotune, workloads
+    g = workloads.batch_graph(seed=seed, scale=scale)
+    paths = workloads.batch_walks(3, g, count, lengths=(2, 10))
+    eng = rg.Engine(device=device)
+    hg = rg.HeteroGraph.from_synthetic(eng, g)
+    for mp in paths:                                   # leaves built untimed
+        eng.run_metapath(hg, mp, keep=False)
+    t0 = time.perf_counter()
+    plain_nnz = [eng.run_metapath(hg, mp, keep=False)[1]["nnz"] for mp in paths]
+    plain_s = time.perf_counter() - t0
+    out = {"workload": f"five-type schema graph (vertex counts x{scale:g} of 10k-500k), {count} random-walk "
+                       f"meta-paths of 2-10 matrices, uint32 with uint64 escalation",
+           "type_sizes": g.type_sizes, "chains": count, "lanes": lanes,
+           "plain_chains_per_s": count / plain_s, "result_nnz": int(sum(plain_nnz))}
+    if tune:
+        t0 = time.perf_counter()
+        res = autotune.tune(eng, hg, paths, lanes=lanes, reps=2, mode="coordinate")
+        out["autotune"] = {"best": res["best"], "best_ms": res["best_s"] * 1e3, "default_ms": res["default_s"] * 1e3,
+                           "candidates": len(res["table"]), "seconds": time.perf_counter() - t0}
+    t0 = time.perf_counter()
+    b = eng.batch(hg, paths, lanes=lanes)
+    out["record_s"] = time.perf_counter() - t0
+    info = b.info()
+    walls, devs, same = [], [], True
+    for _ in range(reps):
+        t1 = time.perf_counter()
+        nnz, _, dev = b.run()
+        walls.append(time.perf_counter() - t1)
+        devs.append(dev)
+        same = same and list(map(int, nnz)) == list(map(int, plain_nnz))
+    wall = sorted(walls)[len(walls) // 2]
+    out.update({"batched_chains_per_s": count / wall, "speedup_vs_plain": plain_s / wall,
+                "ms_per_run": wall * 1e3, "device_ms_per_run": sorted(devs)[len(devs) // 2] * 1e3,
+                "graph_nodes": info["graph_nodes"], "gpu_launches_per_run": info["launches_per_run"],
+                "identical_nnz": same, "tuning": eng.get_tuning()})
+    b.free()
+    hg.close()
+    eng.close()
+    return out
+
+
+def served_section(rg, eng, hg_retail, g_retail, rates=(100.0, 2000.0), queries=300, lanes=8):
+    """Poisson streams of meta-path queries (2-8 matrices) over two resident
+    graphs, the A/P/V graph and the retail graph, 50/50: plain one query at a
+    time versus the query server (admission against 64 GB)."""
+    from resmcm_ari_gb300 import serve, synth
+    g0 = synth.dblp_like()
+    hg0 = rg.HeteroGraph.from_synthetic(eng, g0)
+    cats = [serve.catalog(eng, hg0, g0, 24, seed=1, max_bytes=4e9),
+            serve.catalog(eng, hg_retail, g_retail, 24, seed=2, max_bytes=4e9)]
+    srv = rg.Server(eng, lanes=lanes, mem_budget_bytes=64 << 30)
+    srv.add_graph(hg0)
+    srv.add_graph(hg_retail)
+    out = {"workload": "Poisson arrivals, 2-8-matrix random-walk meta-paths (24 per graph, RES-predicted "
+                       "bytes <= 4 GB) over the A/P/V graph and the retail graph, 50/50",
+           "budget_bytes": 64 << 30, "lanes": lanes, "rates": []}
+    for rate in rates:
+        stream = serve.poisson_stream(7, rate, queries, cats)
+        p = serve.run_plain(eng, [hg0, hg_retail], stream)
+        s_ = serve.run_served(srv, stream)
+        same = all(s_["results"][i] == p["results"][i] for i in range(len(stream)))
+        out["rates"].append({"offered_qps": rate, "queries": queries,
+                             "plain": {k: p[k] for k in ("qps", "p50_ms", "p99_ms")},
+                             "served": {k: s_[k] for k in ("qps", "p50_ms", "p99_ms")},
+                             "qps_ratio": s_["qps"] / p["qps"], "identical_results": same})
+    st = srv.stats()
+    out["peak_reserved_bytes"] = st["peak_reserved"]
+    out["max_running"] = st["max_running"]
+    srv.close()
+    hg0.close()
+    return out
 
 
 def select(mps, spec):
@@ -382,6 +469,12 @@ def main():
         e2e = {"value": len(mps) * ws / e2e_s, "unit": "chains/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3}
 
+    batched = served = None
+    if rank == 0 and not args.no_batched:
+        batched = batched_section(rg, local)
+    if rank == 0 and not args.no_served:
+        served = served_section(rg, eng, hg, g)
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_reference(g, mps, 1, 0, f"one full pass over the {len(mps)} chains ({WORKLOAD})")
@@ -402,6 +495,7 @@ def main():
             "nnz_per_s": step_nnz * ws / (ms_per_step / 1e3),
             "result_nnz_per_step": step_nnz,
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+            "batched": batched, "served": served,
         }
         print(json.dumps(line), flush=True)
     hg.close()
