@@ -326,6 +326,11 @@ int32_t upload_csr(rmcm_handle *h, int64_t rows, int64_t cols, const int64_t *ro
         mat_release(h, m);
         return cuda_error(h, e, "upload");
     }
+    {
+        int64_t mx = 0;
+        for (int64_t r = 0; r < rows; r++) mx = std::max<int64_t>(mx, rowptr[r + 1] - rowptr[r]);
+        m->max_row = mx;
+    }
     if (!val) {
         int32_t rc = fill_ones(h, m->d.val, nnz, valtype);
         if (rc != RMCM_OK) {
@@ -440,6 +445,7 @@ int32_t copy_mat(rmcm_handle *h, const rmcm_mat *src, rmcm_mat **out) {
     }
     m->ones = src->ones;
     m->positive = src->positive;
+    m->max_row = src->max_row;
     m->distinct = src->distinct;
     *out = m;
     return RMCM_OK;
@@ -975,6 +981,9 @@ RMCM_API int32_t rmcm_create(rmcm_handle **out, const rmcm_opts *opts) {
         }
     }
     for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&h->ev[i]);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_status, sizeof(int) * kNumStatus);
     if (e == cudaSuccess) e = cudaMemset(h->d_status, 0, sizeof(int) * kNumStatus);
     if (e == cudaSuccess) e = cudaMallocHost((void **)&h->h_status, sizeof(int) * kNumStatus);
@@ -1019,6 +1028,9 @@ RMCM_API int32_t rmcm_destroy(rmcm_handle *h) {
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
     for (auto &e : h->ev)
         if (e) cudaEventDestroy(e);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->aux) cudaStreamDestroy(h->aux);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return RMCM_OK;

@@ -77,6 +77,9 @@ struct ProductPlan {
     int64_t flops = 0;
     int64_t nnz = 0;
     bool dense_temp = false;
+    int64_t max_dense_flops = 0;
+    int64_t c_max_row = -1;
+    bool split = false;
     int64_t scratch_bytes = 0;
 };
 
@@ -90,6 +93,7 @@ struct rmcm_mat {
     bool positive = false;              // every value is >= 1 (a counter > 0 then marks presence)
     bool distinct = false;              // no column repeats within a row
     uint64_t *rowsum = nullptr;         // lazily computed row sums (device), owned
+    int64_t max_row = -1;               // longest row (entries); -1 when unknown
     int64_t bytes = 0;
 };
 
@@ -110,6 +114,10 @@ struct rmcm_handle {
     void *scratch = nullptr;
     int64_t scratch_bytes = 0;
     cudaEvent_t ev[8] = {};
+    // second stream for work that overlaps the main stream's kernels inside
+    // one operation (forked and joined with the two events)
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     rmcm::Tuning tune;
     int32_t prof_level = 0;
     std::vector<rmcm::ProdRecord> prof;

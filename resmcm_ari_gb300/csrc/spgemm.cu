@@ -132,46 +132,166 @@ __device__ __forceinline__ unsigned long long sat_add(unsigned long long a, unsi
 // safe (its kernels skip the overflow checks), and a row with S greater than
 // (its possible distinct columns) x (largest value) is certain to overflow,
 // which raises *certain.
+// Per-product totals of the analysis, accumulated per CTA in shared memory
+// and added to the global words once per CTA.
+struct AnalyzeOut {
+    int64_t *flops;                        // per row
+    uint8_t *bin_of;                       // per row
+    int32_t *bin_count;                    // [kNumBins]
+    int32_t *dense_max_alen;
+    unsigned long long *flops_total;
+    int32_t *certain;
+    unsigned long long *dense_max_flops;
+};
+
+struct AnalyzeShared {
+    int32_t cnt[kNumBins];
+    int32_t max_alen;
+    int32_t certain;
+    unsigned long long flops;
+    unsigned long long max_flops;
+};
+
+__device__ __forceinline__ void analyze_shared_init(AnalyzeShared &sh) {
+    if (threadIdx.x < kNumBins) sh.cnt[threadIdx.x] = 0;
+    if (threadIdx.x == 0) {
+        sh.max_alen = 0;
+        sh.certain = 0;
+        sh.flops = 0;
+        sh.max_flops = 0;
+    }
+}
+
+__device__ __forceinline__ void analyze_shared_flush(AnalyzeShared &sh, const AnalyzeOut &o) {
+    if (threadIdx.x < kNumBins && sh.cnt[threadIdx.x]) atomicAdd(o.bin_count + threadIdx.x, sh.cnt[threadIdx.x]);
+    if (threadIdx.x == 0) {
+        if (sh.flops) atomicAdd(o.flops_total, sh.flops);
+        if (sh.max_alen) atomicMax(o.dense_max_alen, sh.max_alen);
+        if (sh.max_flops) atomicMax(o.dense_max_flops, sh.max_flops);
+        if (sh.certain) atomicOr(o.certain, 1);
+    }
+}
+
+// Bin, overflow flags and totals of row r from its products f and its
+// saturating count bound srow.
 template <typename V>
-__global__ void k_analyze(DevCsr A, DevCsr B, BinParams bp, int64_t *flops, uint8_t *bin_of,
-                          int32_t *bin_count, int32_t *dense_max_alen, unsigned long long *flops_total,
-                          int32_t *certain) {
+__device__ __forceinline__ void analyze_row(int64_t r, int64_t f, unsigned long long srow, int64_t alen,
+                                            int64_t ncols, const BinParams &bp, const AnalyzeOut &o,
+                                            AnalyzeShared &sh) {
+    const int b = classify(f, ncols, bp);
+    const unsigned long long vmax = sizeof(V) == 4 ? 0xffffffffull : ~0ull;
+    const bool risky = sizeof(V) == 4 ? srow > vmax : srow == ~0ull;
+    o.flops[r] = f;
+    o.bin_of[r] = (uint8_t)(b | (risky ? kRiskyBit : 0));
+    if (f) atomicAdd(&sh.flops, (unsigned long long)f);
+    if (sizeof(V) == 4 && risky) {
+        const unsigned long long distinct = (unsigned long long)min(f, ncols);
+        if (srow == ~0ull || srow / vmax > distinct) sh.certain = 1;
+    }
+    if (b != kEmptyBin) {
+        atomicAdd(&sh.cnt[b], 1);
+        if (b == kBinDense) {
+            atomicMax(&sh.max_alen, (int32_t)(alen < (int64_t)INT_MAX ? alen : (int64_t)INT_MAX));
+            atomicMax(&sh.max_flops, (unsigned long long)f);
+        }
+    }
+}
+
+// Products and count bound of A entries [k0, k1) (strided by `step` from k0).
+template <typename V>
+__device__ __forceinline__ void analyze_entries(const DevCsr &A, const DevCsr &B, int64_t k0, int64_t k1, int step,
+                                                int64_t &f, unsigned long long &srow) {
+    const V *Aval = (const V *)A.val;
+    for (int64_t k = k0; k < k1; k += step) {
+        const int32_t a = A.col[k];
+        const int64_t len = B.rowptr[a + 1] - B.rowptr[a];
+        f += len;
+        const unsigned long long bsum = B.rowsum ? B.rowsum[a] : (unsigned long long)len;
+        const unsigned long long av = Aval[k];
+        const unsigned long long prod = __umul64hi(av, bsum) ? ~0ull : av * bsum;
+        srow = sat_add(srow, prod);
+    }
+}
+
+// Warp per row of A: flops and bin; per-bin row counts and the longest
+// A row of the dense bin (it sizes the cursor scratch).  It also bounds the
+// row's total count S = sum_k A[r][k] * rowsum(B[k]) (saturating): no entry
+// of the row can exceed S, so a row with S within the value type is marked
+// safe (its kernels skip the overflow checks), and a row with S greater than
+// (its possible distinct columns) x (largest value) is certain to overflow,
+// which raises *certain.  Rows with more than long_min entries are left to
+// k_analyze_long (appended to long_list) so no warp walks a huge row alone.
+template <typename V>
+__global__ void __launch_bounds__(256) k_analyze(DevCsr A, DevCsr B, BinParams bp, AnalyzeOut o, int64_t long_min,
+                                                 int32_t *long_list, int32_t *nlong) {
+    __shared__ AnalyzeShared sh;
+    analyze_shared_init(sh);
+    __syncthreads();
     const int lane = threadIdx.x & 31;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const V *Aval = (const V *)A.val;
     for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < A.rows; r += nwarps) {
         const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
+        if (a1 - a0 > long_min) {
+            if (lane == 0) long_list[atomicAdd(nlong, 1)] = (int32_t)r;
+            continue;
+        }
         int64_t f = 0;
         unsigned long long srow = 0;
-        for (int64_t k = a0 + lane; k < a1; k += 32) {
-            const int32_t a = A.col[k];
-            const int64_t len = B.rowptr[a + 1] - B.rowptr[a];
-            f += len;
-            const unsigned long long bsum = B.rowsum ? B.rowsum[a] : (unsigned long long)len;
-            const unsigned long long av = Aval[k];
-            const unsigned long long prod = __umul64hi(av, bsum) ? ~0ull : av * bsum;
-            srow = sat_add(srow, prod);
-        }
+        analyze_entries<V>(A, B, a0 + lane, a1, 32, f, srow);
+        f = warp_sum(f);
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) srow = sat_add(srow, __shfl_xor_sync(kFull, srow, d));
+        if (lane == 0) analyze_row<V>(r, f, srow, a1 - a0, B.cols, bp, o, sh);
+    }
+    __syncthreads();
+    analyze_shared_flush(sh, o);
+}
+
+// Long rows: the whole grid walks each long row, CTA b taking the b-th slice
+// of its entries; partial products (int64) and count bounds (uint64, with a
+// saturation flag) meet in per-row accumulators.
+template <typename V>
+__global__ void __launch_bounds__(256) k_analyze_long(DevCsr A, DevCsr B, const int32_t *long_list,
+                                                      const int32_t *nlong, unsigned long long *acc_f,
+                                                      unsigned long long *acc_s, int32_t *sat) {
+    const int nl = *nlong;
+    const int lane = threadIdx.x & 31;
+    for (int j = 0; j < nl; j++) {
+        const int32_t r = long_list[j];
+        const int64_t a0 = A.rowptr[r], alen = A.rowptr[r + 1] - a0;
+        const int64_t k0 = a0 + alen * blockIdx.x / gridDim.x, k1 = a0 + alen * (blockIdx.x + 1) / gridDim.x;
+        int64_t f = 0;
+        unsigned long long srow = 0;
+        analyze_entries<V>(A, B, k0 + threadIdx.x, k1, blockDim.x, f, srow);
         f = warp_sum(f);
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) srow = sat_add(srow, __shfl_xor_sync(kFull, srow, d));
         if (lane == 0) {
-            const int b = classify(f, B.cols, bp);
-            const unsigned long long vmax = sizeof(V) == 4 ? 0xffffffffull : ~0ull;
-            const bool risky = sizeof(V) == 4 ? srow > vmax : srow == ~0ull;
-            flops[r] = f;
-            bin_of[r] = (uint8_t)(b | (risky ? kRiskyBit : 0));
-            if (f) atomicAdd(flops_total, (unsigned long long)f);
-            if (sizeof(V) == 4 && risky) {
-                const unsigned long long distinct = (unsigned long long)min(f, B.cols);
-                if (srow == ~0ull || srow / vmax > distinct) atomicOr(certain, 1);
-            }
-            if (b != kEmptyBin) {
-                atomicAdd(bin_count + b, 1);
-                if (b == kBinDense) atomicMax(dense_max_alen, (int32_t)(a1 - a0 < (int64_t)INT_MAX ? a1 - a0 : (int64_t)INT_MAX));
+            if (f) atomicAdd(acc_f + j, (unsigned long long)f);
+            if (srow) {
+                const unsigned long long old = atomicAdd(acc_s + j, srow);
+                if (srow == ~0ull || old > ~0ull - srow) atomicOr(sat + j, 1);
             }
         }
     }
+}
+
+template <typename V>
+__global__ void __launch_bounds__(256) k_analyze_long_finish(DevCsr A, DevCsr B, BinParams bp, AnalyzeOut o,
+                                                             const int32_t *long_list, const int32_t *nlong,
+                                                             const unsigned long long *acc_f,
+                                                             const unsigned long long *acc_s, const int32_t *sat) {
+    __shared__ AnalyzeShared sh;
+    analyze_shared_init(sh);
+    __syncthreads();
+    const int nl = *nlong;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nl; j += gridDim.x * blockDim.x) {
+        const int32_t r = long_list[j];
+        const unsigned long long srow = sat[j] ? ~0ull : acc_s[j];
+        analyze_row<V>(r, (int64_t)acc_f[j], srow, A.rowptr[r + 1] - A.rowptr[r], B.cols, bp, o, sh);
+    }
+    __syncthreads();
+    analyze_shared_flush(sh, o);
 }
 
 // Saturating row sums of a matrix's values (warp per row).
@@ -757,11 +877,11 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
 // stride `tstride` entries) and its length goes to cnt[r]; the symbolic pass
 // is skipped for these rows and k_copy_rows compacts the slots into C.
 template <typename V, bool NUMERIC, bool TEMP>
-__global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows,
+__global__ void __launch_bounds__(kDenseThreads, sizeof(V) == 4 ? 3 : 1) k_dense(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows,
                                                          int32_t nrows, int64_t *cnt, int32_t *cursors,
                                                          int64_t cur_stride, int32_t W, int *st, int64_t tstride,
                                                          const uint8_t *bin_of, bool positive, bool b_distinct,
-                                                         bool abort_mode) {
+                                                         bool abort_mode, const int32_t *skip) {
     constexpr int NT = kDenseThreads;
     constexpr int kPull = 4;   // register accumulators per thread: windows of up to 4 * NT columns
     static_assert(kChunk == NT, "the dense kernel stages one A entry per thread");
@@ -793,6 +913,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
             __syncthreads();
             if (s_abort) break;
         }
+        if (skip && skip[ri] >= 0) continue;   // a split row: written by the split kernels
         const int32_t r = rows[ri];
         const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
         // A row that cannot overflow needs no checks, and when every input
@@ -991,6 +1112,181 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
 }
 
 // ------------------------------------------------------------------------
+// split dense rows (single-window rows whose products exceed a fair share)
+// ------------------------------------------------------------------------
+//
+// One CTA per dense row leaves the device idle behind the heaviest row when
+// rows are skewed (a few Zipf-popular rows holding most of the products).
+// Such a row is split by ranges of its A entries into parts; a CTA per part
+// accumulates its range in a shared-memory window (presence bytes + counters,
+// as the dense bin does) and adds the window's nonzero counters into a global
+// per-row accumulator (uint64 counters + presence bits).  One CTA per split
+// row then writes the row in column order.  Counts are non-negative, so a
+// part overflows only if the whole row does.
+
+constexpr int kSplitThreads = 512;
+
+// Per dense-list row: number of parts (>= 2 only above fpart) and a slot.
+__global__ void k_split_select(const int32_t *rows, int32_t n, const int64_t *flops, int64_t fpart, int32_t pmax,
+                               int32_t *slot_of, int32_t *row_of_slot, int32_t *parts, int32_t *nslots,
+                               int32_t max_slots) {
+    for (int64_t ri = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; ri < n; ri += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t f = flops[rows[ri]];
+        int32_t slot = -1;
+        if (f > fpart) {
+            const int64_t p = min((int64_t)pmax, (f + fpart - 1) / fpart);
+            const int32_t s_ = atomicAdd(nslots, 1);
+            if (s_ < max_slots) {
+                slot = s_;
+                row_of_slot[s_] = (int32_t)ri;
+                parts[s_] = (int32_t)p;
+            }
+        }
+        slot_of[ri] = slot;
+    }
+}
+
+// Exclusive scan of the parts of the used slots (one block, max_slots <= 1024).
+__global__ void __launch_bounds__(1024) k_split_tasks(const int32_t *parts, const int32_t *nslots, int32_t max_slots,
+                                                      int32_t *task_start) {
+    __shared__ int s_warp[32];
+    const int ns = min(*nslots, max_slots);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int v = tid < ns ? parts[tid] : 0;
+    int incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int o = __shfl_up_sync(kFull, incl, d);
+        if (lane >= d) incl += o;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    int base = 0;
+    for (int w = 0; w < warp; w++) base += s_warp[w];
+    if (tid < ns) task_start[tid] = base + incl - v;
+    if (tid == ns - 1) task_start[ns] = base + incl;
+    if (ns == 0 && tid == 0) task_start[0] = 0;
+}
+
+// One CTA per task (slot, part): the part's A-entry range into the shared
+// window, then its nonzero counters into the slot's global accumulator.
+template <typename V>
+__global__ void __launch_bounds__(kSplitThreads) k_dense_split(DevCsr A, DevCsr B, const int32_t *rows,
+                                                               const int32_t *row_of_slot, const int32_t *parts,
+                                                               const int32_t *task_start, const int32_t *nslots,
+                                                               int32_t max_slots, int32_t W,
+                                                               unsigned long long *G, uint32_t *Gbits,
+                                                               const uint8_t *bin_of, int *st) {
+    constexpr int NT = kSplitThreads;
+    using AtomV = typename std::conditional<sizeof(V) == 4, unsigned int, unsigned long long>::type;
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint8_t *present = smem;
+    V *acc = (V *)(smem + (((size_t)W + 15) & ~(size_t)15));
+    __shared__ ChunkStage<V> sg;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int ns = min(*nslots, max_slots);
+    const int ntasks = task_start[ns];
+    for (int i = tid; i < W / 16; i += NT) ((uint4 *)present)[i] = make_uint4(0, 0, 0, 0);
+    for (int i = tid; i < W; i += NT) acc[i] = 0;
+    bool ovf = false;
+    __syncthreads();
+    for (int task = blockIdx.x; task < ntasks; task += gridDim.x) {
+        int lo = 0, hi = ns - 1;   // last slot with task_start <= task
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (task_start[mid] <= task) lo = mid;
+            else hi = mid - 1;
+        }
+        const int slot = lo;
+        const int part = task - task_start[slot];
+        const int np = parts[slot];
+        const int32_t r = rows[row_of_slot[slot]];
+        const int64_t a0 = A.rowptr[r], alen = A.rowptr[r + 1] - a0;
+        const int64_t ka = a0 + alen * part / np, kb = a0 + alen * (part + 1) / np;
+        const bool checked = (bin_of[r] & kRiskyBit) != 0;
+        for (int64_t k0 = ka; k0 < kb; k0 += kChunk) {
+            const int n = (int)(kb - k0 < (int64_t)kChunk ? kb - k0 : (int64_t)kChunk);
+            stage_full_rows<NT, V, true>(sg, A, B, k0, n);
+            stream_chunk<NT, V, true>(sg, n, B, checked, ovf, [&](int32_t c, V p) {
+                present[c] = 1;
+                if (checked) add_shared_chk(acc + c, p, ovf);
+                else atomicAdd((AtomV *)(acc + c), (AtomV)p);
+            });
+            __syncthreads();
+        }
+        // merge: one global atomic per present column, then clear the window
+        unsigned long long *g = G + (int64_t)slot * W;
+        uint32_t *gb = Gbits + (int64_t)slot * (W / 32);
+        for (int c = tid; c < W; c += NT) {
+            const bool here = present[c] != 0;
+            const unsigned bits = __ballot_sync(kFull, here);
+            if (here) {
+                const unsigned long long v = (unsigned long long)acc[c];
+                if (v) {
+                    const unsigned long long old = atomicAdd(g + c, v);
+                    ovf |= old > ~0ull - v;
+                }
+                present[c] = 0;
+                acc[c] = 0;
+            }
+            if (lane == 0 && bits) atomicOr(gb + (c >> 5), bits);
+        }
+        __syncthreads();
+    }
+    if (__syncthreads_or(ovf) && tid == 0) raise_status(st, kOverflow);
+}
+
+// One CTA per split row: the accumulated row, in column order, into its
+// padded slot of the temporary (row ri at ri * tstride); its length to cnt.
+template <typename V>
+__global__ void __launch_bounds__(kSplitThreads) k_split_finish(DevCsr T, const int32_t *rows,
+                                                                const int32_t *row_of_slot, const int32_t *nslots,
+                                                                int32_t max_slots, int64_t ncols, int32_t W,
+                                                                const unsigned long long *G, const uint32_t *Gbits,
+                                                                int64_t tstride, int64_t *cnt, int *st) {
+    constexpr int NT = kSplitThreads, NW = NT / 32;
+    __shared__ int64_t s_warp[NW];
+    const int ns = min(*nslots, max_slots);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    bool ovf = false;
+    for (int slot = blockIdx.x; slot < ns; slot += gridDim.x) {
+        const int32_t ri = row_of_slot[slot];
+        const int32_t r = rows[ri];
+        const unsigned long long *g = G + (int64_t)slot * W;
+        const uint32_t *gb = Gbits + (int64_t)slot * (W / 32);
+        const int groups = (int)((ncols + 31) >> 5);
+        const int gchunk = (groups + NW - 1) / NW;
+        const int g0 = min(warp * gchunk, groups), g1 = min(g0 + gchunk, groups);
+        int64_t mine = 0;
+        for (int q = g0; q < g1; q++) mine += __popc(gb[q]);
+        if (lane == 0) s_warp[warp] = mine;
+        __syncthreads();
+        int64_t base = 0, total = 0;
+        for (int w = 0; w < NW; w++) {
+            if (w < warp) base += s_warp[w];
+            total += s_warp[w];
+        }
+        int64_t pos = (int64_t)ri * tstride + base;
+        for (int q = g0; q < g1; q++) {
+            const unsigned bits = gb[q];
+            if (bits & (1u << lane)) {
+                const int64_t o = pos + __popc(bits & lt_mask);
+                const int32_t c = q * 32 + lane;
+                const unsigned long long v = g[c];
+                if (sizeof(V) == 4) ovf |= v > 0xffffffffull;
+                T.col[o] = c;
+                ((V *)T.val)[o] = (V)v;
+            }
+            pos += __popc(bits);
+        }
+        if (tid == 0) cnt[r] = total;
+        __syncthreads();
+    }
+    if (__syncthreads_or(ovf) && tid == 0) raise_status(st, kOverflow);
+}
+
+// ------------------------------------------------------------------------
 // rank bin: wide rows (more columns than a dense window, at most kRankCols)
 // ------------------------------------------------------------------------
 //
@@ -1158,15 +1454,21 @@ __device__ __forceinline__ int64_t block_scan_i64(int64_t v, int64_t *s_warp, in
 
 // rowptr[i+1] = inclusive partial sums within a tile; tile sums to tile_sum.
 __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int64_t *cnt, int64_t m, int64_t *rowptr,
-                                                             int64_t *tile_sum) {
+                                                             int64_t *tile_sum, unsigned long long *row_max) {
     __shared__ int64_t s_warp[32];
     const int64_t t0 = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
     int64_t v[kScanItems];
-    int64_t s = 0;
+    int64_t s = 0, mx = 0;
 #pragma unroll
     for (int i = 0; i < kScanItems; i++) {
         v[i] = (t0 + i < m) ? cnt[t0 + i] : 0;
         s += v[i];
+        mx = max(mx, v[i]);
+    }
+    if (row_max) {
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) mx = max(mx, (int64_t)__shfl_xor_sync(kFull, mx, d));
+        if ((threadIdx.x & 31) == 0 && mx > 0) atomicMax(row_max, (unsigned long long)mx);
     }
     int64_t tot;
     int64_t run = block_scan_i64(s, s_warp, &tot);
@@ -1268,14 +1570,33 @@ int32_t set_smem(rmcm_handle *h, F *kernel, int64_t bytes) {
     return RMCM_OK;
 }
 
-// Row-padded temporary of the single-pass dense rows.
+// Row-padded temporary of the single-pass dense rows, and the buffers of the
+// rows split over several CTAs.
 struct DenseTemp {
     bool active = false;
     int32_t *col = nullptr;
     void *val = nullptr;
     int64_t stride = 0;
     int64_t bytes = 0;
+    // split rows
+    bool split = false;
+    const int64_t *flops = nullptr;   // per-row products (scratch)
+    int64_t fpart = 0;                // products per part
+    int32_t pmax = 0;                 // parts per row at most
+    int32_t max_slots = 0;            // split rows at most
+    int32_t *nslots = nullptr;        // device counter
+    int32_t *slot_of = nullptr, *row_of_slot = nullptr, *parts = nullptr, *task_start = nullptr;
+    unsigned long long *G = nullptr;
+    uint32_t *Gbits = nullptr;
+    void *split_mem = nullptr;
+    int64_t split_bytes = 0;
 };
+
+// Rows with fewer products than this are never split.
+constexpr int64_t kSplitMinFlops = 1 << 20;
+
+// A rows with more entries than this are analysed by the whole grid.
+constexpr int64_t kLongAnalyze = 16384;
 
 template <typename V, bool NUMERIC>
 int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevCsr &C, const int32_t *lists,
@@ -1356,9 +1677,36 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                         DevCsr T = C;
                         T.col = temp->col;
                         T.val = temp->val;
+                        if (temp->split) {
+                            k_split_select<<<grid_for(h, n, 256, 8), 256, 0, s>>>(
+                                list, n, temp->flops, temp->fpart, temp->pmax, temp->slot_of, temp->row_of_slot,
+                                temp->parts, temp->nslots, temp->max_slots);
+                            k_split_tasks<<<1, 1024, 0, s>>>(temp->parts, temp->nslots, temp->max_slots,
+                                                              temp->task_start);
+                            h->launches += 2;
+                        }
+                        if (temp->split) {
+                            // the split rows run on the second stream, beside the dense bin
+                            auto ks = k_dense_split<V>;
+                            RMCM_TRY(set_smem(h, ks, sm));
+                            RMCM_CUDA(h, cudaEventRecord(h->ev_fork, s));
+                            RMCM_CUDA(h, cudaStreamWaitEvent(h->aux, h->ev_fork, 0));
+                            k_dense_split<V><<<(int)((int64_t)h->sm_count * per_sm), kSplitThreads, sm, h->aux>>>(
+                                A, B, list, temp->row_of_slot, temp->parts, temp->task_start, temp->nslots,
+                                temp->max_slots, (int32_t)W, temp->G, temp->Gbits, bin_of, st);
+                            k_split_finish<V><<<temp->max_slots, kSplitThreads, 0, h->aux>>>(
+                                T, list, temp->row_of_slot, temp->nslots, temp->max_slots, ncols, (int32_t)W,
+                                temp->G, temp->Gbits, temp->stride, cnt, st);
+                            h->launches += 2;
+                        }
                         kern<<<grid, kDenseThreads, sm, s>>>(A, B, T, list, n, cnt, nullptr, 0, (int32_t)W, st,
                                                              temp->stride, bin_of, positive, b_distinct,
-                                                             h->abort_on_certain_overflow);
+                                                             h->abort_on_certain_overflow,
+                                                             temp->split ? temp->slot_of : nullptr);
+                        if (temp->split) {
+                            RMCM_CUDA(h, cudaEventRecord(h->ev_join, h->aux));
+                            RMCM_CUDA(h, cudaStreamWaitEvent(s, h->ev_join, 0));
+                        }
                     } else {
                         const int grid = (int)std::min<int64_t>((int64_t)n, (int64_t)h->sm_count * 8);
                         k_copy_rows<V><<<grid, 256, 0, s>>>(list, n, C, temp->col, (const V *)temp->val,
@@ -1380,7 +1728,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                     grid = (int)std::max<int64_t>(1, cursor_cap / stride);
                 }
                 kern<<<grid, kDenseThreads, sm, s>>>(A, B, C, list, n, cnt, cursor_base, stride, (int32_t)W, st, 0, bin_of,
-                                                     positive, b_distinct, h->abort_on_certain_overflow);
+                                                     positive, b_distinct, h->abort_on_certain_overflow, nullptr);
                 break;
             }
         }
@@ -1390,11 +1738,12 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
     return RMCM_OK;
 }
 
-int32_t scan_rowptr(rmcm_handle *h, const int64_t *cnt, int64_t m, int64_t *rowptr, int64_t *tile_sum) {
+int32_t scan_rowptr(rmcm_handle *h, const int64_t *cnt, int64_t m, int64_t *rowptr, int64_t *tile_sum,
+                    unsigned long long *row_max) {
     cudaStream_t s = h->stream;
     const int64_t ntiles = std::max<int64_t>(1, (m + kScanTile - 1) / kScanTile);
     if (m > 0) {
-        k_scan_tiles<<<(unsigned)ntiles, kScanThreads, 0, s>>>(cnt, m, rowptr, tile_sum);
+        k_scan_tiles<<<(unsigned)ntiles, kScanThreads, 0, s>>>(cnt, m, rowptr, tile_sum, row_max);
         h->launches++;
     } else {
         RMCM_CUDA(h, cudaMemsetAsync(tile_sum, 0, sizeof(int64_t), s));
@@ -1453,8 +1802,9 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     int64_t *tiles = (int64_t *)(sc + o_tiles);
     uint8_t *bin_of = (uint8_t *)(sc + o_bin);
     int32_t *lists = (int32_t *)(sc + o_lists);
-    // small: [0..4] bin counts, [8..12] bin cursors, [16] longest dense A row,
-    // [32..33] total flops (u64), [40] overflow certain, [48..51] profiling sums
+    // small: [0..6] bin counts, [8..14] bin cursors, [16] longest dense A row,
+    // [32..33] total flops (u64), [36..37] largest dense-row flops (u64),
+    // [40] overflow certain, [42] split slots, [48..51] profiling sums
     int32_t *small = (int32_t *)(sc + o_small);
     RMCM_CUDA(h, cudaMemsetAsync(small, 0, 256, s));
 
@@ -1467,6 +1817,8 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         for (auto &e : rec->ev) RMCM_CUDA(h, cudaEventCreate(&e));
         RMCM_CUDA(h, cudaEventRecord(rec->ev[0], s));
     }
+    void *long_mem = nullptr;
+    int64_t long_bytes = 0;
     BinParams bp;
     bp.dense_win = sizeof(V) == 4 ? kDenseWinU32 : kDenseWinU64;
     bp.hash_max = h->tune.hash_max_flops;
@@ -1478,11 +1830,36 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         bp.inv_load_q8 = (int32_t)std::ceil(256.0 / h->tune.hash_load);
     }
     if (m > 0) {
-        k_analyze<V><<<grid_for(h, m * 32, 256, 8), 256, 0, s>>>(A, B, bp, flops, bin_of, small, small + 16,
-                                                                  (unsigned long long *)(small + 32), small + 40);
+        AnalyzeOut ao{flops, bin_of, small, small + 16, (unsigned long long *)(small + 32), small + 40,
+                      (unsigned long long *)(small + 36)};
+        // rows longer than kLongAnalyze entries: walked by the whole grid
+        const bool long_rows = Am->max_row > kLongAnalyze;
+        const int64_t max_long = A.nnz / kLongAnalyze + 1;
+        if (long_rows) {
+            long_bytes = 24 * max_long + 256;
+            RMCM_TRY(dev_alloc(h, (void **)&long_mem, long_bytes));
+            RMCM_CUDA(h, cudaMemsetAsync(long_mem, 0, long_bytes, s));
+        }
+        int32_t *nlong = small + 43;
+        unsigned long long *acc_f = long_rows ? (unsigned long long *)long_mem : nullptr;
+        unsigned long long *acc_s = long_rows ? acc_f + max_long : nullptr;
+        int32_t *lsat = long_rows ? (int32_t *)(acc_s + max_long) : nullptr;
+        int32_t *llist = long_rows ? lsat + max_long : nullptr;
+        k_analyze<V><<<grid_for(h, m * 32, 256, 8), 256, 0, s>>>(A, B, bp, ao, long_rows ? kLongAnalyze : INT64_MAX,
+                                                                  llist, nlong);
+        h->launches++;
+        if (long_rows) {
+            k_analyze_long<V><<<h->sm_count * 4, 256, 0, s>>>(A, B, llist, nlong, acc_f, acc_s, lsat);
+            k_analyze_long_finish<V><<<4, 256, 0, s>>>(A, B, bp, ao, llist, nlong, acc_f, acc_s, lsat);
+            h->launches += 2;
+        }
         k_scatter<<<grid_for(h, m, 256, 8), 256, 0, s>>>(m, bin_of, small, small + 8, lists);
         k_zero_counts<<<grid_for(h, m, 256, 8), 256, 0, s>>>(m, bin_of, cnt);
-        h->launches += 3;
+        h->launches += 2;
+        if (long_mem) {
+            dev_free(h, long_mem, long_bytes);
+            long_mem = nullptr;
+        }
         RMCM_CUDA(h, cudaGetLastError());
     }
     if (rec) RMCM_CUDA(h, cudaEventRecord(h->prof[rec_idx].ev[1], s));
@@ -1557,9 +1934,57 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     if (replay && plan->dense_temp && !dtemp.active)
         return set_error(h, RMCM_ENOMEM, "replay: dense temporary could not be allocated");
     if (record) plan->dense_temp = dtemp.active;
+    // Dense rows with far more products than a fair share of the device are
+    // split over several CTAs (k_dense_split).
+    int64_t max_dense_f = 0;
+    if (replay) max_dense_f = plan->max_dense_flops;
+    else memcpy(&max_dense_f, (int32_t *)h->h_pinned + 36, sizeof(int64_t));
+    if (record) plan->max_dense_flops = max_dense_f;
+    if (dtemp.active) {
+        const int64_t fpart = std::max<int64_t>(kSplitMinFlops, flops_total / ((int64_t)h->sm_count * 4));
+        if (max_dense_f > fpart) {
+            const int32_t nd = counts[kBinDense];
+            const int32_t max_slots = (int32_t)std::min<int64_t>(std::min<int64_t>(1024, nd), flops_total / fpart + 1);
+            const int64_t Wt = (B.cols + 31) / 32 * 32;
+            auto al = [](int64_t x) { return (x + 255) & ~255LL; };
+            const int64_t o_slot = 0;
+            const int64_t o_row = o_slot + al(4LL * nd);
+            const int64_t o_parts = o_row + al(4LL * max_slots);
+            const int64_t o_ts = o_parts + al(4LL * max_slots);
+            const int64_t o_g = o_ts + al(4LL * (max_slots + 1));
+            const int64_t o_gb = o_g + al(8LL * max_slots * Wt);
+            const int64_t total = o_gb + al(4LL * max_slots * (Wt / 32));
+            void *mem = nullptr;
+            if (dev_alloc(h, &mem, total) == RMCM_OK) {
+                char *b = (char *)mem;
+                dtemp.split = true;
+                dtemp.flops = flops;
+                dtemp.fpart = fpart;
+                dtemp.pmax = h->sm_count * 2;
+                dtemp.max_slots = max_slots;
+                dtemp.nslots = small + 42;
+                dtemp.slot_of = (int32_t *)(b + o_slot);
+                dtemp.row_of_slot = (int32_t *)(b + o_row);
+                dtemp.parts = (int32_t *)(b + o_parts);
+                dtemp.task_start = (int32_t *)(b + o_ts);
+                dtemp.G = (unsigned long long *)(b + o_g);
+                dtemp.Gbits = (uint32_t *)(b + o_gb);
+                dtemp.split_mem = mem;
+                dtemp.split_bytes = total;
+                RMCM_CUDA(h, cudaMemsetAsync(b + o_g, 0, total - o_g, s));
+            } else {
+                h->last_error.clear();
+            }
+        }
+    }
+    if (replay && plan->split && !dtemp.split)
+        return set_error(h, RMCM_ENOMEM, "replay: split-row buffers could not be allocated");
+    if (record) plan->split = dtemp.split;
     auto drop_temp = [&]() {
         if (dtemp.active) dev_free(h, dtemp.col, dtemp.bytes);
+        if (dtemp.split) dev_free(h, dtemp.split_mem, dtemp.split_bytes);
         dtemp.active = false;
+        dtemp.split = false;
     };
 
     // symbolic
@@ -1572,12 +1997,13 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     }
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[2], s);
     rc = launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap, &dtemp, bin_of, positive, Bm->distinct);
-    if (rc == RMCM_OK) rc = scan_rowptr(h, cnt, m, C->d.rowptr, tiles);
+    if (rc == RMCM_OK) rc = scan_rowptr(h, cnt, m, C->d.rowptr, tiles, (unsigned long long *)(small + 44));
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[3], s);
     // nnz to the host, then the output arrays
     int64_t *hp = h->h_pinned;
     if (rc == RMCM_OK && !replay) {
         cudaError_t e = cudaMemcpyAsync(hp, C->d.rowptr + m, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hp + 1, small + 44, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) rc = cuda_error(h, e, "spgemm nnz download");
     }
@@ -1588,7 +2014,11 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         if (cudaGetLastError() != cudaSuccess) rc = set_error(h, RMCM_ECUDA, "replay nnz check launch");
     }
     const int64_t nnz = replay ? plan->nnz : hp[0];
-    if (record) plan->nnz = nnz;
+    const int64_t c_max_row = replay ? plan->c_max_row : hp[1];
+    if (record) {
+        plan->nnz = nnz;
+        plan->c_max_row = c_max_row;
+    }
     if (rc == RMCM_OK && h->abort_on_certain_overflow && !replay) {
         // single-pass dense rows already computed their counts: stop early if
         // any of them overflowed, so the caller can recompute in uint64
@@ -1664,6 +2094,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     }
     C->positive = positive;
     C->distinct = true;
+    C->max_row = c_max_row;
     *Cout = C;
     return RMCM_OK;
 }
@@ -1702,6 +2133,7 @@ int32_t convert_values(rmcm_handle *h, const rmcm_mat *src, int32_t valtype, rmc
     m->ones = src->ones;
     m->positive = src->positive;
     m->distinct = src->distinct;
+    m->max_row = src->max_row;
     *out = m;
     return RMCM_OK;
 }

@@ -383,3 +383,64 @@ def test_cli_flags(native, tmp_path):
     assert (rows, cols) == (3, 3) and int(rp[-1]) == 7 and set(val.tolist()) <= {1, 2}
     cnt = (cnt_dir / "1-3-0-0-1.cnt").read_text().split()
     assert cnt == ["4", "3", "5", "2", "6", "2"]        # global author ids 4..6 and their row sizes
+
+
+def test_heavy_dense_rows_are_split_over_ctas(native, engine):
+    """One row with ~4.7M products (above the split threshold) among light
+    rows: the heavy row goes through the split kernels, the rest through the
+    dense bin; both must match scipy, in uint32 and uint64."""
+    rng = np.random.default_rng(31)
+    m, k, n = 40, 3000, 1800
+    a_nnz = rng.integers(1, 30, m)
+    a_nnz[7] = k                         # the heavy row: every B row
+    A = _random_csr(rng, m, k, a_nnz, vmax=3)
+    B = _random_csr(rng, k, n, rng.integers(1500, 1800, k), vmax=3)
+    for vt in (native.VAL_U32, native.VAL_U64):
+        eng = native.Engine(device=0)
+        eng.set_profiling(1)
+        _check_product(native, eng, A, B, vt)
+        st = eng.product_stats()[0]
+        assert st["flops"] > (1 << 22) and st["bin_rows"][4] > 0
+        eng.close()
+
+
+def test_split_rows_replay_in_a_batch(native):
+    """A star-shaped relation gives one vertex millions of two-step paths; the
+    batch replays its split product exactly."""
+    rng = np.random.default_rng(32)
+    n0, n1, n2 = 4, 2600, 1800
+    src01 = np.concatenate([np.zeros(n1, np.int64), rng.integers(1, n0, 50)])
+    dst01 = np.concatenate([np.arange(n1), rng.integers(0, n1, 50)])
+    deg = rng.integers(1700, 1790, n1)
+    src12 = np.repeat(np.arange(n1), deg)
+    dst12 = np.concatenate([rng.choice(n2, d, replace=False) for d in deg])
+    src01, dst01 = synth.dedup_pairs_keep_order(src01, dst01, n1)
+    g = synth.SyntheticHIN("star", [n0, n1, n2], [synth.Relation(0, 1, 0, 1, src01, dst01),
+                                                  synth.Relation(1, 2, 2, 3, src12, dst12)])
+    eng = native.Engine(device=0)
+    hg = native.HeteroGraph.from_synthetic(eng, g)
+    paths = ["0-0-1-2-2", "0-0-1-2-2-3-1", "2-3-1-1-0-0-1-2-2"]
+    plain = []
+    for mp in paths:
+        C, _, rc = eng.run_metapath(hg, mp)
+        plain.append(eng.digest(C))
+        C.free()
+    b = eng.batch(hg, paths, lanes=2)
+    for _ in range(2):
+        nnz, dig, _ = b.run()
+        assert [(int(a), int(x)) for a, x in zip(nnz, dig)] == plain
+    b.free()
+    hg.close()
+    eng.close()
+
+
+def test_long_rows_are_analysed_by_the_whole_grid(native, engine):
+    """A rows longer than the per-warp analysis limit (16384 entries): their
+    products and count bounds come from grid-wide partial sums."""
+    rng = np.random.default_rng(33)
+    m, k, n = 6, 60000, 700
+    a_nnz = np.array([3, 40000, 10, 20000, 0, 5])
+    A = _random_csr(rng, m, k, a_nnz, vmax=4)
+    B = _random_csr(rng, k, n, rng.integers(0, 6, k), vmax=4)
+    for vt in (native.VAL_U32, native.VAL_U64):
+        _check_product(native, engine, A, B, vt)
