@@ -25,6 +25,10 @@ SpGEMM chain) over all four chains, results computed in full and freed.
   the retail graph) at two offered rates, the plain one-query-at-a-time path
   versus the query server; queries/s, p50 and p99 latency of both and
   whether every result (nnz + digest) matches.
+* stress: the twelve-matrix uint64 chain over the X/Y/Z graph at x0.1 vertex
+  and edge counts (intermediates of ~1e9 entries); time, multiply-adds per
+  second, peak device bytes, and the largest estimated intermediate of the
+  RES order versus left to right.
 
 --impl reference times that CPU implementation alone, as the reference arm.
 Multi-GPU (torchrun): every rank runs the full workload on its own GPU
@@ -68,6 +72,7 @@ def parse():
     ap.add_argument("--detail", action="store_true", help="per-product stats to stderr")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched (CUDA graph) section")
     ap.add_argument("--no-served", action="store_true", help="skip the served (query server) section")
+    ap.add_argument("--no-stress", action="store_true", help="skip the stress (12-matrix uint64 chain) section")
     return ap.parse_args()
 
 
@@ -292,6 +297,45 @@ def served_section(rg, eng, hg_retail, g_retail, rates=(100.0, 2000.0), queries=
     return out
 
 
+def stress_section(rg, device, scale=0.1):
+    """The twelve-matrix uint64 chain Z-Y-X-Y-X-Y-Z-Y-X-Y-X-Y-Z over the X/Y/Z
+    graph (both-side Zipf(1.6) X-Y degrees), vertex and edge counts x``scale``:
+    one timed run after the leaves are built."""
+    from resmcm_ari_gb300 import workloads
+    g = workloads.stress_scaled(scale)
+    eng = rg.Engine(device=device, valtype=rg.VAL_U64)
+    hg = rg.HeteroGraph.from_synthetic(eng, g)
+    mp = workloads.STRESS_CHAIN
+    leaves = hg.leaves(mp, rg.VAL_U64)
+    c = eng.estimate(leaves)
+    split, _, _ = eng.order(c)
+    L = c.shape[0]
+    inter = []
+
+    def walk(i, j):
+        if i != j:
+            k = int(split[i, j])
+            walk(i, k)
+            walk(k + 1, j)
+            inter.append(float(c[i, j]))
+
+    walk(0, L - 1)
+    eng.mem_peak(reset=True)
+    C, t, rc = eng.run_metapath(hg, mp, keep=True)
+    peak = eng.mem_peak()
+    out = {"workload": f"X=Y={g.type_sizes[0]}, Z={g.type_sizes[2]}, X-Y {g.relations[0].src.size} edges "
+                       f"(both-side Zipf 1.6), Y-Z 1-4 per Y; chain {mp} (12 matrices), uint64 with overflow check",
+           "scale": scale, "status": int(rc), "result_nnz": int(C.nnz), "seconds": t["total_s"],
+           "spgemm_s": t["spgemm_s"], "multiply_adds": int(t["flops"]),
+           "multiply_adds_per_s": t["flops"] / t["total_s"] if t["total_s"] else None,
+           "peak_device_bytes": int(peak),
+           "est_largest_intermediate_nnz": {"res_order": max(inter), "left_to_right": max(c[0, j] for j in range(1, L))}}
+    C.free()
+    hg.close()
+    eng.close()
+    return out
+
+
 def select(mps, spec):
     if spec == "all":
         return list(mps)
@@ -474,6 +518,9 @@ def main():
         batched = batched_section(rg, local)
     if rank == 0 and not args.no_served:
         served = served_section(rg, eng, hg, g)
+    stress = None
+    if rank == 0 and not args.no_stress:
+        stress = stress_section(rg, local)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -495,7 +542,7 @@ def main():
             "nnz_per_s": step_nnz * ws / (ms_per_step / 1e3),
             "result_nnz_per_step": step_nnz,
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
-            "batched": batched, "served": served,
+            "batched": batched, "served": served, "stress": stress,
         }
         print(json.dumps(line), flush=True)
     hg.close()

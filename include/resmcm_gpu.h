@@ -116,6 +116,9 @@ RMCM_API int32_t rmcm_set_stream(rmcm_handle *h, void *stream);
 RMCM_API void *rmcm_get_stream(const rmcm_handle *h);
 /* Bytes of device memory currently held by matrices and scratch. */
 RMCM_API int64_t rmcm_mem_in_use(const rmcm_handle *h);
+/* Largest rmcm_mem_in_use since the handle was created or the last reset
+ * (reset != 0 restarts it from the current use). */
+RMCM_API int64_t rmcm_mem_peak(rmcm_handle *h, int32_t reset);
 /* Number of kernels this handle has launched so far. */
 RMCM_API int64_t rmcm_kernel_launches(const rmcm_handle *h);
 /* Profiling of SpGEMM products: 0 off, 1 CUDA-event times, 2 times and

@@ -133,6 +133,7 @@ def lib():
         "rmcm_set_stream": ([vp, vp], i32),
         "rmcm_get_stream": ([vp], vp),
         "rmcm_mem_in_use": ([vp], i64),
+        "rmcm_mem_peak": ([vp, i32], i64),
         "rmcm_kernel_launches": ([vp], i64),
         "rmcm_set_profiling": ([vp, i32], i32),
         "rmcm_get_product_stats": ([vp, C.POINTER(ProductStats), i32, C.POINTER(i32), i32], i32),
@@ -534,6 +535,10 @@ class Engine:
     @property
     def mem_in_use(self) -> int:
         return lib().rmcm_mem_in_use(self._h)
+
+    def mem_peak(self, reset: bool = False) -> int:
+        """High-water mark of device bytes in use (rmcm_mem_peak)."""
+        return lib().rmcm_mem_peak(self._h, 1 if reset else 0)
 
     @property
     def kernel_launches(self) -> int:

@@ -52,6 +52,7 @@ int32_t dev_alloc(rmcm_handle *h, void **p, int64_t bytes) {
         return cuda_error(h, e, "cudaMallocAsync");
     }
     h->in_use += bytes;
+    if (h->in_use > h->peak) h->peak = h->in_use;
     return RMCM_OK;
 }
 
@@ -1049,6 +1050,12 @@ RMCM_API int32_t rmcm_set_stream(rmcm_handle *h, void *stream) {
 
 RMCM_API void *rmcm_get_stream(const rmcm_handle *h) { return h ? (void *)h->stream : nullptr; }
 RMCM_API int64_t rmcm_mem_in_use(const rmcm_handle *h) { return h ? h->in_use : 0; }
+RMCM_API int64_t rmcm_mem_peak(rmcm_handle *h, int32_t reset) {
+    if (!h) return 0;
+    const int64_t p = h->peak;
+    if (reset) h->peak = h->in_use;
+    return p;
+}
 RMCM_API int64_t rmcm_kernel_launches(const rmcm_handle *h) { return h ? h->launches : 0; }
 
 RMCM_API int32_t rmcm_set_profiling(rmcm_handle *h, int32_t level) {

@@ -104,6 +104,7 @@ struct rmcm_handle {
     int32_t valtype = RMCM_VAL_AUTO;
     int64_t budget = 0;
     int64_t in_use = 0;
+    int64_t peak = 0;               // high-water mark of in_use since the last reset
     int64_t launches = 0;
     int sm_count = 0;
     std::string last_error;

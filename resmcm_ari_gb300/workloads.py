@@ -6,8 +6,9 @@
                          meta-paths of 2-10 matrices, filtered by the RES estimate
 * ``poisson_queries``    a seeded Poisson arrival stream of meta-path queries
                          over two resident graphs (served)
-* ``stress_chain``       X/Y/Z graph with both-side Zipf(1.6) degrees and a
-                         12-matrix chain in uint64 (memory bound)
+* ``stress_graph``       X/Y/Z graph with both-side Zipf(1.6) degrees; its
+                         12-matrix chain ``STRESS_CHAIN`` runs in uint64
+                         (memory bound)
 
 The published datasets of the reference's paper are not redistributable, so
 these synthetic graphs stand in for them with the configured sizes, degree
@@ -112,3 +113,14 @@ def stress_graph(seed: int = 4, n_x: int = 5_000_000, n_y: int = 5_000_000, n_z:
     g = synth.SyntheticHIN(f"stress_s{seed}", [n_x, n_y, n_z])
     g.relations = [synth.Relation(0, 1, 0, 1, src, dst), synth.Relation(1, 2, 2, 3, ysrc, zdst)]
     return g
+
+
+# Z-Y-X-Y-X-Y-Z-Y-X-Y-X-Y-Z over the stress graph (X=0, Y=1, Z=2; edge types
+# X->Y 0, Y->X 1, Y->Z 2, Z->Y 3): twelve matrices, a Z x Z result.
+STRESS_CHAIN = "2-3-1-1-0-0-1-1-0-0-1-2-2-3-1-1-0-0-1-1-0-0-1-2-2"
+
+
+def stress_scaled(scale: float, seed: int = 4) -> synth.SyntheticHIN:
+    """The stress graph with every vertex and edge count multiplied by ``scale``."""
+    return stress_graph(seed=seed, n_x=max(2, int(5_000_000 * scale)), n_y=max(2, int(5_000_000 * scale)),
+                        n_z=max(2, int(100_000 * scale)), xy_edges=max(1, int(60_000_000 * scale)))
