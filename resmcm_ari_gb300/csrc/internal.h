@@ -80,6 +80,7 @@ struct ProductPlan {
     int64_t max_dense_flops = 0;
     int64_t c_max_row = -1;
     bool split = false;
+    int32_t n_front = 0;
     int64_t scratch_bytes = 0;
 };
 

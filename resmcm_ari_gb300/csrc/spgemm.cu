@@ -877,11 +877,11 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
 // stride `tstride` entries) and its length goes to cnt[r]; the symbolic pass
 // is skipped for these rows and k_copy_rows compacts the slots into C.
 template <typename V, bool NUMERIC, bool TEMP>
-__global__ void __launch_bounds__(kDenseThreads, sizeof(V) == 4 ? 3 : 1) k_dense(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows,
+__global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows,
                                                          int32_t nrows, int64_t *cnt, int32_t *cursors,
                                                          int64_t cur_stride, int32_t W, int *st, int64_t tstride,
                                                          const uint8_t *bin_of, bool positive, bool b_distinct,
-                                                         bool abort_mode, const int32_t *skip) {
+                                                         bool abort_mode) {
     constexpr int NT = kDenseThreads;
     constexpr int kPull = 4;   // register accumulators per thread: windows of up to 4 * NT columns
     static_assert(kChunk == NT, "the dense kernel stages one A entry per thread");
@@ -913,7 +913,6 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(V) == 4 ? 3 : 1) k_dense
             __syncthreads();
             if (s_abort) break;
         }
-        if (skip && skip[ri] >= 0) continue;   // a split row: written by the split kernels
         const int32_t r = rows[ri];
         const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
         // A row that cannot overflow needs no checks, and when every input
@@ -1126,23 +1125,27 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(V) == 4 ? 3 : 1) k_dense
 
 constexpr int kSplitThreads = 512;
 
-// Per dense-list row: number of parts (>= 2 only above fpart) and a slot.
+// Per dense-list row: split rows (products above fpart, at most max_slots of
+// them) go to the back of the permuted list `perm` with a slot and a number
+// of parts, the other rows to the front; k_dense then runs over the front.
 __global__ void k_split_select(const int32_t *rows, int32_t n, const int64_t *flops, int64_t fpart, int32_t pmax,
-                               int32_t *slot_of, int32_t *row_of_slot, int32_t *parts, int32_t *nslots,
+                               int32_t *perm, int32_t *front, int32_t *nslots, int32_t *row_of_slot, int32_t *parts,
                                int32_t max_slots) {
     for (int64_t ri = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; ri < n; ri += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t f = flops[rows[ri]];
-        int32_t slot = -1;
+        const int32_t r = rows[ri];
+        const int64_t f = flops[r];
+        bool split = false;
         if (f > fpart) {
-            const int64_t p = min((int64_t)pmax, (f + fpart - 1) / fpart);
             const int32_t s_ = atomicAdd(nslots, 1);
             if (s_ < max_slots) {
-                slot = s_;
-                row_of_slot[s_] = (int32_t)ri;
-                parts[s_] = (int32_t)p;
+                const int32_t pos = n - 1 - s_;
+                perm[pos] = r;
+                row_of_slot[s_] = pos;
+                parts[s_] = (int32_t)min((int64_t)pmax, (f + fpart - 1) / fpart);
+                split = true;
             }
         }
-        slot_of[ri] = slot;
+        if (!split) perm[atomicAdd(front, 1)] = r;
     }
 }
 
@@ -1585,7 +1588,10 @@ struct DenseTemp {
     int32_t pmax = 0;                 // parts per row at most
     int32_t max_slots = 0;            // split rows at most
     int32_t *nslots = nullptr;        // device counter
-    int32_t *slot_of = nullptr, *row_of_slot = nullptr, *parts = nullptr, *task_start = nullptr;
+    int32_t *front = nullptr;         // device counter: rows of the dense list not split
+    int32_t n_front = 0;              // its value on the host
+    int32_t *perm = nullptr;          // dense list, unsplit rows first
+    int32_t *row_of_slot = nullptr, *parts = nullptr, *task_start = nullptr;
     unsigned long long *G = nullptr;
     uint32_t *Gbits = nullptr;
     void *split_mem = nullptr;
@@ -1678,39 +1684,35 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                         T.col = temp->col;
                         T.val = temp->val;
                         if (temp->split) {
-                            k_split_select<<<grid_for(h, n, 256, 8), 256, 0, s>>>(
-                                list, n, temp->flops, temp->fpart, temp->pmax, temp->slot_of, temp->row_of_slot,
-                                temp->parts, temp->nslots, temp->max_slots);
-                            k_split_tasks<<<1, 1024, 0, s>>>(temp->parts, temp->nslots, temp->max_slots,
-                                                              temp->task_start);
-                            h->launches += 2;
-                        }
-                        if (temp->split) {
                             // the split rows run on the second stream, beside the dense bin
                             auto ks = k_dense_split<V>;
                             RMCM_TRY(set_smem(h, ks, sm));
                             RMCM_CUDA(h, cudaEventRecord(h->ev_fork, s));
                             RMCM_CUDA(h, cudaStreamWaitEvent(h->aux, h->ev_fork, 0));
                             k_dense_split<V><<<(int)((int64_t)h->sm_count * per_sm), kSplitThreads, sm, h->aux>>>(
-                                A, B, list, temp->row_of_slot, temp->parts, temp->task_start, temp->nslots,
+                                A, B, temp->perm, temp->row_of_slot, temp->parts, temp->task_start, temp->nslots,
                                 temp->max_slots, (int32_t)W, temp->G, temp->Gbits, bin_of, st);
                             k_split_finish<V><<<temp->max_slots, kSplitThreads, 0, h->aux>>>(
-                                T, list, temp->row_of_slot, temp->nslots, temp->max_slots, ncols, (int32_t)W,
+                                T, temp->perm, temp->row_of_slot, temp->nslots, temp->max_slots, ncols, (int32_t)W,
                                 temp->G, temp->Gbits, temp->stride, cnt, st);
                             h->launches += 2;
                         }
-                        kern<<<grid, kDenseThreads, sm, s>>>(A, B, T, list, n, cnt, nullptr, 0, (int32_t)W, st,
-                                                             temp->stride, bin_of, positive, b_distinct,
-                                                             h->abort_on_certain_overflow,
-                                                             temp->split ? temp->slot_of : nullptr);
+                        // split rows sit at the back of the permuted list: the dense
+                        // kernel takes its front
+                        const int32_t *dl = temp->split ? temp->perm : list;
+                        const int32_t dn = temp->split ? temp->n_front : n;
+                        if (dn > 0)
+                            kern<<<std::max(1, std::min(grid, dn)), kDenseThreads, sm, s>>>(
+                                A, B, T, dl, dn, cnt, nullptr, 0, (int32_t)W, st, temp->stride, bin_of, positive,
+                                b_distinct, h->abort_on_certain_overflow);
                         if (temp->split) {
                             RMCM_CUDA(h, cudaEventRecord(h->ev_join, h->aux));
                             RMCM_CUDA(h, cudaStreamWaitEvent(s, h->ev_join, 0));
                         }
                     } else {
                         const int grid = (int)std::min<int64_t>((int64_t)n, (int64_t)h->sm_count * 8);
-                        k_copy_rows<V><<<grid, 256, 0, s>>>(list, n, C, temp->col, (const V *)temp->val,
-                                                             temp->stride);
+                        k_copy_rows<V><<<grid, 256, 0, s>>>(temp->split ? temp->perm : list, n, C, temp->col,
+                                                             (const V *)temp->val, temp->stride);
                     }
                     break;
                 }
@@ -1728,7 +1730,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                     grid = (int)std::max<int64_t>(1, cursor_cap / stride);
                 }
                 kern<<<grid, kDenseThreads, sm, s>>>(A, B, C, list, n, cnt, cursor_base, stride, (int32_t)W, st, 0, bin_of,
-                                                     positive, b_distinct, h->abort_on_certain_overflow, nullptr);
+                                                     positive, b_distinct, h->abort_on_certain_overflow);
                 break;
             }
         }
@@ -1947,8 +1949,8 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
             const int32_t max_slots = (int32_t)std::min<int64_t>(std::min<int64_t>(1024, nd), flops_total / fpart + 1);
             const int64_t Wt = (B.cols + 31) / 32 * 32;
             auto al = [](int64_t x) { return (x + 255) & ~255LL; };
-            const int64_t o_slot = 0;
-            const int64_t o_row = o_slot + al(4LL * nd);
+            const int64_t o_perm = 0;
+            const int64_t o_row = o_perm + al(4LL * nd);
             const int64_t o_parts = o_row + al(4LL * max_slots);
             const int64_t o_ts = o_parts + al(4LL * max_slots);
             const int64_t o_g = o_ts + al(4LL * (max_slots + 1));
@@ -1963,7 +1965,8 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
                 dtemp.pmax = h->sm_count * 2;
                 dtemp.max_slots = max_slots;
                 dtemp.nslots = small + 42;
-                dtemp.slot_of = (int32_t *)(b + o_slot);
+                dtemp.front = small + 46;
+                dtemp.perm = (int32_t *)(b + o_perm);
                 dtemp.row_of_slot = (int32_t *)(b + o_row);
                 dtemp.parts = (int32_t *)(b + o_parts);
                 dtemp.task_start = (int32_t *)(b + o_ts);
@@ -1980,6 +1983,26 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     if (replay && plan->split && !dtemp.split)
         return set_error(h, RMCM_ENOMEM, "replay: split-row buffers could not be allocated");
     if (record) plan->split = dtemp.split;
+    if (dtemp.split) {
+        // choose the split rows now: the dense kernel needs the count of the others
+        int32_t dense_off = 0;
+        for (int b = 0; b < kBinDense; b++) dense_off += counts[b];
+        const int32_t nd = counts[kBinDense];
+        k_split_select<<<grid_for(h, nd, 256, 8), 256, 0, s>>>(lists + dense_off, nd, flops, dtemp.fpart, dtemp.pmax,
+                                                               dtemp.perm, dtemp.front, dtemp.nslots,
+                                                               dtemp.row_of_slot, dtemp.parts, dtemp.max_slots);
+        k_split_tasks<<<1, 1024, 0, s>>>(dtemp.parts, dtemp.nslots, dtemp.max_slots, dtemp.task_start);
+        h->launches += 2;
+        RMCM_CUDA(h, cudaGetLastError());
+        if (replay) {
+            dtemp.n_front = plan->n_front;
+        } else {
+            RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned + 2, dtemp.front, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            RMCM_CUDA(h, cudaStreamSynchronize(s));
+            dtemp.n_front = ((int32_t *)(h->h_pinned + 2))[0];
+        }
+        if (record) plan->n_front = dtemp.n_front;
+    }
     auto drop_temp = [&]() {
         if (dtemp.active) dev_free(h, dtemp.col, dtemp.bytes);
         if (dtemp.split) dev_free(h, dtemp.split_mem, dtemp.split_bytes);
