@@ -119,6 +119,7 @@ int32_t mat_alloc(rmcm_handle *h, int64_t rows, int64_t cols, int64_t nnz, int32
 void mat_release(rmcm_handle *h, rmcm_mat *m) {
     if (!m) return;
     if (m->rowsum) dev_free(h, m->rowsum, 8 * m->d.rows);
+    if (m->est_long) dev_free(h, m->est_long, 4 * (int64_t)m->n_est_long);
     dev_free(h, m->d.rowptr, 8 * (m->d.rows + 1));
     if (m->d.col) dev_free(h, m->d.col, 4 * m->d.nnz);
     if (m->d.val) dev_free(h, m->d.val, val_bytes(m->valtype) * m->d.nnz);
@@ -329,8 +330,25 @@ int32_t upload_csr(rmcm_handle *h, int64_t rows, int64_t cols, const int64_t *ro
     }
     {
         int64_t mx = 0;
-        for (int64_t r = 0; r < rows; r++) mx = std::max<int64_t>(mx, rowptr[r + 1] - rowptr[r]);
+        std::vector<int32_t> lng;
+        for (int64_t r = 0; r < rows; r++) {
+            const int64_t len = rowptr[r + 1] - rowptr[r];
+            mx = std::max<int64_t>(mx, len);
+            if (len > kEstLongRow) lng.push_back((int32_t)r);
+        }
         m->max_row = mx;
+        m->n_est_long = (int32_t)lng.size();
+        if (!lng.empty()) {
+            int32_t rc = dev_alloc(h, (void **)&m->est_long, 4 * (int64_t)lng.size());
+            if (rc == RMCM_OK) {
+                e = cudaMemcpyAsync(m->est_long, lng.data(), 4 * lng.size(), cudaMemcpyHostToDevice, s);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            }
+            if (rc != RMCM_OK || e != cudaSuccess) {
+                mat_release(h, m);
+                return rc != RMCM_OK ? rc : cuda_error(h, e, "upload");
+            }
+        }
     }
     if (!val) {
         int32_t rc = fill_ones(h, m->d.val, nnz, valtype);

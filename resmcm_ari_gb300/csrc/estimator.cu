@@ -46,7 +46,7 @@ struct LevelArgs {
 };
 
 __global__ void __launch_bounds__(kEstThreads) k_res_level(DevCsr M, const double *r_next, double *r_cur,
-                                                           LevelArgs la, double *partial) {
+                                                           LevelArgs la, double *partial, bool skip_long) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int G = 32 / la.jp;
     const int g = lane / la.jp;
@@ -63,6 +63,7 @@ __global__ void __launch_bounds__(kEstThreads) k_res_level(DevCsr M, const doubl
             r_cur[u * la.len + la.i] = s > 1.0 ? 1.0 : s;
         }
         if (la.nj == 0) continue;
+        if (skip_long && a1 - a0 > kEstLongRow) continue;   // a CTA of k_res_long takes it
         double prod = 1.0;
         if (active_j) {
             for (int64_t k = a0 + g; k < a1; k += G) {
@@ -90,6 +91,50 @@ __global__ void __launch_bounds__(kEstThreads) k_res_level(DevCsr M, const doubl
         double acc = 0.0;
         for (int w = 0; w < kEstThreads / 32; w++) acc = __dadd_rn(acc, s_part[w][threadIdx.x]);
         partial[(int64_t)blockIdx.x * kMaxLen + threadIdx.x] = acc;
+    }
+}
+
+// A CTA per long row (rows listed ascending): warp w multiplies the factors
+// of the w-th of 32 equal slices of the row, grouped as in k_res_level, and
+// the 32 warp products are combined in warp order.  The row's terms
+// s * dim_j go to partial[block], after the partials of k_res_level, so the
+// reduction still adds them in a fixed order.
+constexpr int kEstLongThreads = 1024;
+
+__global__ void __launch_bounds__(kEstLongThreads) k_res_long(DevCsr M, const double *r_next, double *r_cur,
+                                                              LevelArgs la, const int32_t *long_rows,
+                                                              double *partial) {
+    __shared__ double s_prod[kEstLongThreads / 32][kMaxLen];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int G = 32 / la.jp;
+    const int g = lane / la.jp;
+    const int jo = lane % la.jp;
+    const bool active_j = jo < la.nj && g < G;
+    const int j = la.i + 1 + jo;
+    const int64_t u = long_rows[blockIdx.x];
+    const int64_t a0 = M.rowptr[u], len = M.rowptr[u + 1] - a0;
+    const int64_t k0 = a0 + len * warp / (kEstLongThreads / 32), k1 = a0 + len * (warp + 1) / (kEstLongThreads / 32);
+    double prod = 1.0;
+    if (active_j) {
+        for (int64_t k = k0 + g; k < k1; k += G) {
+            const int32_t v = M.col[k];
+            const double rv = r_next[(int64_t)v * la.len + j];
+            prod = __dmul_rn(prod, __dsub_rn(1.0, rv));
+        }
+    }
+    for (int d = la.jp; d < 32; d <<= 1) {
+        const double o = __shfl_xor_sync(kFull, prod, d);
+        prod = __dmul_rn(prod, o);
+    }
+    if (g == 0 && active_j) s_prod[warp][jo] = prod;
+    __syncthreads();
+    if ((int)threadIdx.x < la.nj) {
+        double p = 1.0;
+        for (int w = 0; w < kEstLongThreads / 32; w++) p = __dmul_rn(p, s_prod[w][threadIdx.x]);
+        const int jj = la.i + 1 + threadIdx.x;
+        const double sv = __dsub_rn(1.0, p);
+        r_cur[u * la.len + jj] = sv;
+        partial[(int64_t)blockIdx.x * kMaxLen + threadIdx.x] = __dmul_rn(sv, la.dims[jj]);
     }
 }
 
@@ -124,9 +169,11 @@ int32_t estimate(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, double *c_
     }
     // grid is fixed by the row count only, so the reduction order is stable
     const int64_t blocks_cap = (int64_t)h->sm_count * 8;
+    int64_t long_cap = 0;
+    for (int i = 0; i < len; i++) long_cap = std::max<int64_t>(long_cap, chain[i]->n_est_long);
     auto al = [](int64_t x) { return (x + 255) & ~255LL; };
     const int64_t rbytes = al(8 * max_rows * len);
-    const int64_t pbytes = al(8 * blocks_cap * kMaxLen);
+    const int64_t pbytes = al(8 * (blocks_cap + long_cap) * kMaxLen);
     double *r_a = nullptr, *r_b = nullptr, *part = nullptr;
     RMCM_TRY(dev_alloc(h, (void **)&r_a, 2 * rbytes + pbytes));
     r_b = (double *)((char *)r_a + rbytes);
@@ -146,10 +193,18 @@ int32_t estimate(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, double *c_
         for (int j = 0; j < len; j++) la.dims[j] = (double)chain[j]->d.cols;
         int64_t blocks = (M.rows * 32 + kEstThreads - 1) / kEstThreads;
         blocks = std::max<int64_t>(1, std::min(blocks, blocks_cap));
-        k_res_level<<<(unsigned)blocks, kEstThreads, 0, s>>>(M, r_next, r_cur, la, part);
+        // rows of more than kEstLongRow entries (known for uploaded matrices)
+        // get a whole CTA each
+        const int32_t nlong = la.nj > 0 && chain[i]->n_est_long > 0 ? chain[i]->n_est_long : 0;
+        k_res_level<<<(unsigned)blocks, kEstThreads, 0, s>>>(M, r_next, r_cur, la, part, nlong > 0);
         h->launches++;
+        if (nlong > 0) {
+            k_res_long<<<(unsigned)nlong, kEstLongThreads, 0, s>>>(M, r_next, r_cur, la, chain[i]->est_long,
+                                                                   part + blocks * kMaxLen);
+            h->launches++;
+        }
         if (la.nj > 0) {
-            k_res_reduce<<<1, 256, 0, s>>>(part, (int32_t)blocks, la, c_dev);
+            k_res_reduce<<<1, 256, 0, s>>>(part, (int32_t)(blocks + nlong), la, c_dev);
             h->launches++;
         }
         e = cudaGetLastError();
@@ -259,7 +314,7 @@ extern "C" RMCM_API int32_t rmcm_estimate_noalloc(int32_t len, const int64_t *ro
         for (int j = 0; j < len; j++) la.dims[j] = (double)cols[j];
         int64_t blocks = (M.rows * 32 + kEstThreads - 1) / kEstThreads;
         blocks = std::max<int64_t>(1, std::min(blocks, blocks_cap));
-        k_res_level<<<(unsigned)blocks, kEstThreads, 0, s>>>(M, r_next, r_cur, la, part);
+        k_res_level<<<(unsigned)blocks, kEstThreads, 0, s>>>(M, r_next, r_cur, la, part, false);
         if (la.nj > 0) k_res_reduce<<<1, 256, 0, s>>>(part, (int32_t)blocks, la, c_dev);
         e = cudaGetLastError();
         std::swap(r_cur, r_next);

@@ -95,6 +95,10 @@ struct rmcm_mat {
     bool distinct = false;              // no column repeats within a row
     uint64_t *rowsum = nullptr;         // lazily computed row sums (device), owned
     int64_t max_row = -1;               // longest row (entries); -1 when unknown
+    // rows longer than kEstLongRow entries, ascending (device), when known:
+    // the estimator gives each a whole CTA
+    int32_t *est_long = nullptr;
+    int32_t n_est_long = -1;            // -1: not known (the estimator walks every row per warp)
     int64_t bytes = 0;
 };
 
@@ -146,6 +150,9 @@ struct rmcm_graph {
 };
 
 namespace rmcm {
+
+// Rows with more entries than this get a whole CTA in the estimator.
+constexpr int64_t kEstLongRow = 4096;
 
 // ---- error plumbing ------------------------------------------------------
 int32_t set_error(rmcm_handle *h, int32_t status, const std::string &msg);
