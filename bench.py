@@ -182,6 +182,25 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, ws: int) -> float:
+    """The largest value of x over the ranks (every rank gets it); the
+    process group's backend decides the tensor's device."""
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank: int, ws: int, seconds_max: float) -> float:
+    """Whole-job throughput of independent replicas: every rank processed
+    units_per_rank units; the job took the slowest rank's time."""
+    return units_per_rank * ws / seconds_max
+
+
 def cpu_reference(g, metapaths, steps, warmup, sample_note):
     """Oracle port of the reference's algorithm on all host cores: chains/s over full passes."""
     import oracle
@@ -406,12 +425,9 @@ def main():
     clk = rg_clock.stop() if not args.no_clocks else None
     timed_stats = eng.product_stats(reset=True)
     eng.set_profiling(0)
-    if ws > 1:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(elapsed_ms, ws)
     ms_per_step = elapsed_ms / args.steps
-    value = len(mps) * ws / (ms_per_step / 1e3)
+    value = replica_value(len(mps), ws, ms_per_step / 1e3)
 
     # roofline of the dominant SpGEMM product: bytes from the first pass, event
     # times of all its passes (analysis, symbolic, numeric) from the timed region
@@ -506,11 +522,8 @@ def main():
         torch.cuda.synchronize()
         barrier()
         e2e_s = (time.perf_counter() - t0) / args.steps
-        if ws > 1:
-            t = torch.tensor([e2e_s], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        e2e = {"value": len(mps) * ws / e2e_s, "unit": "chains/s", "h2d_bytes_per_step": int(h2d),
+        e2e_s = max_over_ranks(e2e_s, ws)
+        e2e = {"value": replica_value(len(mps), ws, e2e_s), "unit": "chains/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3}
 
     batched = served = None

@@ -118,6 +118,9 @@ __device__ __forceinline__ int classify(int64_t f, int64_t ncols, const BinParam
     if (need > 8192) return (!one_window && ncols <= kRankCols) ? kBinRank : kBinDense;
     if (need <= 512) return kBinHash512;
     if (need <= 2048) return kBinHash2k;
+    // rows wider than a window that would need the 8192-slot table: the rank
+    // bin's bitmap beats sorting up to 8192 entries with block barriers
+    if (!one_window && ncols <= kRankCols) return kBinRank;
     return kBinHash8k;
 }
 
