@@ -11,7 +11,9 @@ SpGEMM chain) over all four chains, results computed in full and freed.
   starts (CUDA events on the engine's stream, barrier + sync on both sides).
 * e2e: the same chains through the C ABI from pinned HOST buffers: per step
   every leaf CSR is uploaded (rmcm_mat_upload), the chain runs, and every
-  result CSR (rowptr, columns, counts) is copied back to pinned host memory.
+  result CSR (rowptr, columns, counts) is copied back to pinned host memory
+  (rmcm_mat_download_async: a result's copy overlaps the next chain's upload
+  and work; the step ends when every copy has landed).
 * roofline: the dominant numeric SpGEMM pass (largest event time), its
   algorithmic bytes (A + touched B rows + C) over its event-timed duration,
   against the measured HBM copy bandwidth.
@@ -498,19 +500,26 @@ def main():
                           torch.empty(max(nnz, 1), dtype=torch.int64 if vt == rg.VAL_U64 else torch.int32,
                                       pin_memory=True))
             d2h += (rows + 1) * 8 + nnz * 4 + nnz * (8 if vt == rg.VAL_U64 else 4)
-        import ctypes as C_
+
+        def upload(mp):
+            return [eng.upload_ptr(trp.data_ptr(), tcol.data_ptr(), trp.numel() - 1, cols)
+                    for trp, tcol, cols in host[mp]]
 
         def e2e_step():
-            for mp in mps:
-                mats = [eng.upload_ptr(trp.data_ptr(), tcol.data_ptr(), trp.numel() - 1, cols)
-                        for trp, tcol, cols in host[mp]]
+            # a chain's result travels to the host on the transfer stream while
+            # the next chain's leaves are uploaded and multiplied
+            nxt = upload(mps[0])
+            for i, mp in enumerate(mps):
+                mats = nxt
                 Cm, _, _ = eng.chain(mats)
                 rp_b, col_b, val_b = outbuf[mp]
-                eng._check(rg.lib().rmcm_mat_download(eng._h, Cm._h, C_.c_void_p(rp_b.data_ptr()),
-                                                      C_.c_void_p(col_b.data_ptr()), C_.c_void_p(val_b.data_ptr())))
+                eng.download_async(Cm, rp_b.data_ptr(), col_b.data_ptr(), val_b.data_ptr())
                 Cm.free()
                 for m in mats:
                     m.free()
+                if i + 1 < len(mps):
+                    nxt = upload(mps[i + 1])
+            eng.transfers_wait()
 
         for _ in range(max(1, min(args.warmup, 2))):
             e2e_step()

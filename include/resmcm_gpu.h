@@ -170,6 +170,16 @@ RMCM_API int32_t rmcm_mat_info(const rmcm_mat *m, int64_t *rows, int64_t *cols, 
 RMCM_API int32_t rmcm_mat_download(rmcm_handle *h, const rmcm_mat *m, int64_t *rowptr, int32_t *col,
                                    void *val);
 RMCM_API int32_t rmcm_mat_free(rmcm_handle *h, rmcm_mat *m);
+/* Asynchronous download (no reference counterpart: the reference keeps its
+ * results in host memory): the same copies as rmcm_mat_download, issued on
+ * the handle's transfer stream once the work already queued on its stream is
+ * done, so a result can travel to the host while the next chain computes.
+ * The host buffers (pinned memory for full speed) must stay valid until
+ * rmcm_transfers_wait returns; rmcm_mat_free may be called at once — the
+ * matrix is released when its download has landed. */
+RMCM_API int32_t rmcm_mat_download_async(rmcm_handle *h, rmcm_mat *m, int64_t *rowptr, int32_t *col, void *val);
+/* Waits for every asynchronous download of the handle. */
+RMCM_API int32_t rmcm_transfers_wait(rmcm_handle *h);
 
 /* ---- stage (a): RES estimator ---------------------------------------------
  * Replaces the estimator loop of rows_sparse_optimal_matrix_chain_order

@@ -149,6 +149,8 @@ def lib():
         "rmcm_mat_info": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i32)], i32),
         "rmcm_mat_download": ([vp, vp, vp, vp, vp], i32),
         "rmcm_mat_free": ([vp, vp], i32),
+        "rmcm_mat_download_async": ([vp, vp, vp, vp, vp], i32),
+        "rmcm_transfers_wait": ([vp], i32),
         "rmcm_estimate": ([vp, vp, i32, vp], i32),
         "rmcm_order": ([vp, vp, i32, vp, vp, vp], i32),
         "rmcm_spgemm": ([vp, vp, vp, pp], i32),
@@ -636,6 +638,15 @@ class Engine:
 
     def batch(self, graph: HeteroGraph, paths: list, lanes: int = 8) -> Batch:
         return Batch(self, graph, paths, lanes)
+
+    def download_async(self, m: Matrix, rowptr_ptr: int, col_ptr: int, val_ptr: int = 0):
+        """rmcm_mat_download_async into caller-owned (pinned) host buffers;
+        they are valid after transfers_wait()."""
+        self._check(lib().rmcm_mat_download_async(self._h, m._h, C.c_void_p(rowptr_ptr), C.c_void_p(col_ptr),
+                                                  C.c_void_p(val_ptr or None)))
+
+    def transfers_wait(self):
+        self._check(lib().rmcm_transfers_wait(self._h))
 
     def digest(self, m: Matrix) -> tuple:
         """(nnz, digest) of a device matrix (rmcm_mat_digest)."""

@@ -120,6 +120,7 @@ void mat_release(rmcm_handle *h, rmcm_mat *m) {
     if (!m) return;
     if (m->rowsum) dev_free(h, m->rowsum, 8 * m->d.rows);
     if (m->est_long) dev_free(h, m->est_long, 4 * (int64_t)m->n_est_long);
+    if (m->xfer_done) cudaEventDestroy(m->xfer_done);
     dev_free(h, m->d.rowptr, 8 * (m->d.rows + 1));
     if (m->d.col) dev_free(h, m->d.col, 4 * m->d.nnz);
     if (m->d.val) dev_free(h, m->d.val, val_bytes(m->valtype) * m->d.nnz);
@@ -1003,6 +1004,7 @@ RMCM_API int32_t rmcm_create(rmcm_handle **out, const rmcm_opts *opts) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->xfer, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_status, sizeof(int) * kNumStatus);
     if (e == cudaSuccess) e = cudaMemset(h->d_status, 0, sizeof(int) * kNumStatus);
     if (e == cudaSuccess) e = cudaMallocHost((void **)&h->h_status, sizeof(int) * kNumStatus);
@@ -1029,6 +1031,12 @@ RMCM_API int32_t rmcm_create(rmcm_handle **out, const rmcm_opts *opts) {
 RMCM_API int32_t rmcm_destroy(rmcm_handle *h) {
     if (!h) return RMCM_OK;
     while (!h->batches.empty()) rmcm_batch_free(h, *h->batches.begin());
+    if (h->xfer) {
+        // downloads in flight land first; matrices freed meanwhile go now
+        cudaStreamSynchronize(h->xfer);
+        for (rmcm_mat *m : h->deferred) mat_release(h, m);
+        h->deferred.clear();
+    }
     // graphs outliving their handle keep their host arrays only
     for (rmcm_graph *g : h->graphs) {
         for (auto &kv : g->leaves) mat_release(h, kv.second);
@@ -1047,6 +1055,7 @@ RMCM_API int32_t rmcm_destroy(rmcm_handle *h) {
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
     for (auto &e : h->ev)
         if (e) cudaEventDestroy(e);
+    if (h->xfer) cudaStreamDestroy(h->xfer);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
     if (h->aux) cudaStreamDestroy(h->aux);
@@ -1295,10 +1304,55 @@ RMCM_API int32_t rmcm_mat_download(rmcm_handle *h, const rmcm_mat *m, int64_t *r
     return RMCM_OK;
 }
 
+namespace {
+
+// Releases deferred matrices whose download has landed (all of them when
+// `all`, after the transfer stream has been synchronised).
+void release_deferred(rmcm_handle *h, bool all) {
+    auto &d = h->deferred;
+    size_t keep = 0;
+    for (size_t i = 0; i < d.size(); i++) {
+        if (all || cudaEventQuery(d[i]->xfer_done) == cudaSuccess) mat_release(h, d[i]);
+        else d[keep++] = d[i];
+    }
+    d.resize(keep);
+    cudaGetLastError();   // cudaErrorNotReady from the queries is not an error
+}
+
+}  // namespace
+
 RMCM_API int32_t rmcm_mat_free(rmcm_handle *h, rmcm_mat *m) {
     if (!h || !m) return RMCM_EINVAL;
     if (m->graph_owned) return set_error(h, RMCM_EINVAL, "leaf matrices are owned by their graph");
+    release_deferred(h, false);
+    if (m->xfer_done && cudaEventQuery(m->xfer_done) == cudaErrorNotReady) {
+        cudaGetLastError();
+        h->deferred.push_back(m);   // released once its download has landed
+        return RMCM_OK;
+    }
     mat_release(h, m);
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_mat_download_async(rmcm_handle *h, rmcm_mat *m, int64_t *rowptr, int32_t *col, void *val) {
+    if (!h || !m) return RMCM_EINVAL;
+    // the copies start once the work already queued on the handle's stream is done
+    RMCM_CUDA(h, cudaEventRecord(h->ev_fork, h->stream));
+    RMCM_CUDA(h, cudaStreamWaitEvent(h->xfer, h->ev_fork, 0));
+    cudaStream_t x = h->xfer;
+    if (rowptr) RMCM_CUDA(h, cudaMemcpyAsync(rowptr, m->d.rowptr, 8 * (m->d.rows + 1), cudaMemcpyDeviceToHost, x));
+    if (col && m->d.nnz) RMCM_CUDA(h, cudaMemcpyAsync(col, m->d.col, 4 * m->d.nnz, cudaMemcpyDeviceToHost, x));
+    if (val && m->d.nnz)
+        RMCM_CUDA(h, cudaMemcpyAsync(val, m->d.val, val_bytes(m->valtype) * m->d.nnz, cudaMemcpyDeviceToHost, x));
+    if (!m->xfer_done) RMCM_CUDA(h, cudaEventCreateWithFlags(&m->xfer_done, cudaEventDisableTiming));
+    RMCM_CUDA(h, cudaEventRecord(m->xfer_done, x));
+    return RMCM_OK;
+}
+
+RMCM_API int32_t rmcm_transfers_wait(rmcm_handle *h) {
+    if (!h) return RMCM_EINVAL;
+    RMCM_CUDA(h, cudaStreamSynchronize(h->xfer));
+    release_deferred(h, true);
     return RMCM_OK;
 }
 

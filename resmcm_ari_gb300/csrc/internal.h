@@ -99,6 +99,7 @@ struct rmcm_mat {
     // the estimator gives each a whole CTA
     int32_t *est_long = nullptr;
     int32_t n_est_long = -1;            // -1: not known (the estimator walks every row per warp)
+    cudaEvent_t xfer_done = nullptr;    // end of a pending asynchronous download (transfer stream)
     int64_t bytes = 0;
 };
 
@@ -124,6 +125,10 @@ struct rmcm_handle {
     // one operation (forked and joined with the two events)
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // transfer stream of asynchronous downloads; matrices freed while their
+    // download is in flight are released once it has landed
+    cudaStream_t xfer = nullptr;
+    std::vector<rmcm_mat *> deferred;
     rmcm::Tuning tune;
     int32_t prof_level = 0;
     std::vector<rmcm::ProdRecord> prof;

@@ -474,3 +474,26 @@ def test_estimator_long_rows_match_the_oracle(native, oracle_mod):
     og.close()
     hg.close()
     eng.close()
+
+
+def test_async_download_and_deferred_free(native, engine):
+    """rmcm_mat_download_async gives the same arrays as the synchronous copy,
+    even when the matrix is freed before the transfers are waited for."""
+    g = synth.tiny_dblp()
+    hg = native.HeteroGraph.from_synthetic(engine, g)
+    want = []
+    outs = []
+    for mp in ["1-3-0-1-2-4-0-0-1", "1-3-0-0-1"]:
+        C, _, _ = engine.run_metapath(hg, mp)
+        want.append(C.download())
+        rp = np.zeros(C.shape[0] + 1, np.int64)
+        col = np.zeros(max(C.nnz, 1), np.int32)
+        val = np.zeros(max(C.nnz, 1), np.uint64 if C.valtype == native.VAL_U64 else np.uint32)
+        engine.download_async(C, rp.ctypes.data, col.ctypes.data, val.ctypes.data)
+        C.free()                                  # released once the copy has landed
+        outs.append((rp, col, val))
+    engine.transfers_wait()
+    for (rp, col, val), (wrp, wcol, wval) in zip(outs, want):
+        assert np.array_equal(rp, wrp) and np.array_equal(col[:wcol.size], wcol)
+        assert np.array_equal(val[:wval.size].astype(np.uint64), wval.astype(np.uint64))
+    hg.close()
