@@ -1182,9 +1182,14 @@ __global__ void __launch_bounds__(kSplitThreads) k_dense_split(DevCsr A, DevCsr 
                                                                const int32_t *task_start, const int32_t *nslots,
                                                                int32_t max_slots, int32_t W,
                                                                unsigned long long *G, uint32_t *Gbits,
-                                                               const uint8_t *bin_of, int *st) {
+                                                               const uint8_t *bin_of, int *st, int32_t wc,
+                                                               bool pull_ok) {
     constexpr int NT = kSplitThreads;
+    constexpr int kPull = 4;   // register accumulators per thread: rows of up to 4 * NT columns
+    static_assert(kChunk == NT, "one staged A entry per thread");
     using AtomV = typename std::conditional<sizeof(V) == 4, unsigned int, unsigned long long>::type;
+    const V *Aval = (const V *)A.val;
+    const V *Bval = (const V *)B.val;
     extern __shared__ __align__(16) unsigned char smem[];
     uint8_t *present = smem;
     V *acc = (V *)(smem + (((size_t)W + 15) & ~(size_t)15));
@@ -1210,14 +1215,80 @@ __global__ void __launch_bounds__(kSplitThreads) k_dense_split(DevCsr A, DevCsr 
         const int64_t a0 = A.rowptr[r], alen = A.rowptr[r + 1] - a0;
         const int64_t ka = a0 + alen * part / np, kb = a0 + alen * (part + 1) / np;
         const bool checked = (bin_of[r] & kRiskyBit) != 0;
+        // B rows covering all wc columns ("full", as in the dense bin) are
+        // accumulated in registers by column owner; the rest stream through
+        // the shared-memory counters
+        V preg[kPull];
+#pragma unroll
+        for (int j = 0; j < kPull; j++) preg[j] = 0;
+        bool pulled = false;
         for (int64_t k0 = ka; k0 < kb; k0 += kChunk) {
             const int n = (int)(kb - k0 < (int64_t)kChunk ? kb - k0 : (int64_t)kChunk);
-            stage_full_rows<NT, V, true>(sg, A, B, k0, n);
+            int64_t len1[1] = {0};
+            bool full = false;
+            if (tid < n) {
+                const int32_t a = A.col[k0 + tid];
+                const int64_t b0 = B.rowptr[a];
+                const int64_t len = B.rowptr[a + 1] - b0;
+                full = pull_ok && len == wc;
+                sg.bs[tid] = b0;
+                sg.len[tid] = (int32_t)len;
+                sg.va[tid] = Aval[k0 + tid];
+                len1[0] = full ? 0 : len;
+            }
+            const unsigned fb = __ballot_sync(kFull, full);
+            if (lane == 0) sg.wf[tid >> 5] = __popc(fb);
+            stage_scan<NT>(len1, sg.pre, sg.warp_tot);
+            int pf = 0, tf = 0;
+            for (int w = 0; w < NT / 32; w++) {
+                if (w < (tid >> 5)) pf += sg.wf[w];
+                tf += sg.wf[w];
+            }
+            if (full) sg.flist[pf + __popc(fb & ((1u << lane) - 1u))] = tid;
+            __syncthreads();
             stream_chunk<NT, V, true>(sg, n, B, checked, ovf, [&](int32_t c, V p) {
                 present[c] = 1;
                 if (checked) add_shared_chk(acc + c, p, ovf);
                 else atomicAdd((AtomV *)(acc + c), (AtomV)p);
             });
+            for (int i0 = 0; i0 < tf; i0 += 4) {
+                pulled = true;
+                V bvals[4][kPull];
+                V av[4];
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const bool ok = i0 + e < tf;
+                    const int t = sg.flist[ok ? i0 + e : i0];
+                    av[e] = ok ? sg.va[t] : (V)0;
+                    const V *bv = Bval + sg.bs[t];
+#pragma unroll
+                    for (int j = 0; j < kPull; j++) {
+                        const int c = tid + j * NT;
+                        bvals[e][j] = (ok && c < wc) ? bv[c] : (V)0;
+                    }
+                }
+#pragma unroll
+                for (int e = 0; e < 4; e++)
+#pragma unroll
+                    for (int j = 0; j < kPull; j++) {
+                        const V p = checked ? mul_chk(av[e], bvals[e][j], ovf) : (V)(av[e] * bvals[e][j]);
+                        if (checked) ovf |= preg[j] > (V)~(V)0 - p;
+                        preg[j] += p;
+                    }
+            }
+            __syncthreads();
+        }
+        if (pulled) {
+            // each column has one owner; the window's atomics ended at the barrier above
+#pragma unroll
+            for (int j = 0; j < kPull; j++) {
+                const int c = tid + j * NT;
+                if (c < wc) {
+                    if (checked) ovf |= acc[c] > (V)~(V)0 - preg[j];
+                    acc[c] += preg[j];
+                    present[c] = 1;
+                }
+            }
             __syncthreads();
         }
         // merge: one global atomic per present column, then clear the window
@@ -1694,7 +1765,8 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                             RMCM_CUDA(h, cudaStreamWaitEvent(h->aux, h->ev_fork, 0));
                             k_dense_split<V><<<(int)((int64_t)h->sm_count * per_sm), kSplitThreads, sm, h->aux>>>(
                                 A, B, temp->perm, temp->row_of_slot, temp->parts, temp->task_start, temp->nslots,
-                                temp->max_slots, (int32_t)W, temp->G, temp->Gbits, bin_of, st);
+                                temp->max_slots, (int32_t)W, temp->G, temp->Gbits, bin_of, st, (int32_t)ncols,
+                                b_distinct && ncols <= 4 * kSplitThreads);
                             k_split_finish<V><<<temp->max_slots, kSplitThreads, 0, h->aux>>>(
                                 T, temp->perm, temp->row_of_slot, temp->nslots, temp->max_slots, ncols, (int32_t)W,
                                 temp->G, temp->Gbits, temp->stride, cnt, st);

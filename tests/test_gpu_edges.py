@@ -497,3 +497,20 @@ def test_async_download_and_deferred_free(native, engine):
         assert np.array_equal(rp, wrp) and np.array_equal(col[:wcol.size], wcol)
         assert np.array_equal(val[:wval.size].astype(np.uint64), wval.astype(np.uint64))
     hg.close()
+
+
+def test_split_rows_with_full_width_b_rows(native):
+    """Heavy rows split over CTAs whose B rows cover every column take the
+    register path inside the split kernel; uint32 and uint64 match scipy."""
+    rng = np.random.default_rng(35)
+    m, k, n = 24, 2600, 2000
+    a_nnz = rng.integers(1, 40, m)
+    a_nnz[5] = k
+    a_nnz[17] = 2000
+    A = _random_csr(rng, m, k, a_nnz, vmax=3)
+    rows_nnz = np.where(rng.random(k) < 0.6, n, rng.integers(1000, n, k))
+    B = _random_csr(rng, k, n, rows_nnz, vmax=3)
+    for vt in (native.VAL_U32, native.VAL_U64):
+        eng = native.Engine(device=0)
+        _check_product(native, eng, A, B, vt)
+        eng.close()
