@@ -81,6 +81,9 @@ struct ProductPlan {
     int64_t c_max_row = -1;
     bool split = false;
     int32_t n_front = 0;
+    int64_t max_rank_flops = 0;
+    bool rank_split = false;
+    int32_t rank_n_front = 0;
     int64_t scratch_bytes = 0;
 };
 

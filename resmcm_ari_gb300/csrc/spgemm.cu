@@ -145,6 +145,7 @@ struct AnalyzeOut {
     unsigned long long *flops_total;
     int32_t *certain;
     unsigned long long *dense_max_flops;
+    unsigned long long *rank_max_flops;
 };
 
 struct AnalyzeShared {
@@ -153,6 +154,7 @@ struct AnalyzeShared {
     int32_t certain;
     unsigned long long flops;
     unsigned long long max_flops;
+    unsigned long long max_rank_flops;
 };
 
 __device__ __forceinline__ void analyze_shared_init(AnalyzeShared &sh) {
@@ -162,6 +164,7 @@ __device__ __forceinline__ void analyze_shared_init(AnalyzeShared &sh) {
         sh.certain = 0;
         sh.flops = 0;
         sh.max_flops = 0;
+        sh.max_rank_flops = 0;
     }
 }
 
@@ -171,6 +174,7 @@ __device__ __forceinline__ void analyze_shared_flush(AnalyzeShared &sh, const An
         if (sh.flops) atomicAdd(o.flops_total, sh.flops);
         if (sh.max_alen) atomicMax(o.dense_max_alen, sh.max_alen);
         if (sh.max_flops) atomicMax(o.dense_max_flops, sh.max_flops);
+        if (sh.max_rank_flops) atomicMax(o.rank_max_flops, sh.max_rank_flops);
         if (sh.certain) atomicOr(o.certain, 1);
     }
 }
@@ -197,6 +201,7 @@ __device__ __forceinline__ void analyze_row(int64_t r, int64_t f, unsigned long 
             atomicMax(&sh.max_alen, (int32_t)(alen < (int64_t)INT_MAX ? alen : (int64_t)INT_MAX));
             atomicMax(&sh.max_flops, (unsigned long long)f);
         }
+        if (b == kBinRank) atomicMax(&sh.max_rank_flops, (unsigned long long)f);
     }
 }
 
@@ -1483,6 +1488,170 @@ __global__ void __launch_bounds__(kRankThreads) k_rank(DevCsr A, DevCsr B, DevCs
     if (__syncthreads_or(ovf) && tid == 0) raise_status(st, kOverflow);
 }
 
+// ------------------------------------------------------------------------
+// split rank rows (wide rows whose products exceed a fair share)
+// ------------------------------------------------------------------------
+//
+// As for dense rows: a heavy rank row is cut into parts of its A entries.
+// Symbolic: a CTA per part sets the bits of its products in a shared-memory
+// bitmap and ORs the nonzero words into the row's global bitmap; one CTA per
+// row counts the bits.  Numeric: one CTA per row turns the global bitmap into
+// per-word ranks, writes the sorted columns and zeroes the values; then a CTA
+// per part adds its products at their ranks with global atomics.
+
+// Task -> slot (last slot whose first task is <= task).
+__device__ __forceinline__ int split_slot_of(const int32_t *task_start, int ns, int task) {
+    int lo = 0, hi = ns - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (task_start[mid] <= task) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <typename V>
+__global__ void __launch_bounds__(kRankThreads) k_rank_split_sym(DevCsr A, DevCsr B, const int32_t *rows,
+                                                                 const int32_t *row_of_slot, const int32_t *parts,
+                                                                 const int32_t *task_start, const int32_t *nslots,
+                                                                 int32_t max_slots, int32_t nwords, uint32_t *gbits) {
+    constexpr int NT = kRankThreads;
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t *bits = (uint32_t *)smem;
+    __shared__ ChunkStage<V> sg;
+    const int tid = threadIdx.x;
+    const int ns = min(*nslots, max_slots);
+    const int ntasks = task_start[ns];
+    bool ovf = false;
+    for (int task = blockIdx.x; task < ntasks; task += gridDim.x) {
+        const int slot = split_slot_of(task_start, ns, task);
+        const int part = task - task_start[slot], np = parts[slot];
+        const int32_t r = rows[row_of_slot[slot]];
+        const int64_t a0 = A.rowptr[r], alen = A.rowptr[r + 1] - a0;
+        const int64_t ka = a0 + alen * part / np, kb = a0 + alen * (part + 1) / np;
+        for (int i = tid; i < nwords / 4; i += NT) ((uint4 *)bits)[i] = make_uint4(0, 0, 0, 0);
+        __syncthreads();
+        auto set_bit = [&](int32_t c, V) { atomicOr(bits + (c >> 5), 1u << (c & 31)); };
+        for (int64_t k0 = ka; k0 < kb; k0 += kChunk) {
+            const int n = (int)(kb - k0 < (int64_t)kChunk ? kb - k0 : (int64_t)kChunk);
+            stage_full_rows<NT, V, false>(sg, A, B, k0, n);
+            stream_chunk<NT, V, false>(sg, n, B, false, ovf, set_bit);
+            __syncthreads();
+        }
+        uint32_t *g = gbits + (int64_t)slot * nwords;
+        for (int w = tid; w < nwords; w += NT) {
+            const uint32_t b = bits[w];
+            if (b) atomicOr(g + w, b);
+        }
+        __syncthreads();
+    }
+}
+
+// One CTA per split row: its length from the global bitmap.
+__global__ void __launch_bounds__(512) k_rank_split_count(const int32_t *rows, const int32_t *row_of_slot,
+                                                          const int32_t *nslots, int32_t max_slots, int32_t nwords,
+                                                          const uint32_t *gbits, int64_t *cnt) {
+    __shared__ int s_warp[16];
+    const int ns = min(*nslots, max_slots);
+    for (int slot = blockIdx.x; slot < ns; slot += gridDim.x) {
+        const uint32_t *g = gbits + (int64_t)slot * nwords;
+        int mine = 0;
+        for (int w = threadIdx.x; w < nwords; w += 512) mine += __popc(g[w]);
+        int excl;
+        const int total = block_excl_scan<512>(mine, &excl, s_warp);
+        if (threadIdx.x == 0) cnt[rows[row_of_slot[slot]]] = total;
+    }
+}
+
+// One CTA per split row: per-word ranks (set bits before the word) into
+// gpre, the sorted columns into C, the row's values zeroed.
+template <typename V>
+__global__ void __launch_bounds__(kRankThreads) k_rank_split_prep(DevCsr C, const int32_t *rows,
+                                                                  const int32_t *row_of_slot, const int32_t *nslots,
+                                                                  int32_t max_slots, int32_t nwords,
+                                                                  const uint32_t *gbits, uint32_t *gpre, int *st) {
+    constexpr int NT = kRankThreads;
+    __shared__ int s_warp[NT / 32];
+    const int ns = min(*nslots, max_slots);
+    const int tid = threadIdx.x;
+    const int per = (nwords + NT - 1) / NT;
+    for (int slot = blockIdx.x; slot < ns; slot += gridDim.x) {
+        const int32_t r = rows[row_of_slot[slot]];
+        const uint32_t *g = gbits + (int64_t)slot * nwords;
+        uint32_t *pre = gpre + (int64_t)slot * nwords;
+        const int w0 = min(tid * per, nwords), w1 = min(w0 + per, nwords);
+        int mine = 0;
+        for (int w = w0; w < w1; w++) mine += __popc(g[w]);
+        int excl;
+        const int total = block_excl_scan<NT>(mine, &excl, s_warp);
+        const int64_t base = C.rowptr[r];
+        const int64_t rlen = C.rowptr[r + 1] - base;
+        if (tid == 0 && total != rlen) raise_status(st, kInvariant);
+        int64_t pos = excl;
+        for (int w = w0; w < w1; w++) {
+            pre[w] = (uint32_t)pos;
+            uint32_t word = g[w];
+            while (word) {
+                const int b = __ffs(word) - 1;
+                word &= word - 1;
+                if (pos < rlen) {
+                    C.col[base + pos] = w * 32 + b;
+                    ((V *)C.val)[base + pos] = 0;
+                }
+                pos++;
+            }
+        }
+    }
+}
+
+// One CTA per task: the part's products added at their ranks.
+template <typename V>
+__global__ void __launch_bounds__(kRankThreads) k_rank_split_val(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows,
+                                                                 const int32_t *row_of_slot, const int32_t *parts,
+                                                                 const int32_t *task_start, const int32_t *nslots,
+                                                                 int32_t max_slots, int32_t nwords,
+                                                                 const uint32_t *gbits, const uint32_t *gpre,
+                                                                 const uint8_t *bin_of, int *st) {
+    constexpr int NT = kRankThreads;
+    using AtomV = typename std::conditional<sizeof(V) == 4, unsigned int, unsigned long long>::type;
+    __shared__ ChunkStage<V> sg;
+    const int ns = min(*nslots, max_slots);
+    const int ntasks = task_start[ns];
+    bool ovf = false;
+    for (int task = blockIdx.x; task < ntasks; task += gridDim.x) {
+        const int slot = split_slot_of(task_start, ns, task);
+        const int part = task - task_start[slot], np = parts[slot];
+        const int32_t r = rows[row_of_slot[slot]];
+        const int64_t a0 = A.rowptr[r], alen = A.rowptr[r + 1] - a0;
+        const int64_t ka = a0 + alen * part / np, kb = a0 + alen * (part + 1) / np;
+        const bool checked = (bin_of[r] & kRiskyBit) != 0;
+        const uint32_t *g = gbits + (int64_t)slot * nwords;
+        const uint32_t *pre = gpre + (int64_t)slot * nwords;
+        const int64_t base = C.rowptr[r];
+        const int64_t rlen = C.rowptr[r + 1] - base;
+        V *vals = (V *)C.val + base;
+        auto add_val = [&](int32_t c, V p) {
+            const int w = c >> 5;
+            const int64_t pos = (int64_t)pre[w] + __popc(g[w] & ((1u << (c & 31)) - 1u));
+            if (pos < rlen) {
+                if (checked) {
+                    const AtomV old = atomicAdd((AtomV *)(vals + pos), (AtomV)p);
+                    ovf |= old > (AtomV)~(AtomV)0 - (AtomV)p;
+                } else {
+                    atomicAdd((AtomV *)(vals + pos), (AtomV)p);
+                }
+            }
+        };
+        for (int64_t k0 = ka; k0 < kb; k0 += kChunk) {
+            const int n = (int)(kb - k0 < (int64_t)kChunk ? kb - k0 : (int64_t)kChunk);
+            stage_full_rows<NT, V, true>(sg, A, B, k0, n);
+            stream_chunk<NT, V, true>(sg, n, B, checked, ovf, add_val);
+            __syncthreads();
+        }
+    }
+    if (__syncthreads_or(ovf) && threadIdx.x == 0) raise_status(st, kOverflow);
+}
+
 // Compacts TEMP-mode slots into C: row rows[ri] has cnt = rowptr[r+1]-rowptr[r]
 // entries at slot ri of the temporary.
 template <typename V>
@@ -1672,6 +1841,21 @@ struct DenseTemp {
     int64_t split_bytes = 0;
 };
 
+// Buffers of the split rank rows (alive from the symbolic to the numeric pass).
+struct RankSplit {
+    bool active = false;
+    int32_t *perm = nullptr;          // rank list, unsplit rows first
+    int32_t *front = nullptr, *nslots = nullptr;
+    int32_t n_front = 0;
+    int32_t *row_of_slot = nullptr, *parts = nullptr, *task_start = nullptr;
+    int32_t max_slots = 0, pmax = 0;
+    int64_t fpart = 0;
+    int32_t nwords = 0;
+    uint32_t *gbits = nullptr, *gpre = nullptr;
+    void *mem = nullptr;
+    int64_t bytes = 0;
+};
+
 // Rows with fewer products than this are never split.
 constexpr int64_t kSplitMinFlops = 1 << 20;
 
@@ -1682,7 +1866,7 @@ template <typename V, bool NUMERIC>
 int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevCsr &C, const int32_t *lists,
                     const int32_t *counts, int32_t dense_max_alen, int64_t *cnt, int32_t *cursor_base,
                     int64_t cursor_cap, const DenseTemp *temp, const uint8_t *bin_of, bool positive,
-                    bool b_distinct) {
+                    bool b_distinct, const RankSplit *rs) {
     cudaStream_t s = h->stream;
     int *st = h->d_status;
     int32_t off = 0;
@@ -1741,7 +1925,38 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                 RMCM_TRY(set_smem(h, kern, sm));
                 const int per_sm = (int)std::max<int64_t>(1, std::min<int64_t>(4, (200 * 1024) / std::max<int64_t>(sm, 1)));
                 const int grid = (int)std::min<int64_t>((int64_t)n, (int64_t)h->sm_count * per_sm);
-                kern<<<grid, kRankThreads, sm, s>>>(A, B, C, list, n, cnt, st, bin_of);
+                const bool split = rs && rs->active;
+                if (split) {
+                    // split rows on the second stream, beside the unsplit ones
+                    RMCM_CUDA(h, cudaEventRecord(h->ev_fork, s));
+                    RMCM_CUDA(h, cudaStreamWaitEvent(h->aux, h->ev_fork, 0));
+                    const int sgrid = h->sm_count * 2;
+                    if (!NUMERIC) {
+                        auto ks = k_rank_split_sym<V>;
+                        RMCM_TRY(set_smem(h, ks, nwords * 4));
+                        k_rank_split_sym<V><<<sgrid, kRankThreads, nwords * 4, h->aux>>>(
+                            A, B, rs->perm, rs->row_of_slot, rs->parts, rs->task_start, rs->nslots, rs->max_slots,
+                            (int32_t)nwords, rs->gbits);
+                        k_rank_split_count<<<rs->max_slots, 512, 0, h->aux>>>(
+                            rs->perm, rs->row_of_slot, rs->nslots, rs->max_slots, (int32_t)nwords, rs->gbits, cnt);
+                    } else {
+                        k_rank_split_prep<V><<<rs->max_slots, kRankThreads, 0, h->aux>>>(
+                            C, rs->perm, rs->row_of_slot, rs->nslots, rs->max_slots, (int32_t)nwords, rs->gbits,
+                            rs->gpre, st);
+                        k_rank_split_val<V><<<sgrid, kRankThreads, 0, h->aux>>>(
+                            A, B, C, rs->perm, rs->row_of_slot, rs->parts, rs->task_start, rs->nslots,
+                            rs->max_slots, (int32_t)nwords, rs->gbits, rs->gpre, bin_of, st);
+                    }
+                    h->launches += 2;
+                }
+                const int32_t *rl = split ? rs->perm : list;
+                const int32_t rn = split ? rs->n_front : n;
+                if (rn > 0)
+                    kern<<<std::max(1, std::min(grid, rn)), kRankThreads, sm, s>>>(A, B, C, rl, rn, cnt, st, bin_of);
+                if (split) {
+                    RMCM_CUDA(h, cudaEventRecord(h->ev_join, h->aux));
+                    RMCM_CUDA(h, cudaStreamWaitEvent(s, h->ev_join, 0));
+                }
                 break;
             }
             case kBinDense: {
@@ -1881,7 +2096,10 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     int32_t *lists = (int32_t *)(sc + o_lists);
     // small: [0..6] bin counts, [8..14] bin cursors, [16] longest dense A row,
     // [32..33] total flops (u64), [36..37] largest dense-row flops (u64),
-    // [40] overflow certain, [42] split slots, [48..51] profiling sums
+    // [40] overflow certain, [42] dense split slots, [43] long A rows,
+    // [44..45] longest C row (u64), [46] unsplit dense rows, [48..51]
+    // profiling sums, [52] rank split slots, [53] unsplit rank rows,
+    // [54..55] largest rank-row flops (u64)
     int32_t *small = (int32_t *)(sc + o_small);
     RMCM_CUDA(h, cudaMemsetAsync(small, 0, 256, s));
 
@@ -1908,7 +2126,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     }
     if (m > 0) {
         AnalyzeOut ao{flops, bin_of, small, small + 16, (unsigned long long *)(small + 32), small + 40,
-                      (unsigned long long *)(small + 36)};
+                      (unsigned long long *)(small + 36), (unsigned long long *)(small + 54)};
         // rows longer than kLongAnalyze entries: walked by the whole grid
         const bool long_rows = Am->max_row > kLongAnalyze;
         const int64_t max_long = A.nnz / kLongAnalyze + 1;
@@ -1951,7 +2169,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         dense_max_alen = plan->dense_max_alen;
         flops_total = plan->flops;
     } else {
-        RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned, small, 44 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned, small, 64 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         RMCM_CUDA(h, cudaStreamSynchronize(s));
         memcpy(counts, h->h_pinned, sizeof(counts));
         dense_max_alen = ((int32_t *)h->h_pinned)[16];
@@ -2078,6 +2296,73 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         }
         if (record) plan->n_front = dtemp.n_front;
     }
+    // Rank-bin rows likewise (k_rank_split_*)
+    RankSplit rsplit;
+    int64_t max_rank_f = 0;
+    if (replay) max_rank_f = plan->max_rank_flops;
+    else memcpy(&max_rank_f, (int32_t *)h->h_pinned + 54, sizeof(int64_t));
+    if (record) plan->max_rank_flops = max_rank_f;
+    if (counts[kBinRank] > 0) {
+        const int64_t fpart = std::max<int64_t>(kSplitMinFlops, flops_total / ((int64_t)h->sm_count * 4));
+        if (max_rank_f > fpart) {
+            const int32_t nr = counts[kBinRank];
+            const int32_t max_slots = (int32_t)std::min<int64_t>(std::min<int64_t>(1024, nr), flops_total / fpart + 1);
+            const int64_t nwords = (B.cols + 1023) / 1024 * 32;
+            auto al = [](int64_t x) { return (x + 255) & ~255LL; };
+            const int64_t o_perm = 0;
+            const int64_t o_row = o_perm + al(4LL * nr);
+            const int64_t o_parts = o_row + al(4LL * max_slots);
+            const int64_t o_ts = o_parts + al(4LL * max_slots);
+            const int64_t o_bits = o_ts + al(4LL * (max_slots + 1));
+            const int64_t o_pre = o_bits + al(4LL * max_slots * nwords);
+            const int64_t total = o_pre + al(4LL * max_slots * nwords);
+            void *mem = nullptr;
+            if (dev_alloc(h, &mem, total) == RMCM_OK) {
+                char *b = (char *)mem;
+                rsplit.active = true;
+                rsplit.perm = (int32_t *)(b + o_perm);
+                rsplit.row_of_slot = (int32_t *)(b + o_row);
+                rsplit.parts = (int32_t *)(b + o_parts);
+                rsplit.task_start = (int32_t *)(b + o_ts);
+                rsplit.gbits = (uint32_t *)(b + o_bits);
+                rsplit.gpre = (uint32_t *)(b + o_pre);
+                rsplit.nslots = small + 52;
+                rsplit.front = small + 53;
+                rsplit.max_slots = max_slots;
+                rsplit.pmax = h->sm_count * 2;
+                rsplit.fpart = fpart;
+                rsplit.nwords = (int32_t)nwords;
+                rsplit.mem = mem;
+                rsplit.bytes = total;
+                RMCM_CUDA(h, cudaMemsetAsync(b + o_bits, 0, 4LL * max_slots * nwords, s));
+                int32_t roff = 0;
+                for (int b2 = 0; b2 < kBinRank; b2++) roff += counts[b2];
+                k_split_select<<<grid_for(h, nr, 256, 8), 256, 0, s>>>(lists + roff, nr, flops, fpart, rsplit.pmax,
+                                                                       rsplit.perm, rsplit.front, rsplit.nslots,
+                                                                       rsplit.row_of_slot, rsplit.parts, max_slots);
+                k_split_tasks<<<1, 1024, 0, s>>>(rsplit.parts, rsplit.nslots, max_slots, rsplit.task_start);
+                h->launches += 2;
+                RMCM_CUDA(h, cudaGetLastError());
+                if (replay) {
+                    rsplit.n_front = plan->rank_n_front;
+                } else {
+                    RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned + 3, rsplit.front, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+                    RMCM_CUDA(h, cudaStreamSynchronize(s));
+                    rsplit.n_front = ((int32_t *)(h->h_pinned + 3))[0];
+                }
+                if (record) plan->rank_n_front = rsplit.n_front;
+            } else {
+                h->last_error.clear();
+            }
+        }
+    }
+    if (replay && plan->rank_split && !rsplit.active)
+        return set_error(h, RMCM_ENOMEM, "replay: split rank-row buffers could not be allocated");
+    if (record) plan->rank_split = rsplit.active;
+    auto drop_rank = [&]() {
+        if (rsplit.active) dev_free(h, rsplit.mem, rsplit.bytes);
+        rsplit.active = false;
+    };
     auto drop_temp = [&]() {
         if (dtemp.active) dev_free(h, dtemp.col, dtemp.bytes);
         if (dtemp.split) dev_free(h, dtemp.split_mem, dtemp.split_bytes);
@@ -2091,10 +2376,11 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     if (rc != RMCM_OK) {
         drop_cursors();
         drop_temp();
+        drop_rank();
         return rc;
     }
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[2], s);
-    rc = launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap, &dtemp, bin_of, positive, Bm->distinct);
+    rc = launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap, &dtemp, bin_of, positive, Bm->distinct, &rsplit);
     if (rc == RMCM_OK) rc = scan_rowptr(h, cnt, m, C->d.rowptr, tiles, (unsigned long long *)(small + 44));
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[3], s);
     // nnz to the host, then the output arrays
@@ -2127,6 +2413,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
             cudaMemsetAsync(h->d_status + kOverflow, 0, sizeof(int), s);
             drop_cursors();
             drop_temp();
+            drop_rank();
             mat_release(h, C);
             if (rec) {
                 for (auto &e : h->prof[rec_idx].ev) cudaEventDestroy(e);
@@ -2137,9 +2424,10 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     }
     if (rc == RMCM_OK) rc = mat_alloc(h, m, B.cols, nnz, Am->valtype, &C);
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[4], s);
-    if (rc == RMCM_OK) rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap, &dtemp, bin_of, positive, Bm->distinct);
+    if (rc == RMCM_OK) rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap, &dtemp, bin_of, positive, Bm->distinct, &rsplit);
     drop_cursors();
     drop_temp();
+    drop_rank();
     if (rc != RMCM_OK) {
         mat_release(h, C);
         return rc;

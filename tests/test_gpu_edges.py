@@ -514,3 +514,23 @@ def test_split_rows_with_full_width_b_rows(native):
         eng = native.Engine(device=0)
         _check_product(native, eng, A, B, vt)
         eng.close()
+
+
+def test_heavy_rank_rows_are_split_over_ctas(native):
+    """Rows wider than a dense window (rank bin) with millions of products:
+    the heavy rows are split over CTAs (global bitmap + ranks); the light ones
+    stay in the rank kernel; uint32 and uint64 match scipy."""
+    rng = np.random.default_rng(36)
+    m, k, n = 12, 21000, 60000
+    a_nnz = rng.integers(200, 400, m)
+    a_nnz[3] = 20000
+    a_nnz[9] = 15000
+    A = _random_csr(rng, m, k, a_nnz, vmax=3)
+    B = _random_csr(rng, k, n, rng.integers(60, 140, k), vmax=3)
+    for vt in (native.VAL_U32, native.VAL_U64):
+        eng = native.Engine(device=0)
+        eng.set_profiling(1)
+        _check_product(native, eng, A, B, vt)
+        st = eng.product_stats()[0]
+        assert st["bin_rows"][5] > 0
+        eng.close()
