@@ -82,6 +82,7 @@ struct ProductPlan {
     bool split = false;
     int32_t n_front = 0;
     int64_t max_rank_flops = 0;
+    int32_t risky_rows = 0;
     bool rank_split = false;
     int32_t rank_n_front = 0;
     int64_t scratch_bytes = 0;

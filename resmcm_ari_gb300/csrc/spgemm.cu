@@ -38,6 +38,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <tuple>
 #include <type_traits>
 
 #include "internal.h"
@@ -146,12 +147,14 @@ struct AnalyzeOut {
     int32_t *certain;
     unsigned long long *dense_max_flops;
     unsigned long long *rank_max_flops;
+    int32_t *risky_rows;
 };
 
 struct AnalyzeShared {
     int32_t cnt[kNumBins];
     int32_t max_alen;
     int32_t certain;
+    int32_t risky;
     unsigned long long flops;
     unsigned long long max_flops;
     unsigned long long max_rank_flops;
@@ -162,6 +165,7 @@ __device__ __forceinline__ void analyze_shared_init(AnalyzeShared &sh) {
     if (threadIdx.x == 0) {
         sh.max_alen = 0;
         sh.certain = 0;
+        sh.risky = 0;
         sh.flops = 0;
         sh.max_flops = 0;
         sh.max_rank_flops = 0;
@@ -176,6 +180,7 @@ __device__ __forceinline__ void analyze_shared_flush(AnalyzeShared &sh, const An
         if (sh.max_flops) atomicMax(o.dense_max_flops, sh.max_flops);
         if (sh.max_rank_flops) atomicMax(o.rank_max_flops, sh.max_rank_flops);
         if (sh.certain) atomicOr(o.certain, 1);
+        if (sh.risky) atomicAdd(o.risky_rows, sh.risky);
     }
 }
 
@@ -191,6 +196,7 @@ __device__ __forceinline__ void analyze_row(int64_t r, int64_t f, unsigned long 
     o.flops[r] = f;
     o.bin_of[r] = (uint8_t)(b | (risky ? kRiskyBit : 0));
     if (f) atomicAdd(&sh.flops, (unsigned long long)f);
+    if (risky && b != kEmptyBin) atomicAdd(&sh.risky, 1);
     if (sizeof(V) == 4 && risky) {
         const unsigned long long distinct = (unsigned long long)min(f, ncols);
         if (srow == ~0ull || srow / vmax > distinct) sh.certain = 1;
@@ -210,7 +216,33 @@ template <typename V>
 __device__ __forceinline__ void analyze_entries(const DevCsr &A, const DevCsr &B, int64_t k0, int64_t k1, int step,
                                                 int64_t &f, unsigned long long &srow) {
     const V *Aval = (const V *)A.val;
-    for (int64_t k = k0; k < k1; k += step) {
+    int64_t k = k0;
+    // four entries per step: their gathers are independent and overlap
+    for (; k + 3 * (int64_t)step < k1; k += 4 * (int64_t)step) {
+        int32_t a[4];
+        unsigned long long av[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            a[u] = A.col[k + u * step];
+            av[u] = Aval[k + u * step];
+        }
+        int64_t lo[4], hi[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            lo[u] = B.rowptr[a[u]];
+            hi[u] = B.rowptr[a[u] + 1];
+        }
+        unsigned long long bsum[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) bsum[u] = B.rowsum ? B.rowsum[a[u]] : (unsigned long long)(hi[u] - lo[u]);
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            f += hi[u] - lo[u];
+            const unsigned long long prod = __umul64hi(av[u], bsum[u]) ? ~0ull : av[u] * bsum[u];
+            srow = sat_add(srow, prod);
+        }
+    }
+    for (; k < k1; k += step) {
         const int32_t a = A.col[k];
         const int64_t len = B.rowptr[a + 1] - B.rowptr[a];
         f += len;
@@ -884,7 +916,7 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
 // to slot ri of a row-padded temporary (C.col / C.val point at it, slot
 // stride `tstride` entries) and its length goes to cnt[r]; the symbolic pass
 // is skipped for these rows and k_copy_rows compacts the slots into C.
-template <typename V, bool NUMERIC, bool TEMP>
+template <typename V, bool NUMERIC, bool TEMP, bool PRES = true>
 __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows,
                                                          int32_t nrows, int64_t *cnt, int32_t *cursors,
                                                          int64_t cur_stride, int32_t W, int *st, int64_t tstride,
@@ -897,8 +929,10 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
     constexpr int NW = NT / 32;
     using AtomV = typename std::conditional<sizeof(V) == 4, unsigned int, unsigned long long>::type;
     extern __shared__ __align__(16) unsigned char smem[];
+    // PRES = false: no presence bytes (every row's counters mark presence;
+    // launched only when every value is >= 1 and no row can overflow)
     uint8_t *present = smem;
-    V *acc = (V *)(smem + (((size_t)W + 15) & ~(size_t)15));
+    V *acc = (V *)(PRES ? smem + (((size_t)W + 15) & ~(size_t)15) : smem);
     __shared__ ChunkStage<V> sg;
     __shared__ int64_t s_warp[NW];
     __shared__ int32_t s_next;
@@ -907,7 +941,8 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
     const unsigned lt_mask = (1u << lane) - 1u;
     const V *Aval = (const V *)A.val;
     const V *Bval = (const V *)B.val;
-    for (int i = tid; i < W / 16; i += NT) ((uint4 *)present)[i] = make_uint4(0, 0, 0, 0);
+    if (PRES)
+        for (int i = tid; i < W / 16; i += NT) ((uint4 *)present)[i] = make_uint4(0, 0, 0, 0);
     if (NUMERIC)
         for (int i = tid; i < W; i += NT) acc[i] = 0;
     const bool multi = B.cols > W;
@@ -926,7 +961,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
         // A row that cannot overflow needs no checks, and when every input
         // value is >= 1 its counters alone mark presence (no count is 0).
         const bool checked = NUMERIC && (bin_of[r] & kRiskyBit) != 0;
-        const bool track = !NUMERIC || checked || !positive;
+        const bool track = PRES && (!NUMERIC || checked || !positive);
         const int64_t row_base = TEMP ? (int64_t)ri * tstride : (NUMERIC ? C.rowptr[r] : 0);
         const int64_t row_end = TEMP ? row_base + tstride : (NUMERIC ? C.rowptr[r + 1] : 0);
         int64_t out = row_base;
@@ -1816,6 +1851,26 @@ int32_t set_smem(rmcm_handle *h, F *kernel, int64_t bytes) {
     return RMCM_OK;
 }
 
+// Resident CTAs per SM of `kernel` at `threads` threads and `bytes` of dynamic
+// shared memory (cached per device, kernel and size; the kernel's shared
+// memory limit must already be set).
+template <typename F>
+int occupancy(rmcm_handle *h, F *kernel, int threads, int64_t bytes) {
+    static std::mutex mu;
+    static std::map<std::tuple<int, const void *, int64_t>, int> known;
+    std::lock_guard<std::mutex> lock(mu);
+    auto key = std::make_tuple(h->device, (const void *)kernel, bytes);
+    auto it = known.find(key);
+    if (it != known.end()) return it->second;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, (size_t)bytes) != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    known[key] = n;
+    return n;
+}
+
 // Row-padded temporary of the single-pass dense rows, and the buffers of the
 // rows split over several CTAs.
 struct DenseTemp {
@@ -1824,6 +1879,7 @@ struct DenseTemp {
     void *val = nullptr;
     int64_t stride = 0;
     int64_t bytes = 0;
+    bool no_risky = false;            // no row can overflow: with positive inputs, no presence bytes
     // split rows
     bool split = false;
     const int64_t *flops = nullptr;   // per-row products (scratch)
@@ -1964,8 +2020,21 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                     if (!NUMERIC) {
                         // one pass: columns + counts into the padded slots, lengths to cnt
                         const int64_t W = (ncols + 31) / 32 * 32;
-                        const int64_t sm = ((W + 15) & ~15LL) + W * (int64_t)sizeof(V);
-                        auto kern = k_dense<V, true, true>;
+                        // every value >= 1 and no row able to overflow: the
+                        // counters alone mark presence, so the window holds only
+                        // them (a smaller CTA, more of them per SM)
+                        const int64_t sm_full = ((W + 15) & ~15LL) + W * (int64_t)sizeof(V);
+                        const int64_t sm_lite = W * (int64_t)sizeof(V);
+                        bool lite = false;
+                        if (positive && temp->no_risky) {
+                            RMCM_TRY(set_smem(h, k_dense<V, true, true>, sm_full));
+                            RMCM_TRY(set_smem(h, k_dense<V, true, true, false>, sm_lite));
+                            // only where dropping the bytes fits more CTAs per SM
+                            lite = occupancy(h, k_dense<V, true, true, false>, kDenseThreads, sm_lite) >
+                                   occupancy(h, k_dense<V, true, true>, kDenseThreads, sm_full);
+                        }
+                        const int64_t sm = lite ? sm_lite : sm_full;
+                        auto kern = lite ? k_dense<V, true, true, false> : k_dense<V, true, true>;
                         RMCM_TRY(set_smem(h, kern, sm));
                         const int per_sm = (int)std::max<int64_t>(1, std::min<int64_t>(4, (200 * 1024) / std::max<int64_t>(sm, 1)));
                         const int grid = (int)std::min<int64_t>((int64_t)n, (int64_t)h->sm_count * per_sm);
@@ -2099,7 +2168,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     // [40] overflow certain, [42] dense split slots, [43] long A rows,
     // [44..45] longest C row (u64), [46] unsplit dense rows, [48..51]
     // profiling sums, [52] rank split slots, [53] unsplit rank rows,
-    // [54..55] largest rank-row flops (u64)
+    // [54..55] largest rank-row flops (u64), [56] rows that may overflow
     int32_t *small = (int32_t *)(sc + o_small);
     RMCM_CUDA(h, cudaMemsetAsync(small, 0, 256, s));
 
@@ -2126,7 +2195,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     }
     if (m > 0) {
         AnalyzeOut ao{flops, bin_of, small, small + 16, (unsigned long long *)(small + 32), small + 40,
-                      (unsigned long long *)(small + 36), (unsigned long long *)(small + 54)};
+                      (unsigned long long *)(small + 36), (unsigned long long *)(small + 54), small + 56};
         // rows longer than kLongAnalyze entries: walked by the whole grid
         const bool long_rows = Am->max_row > kLongAnalyze;
         const int64_t max_long = A.nnz / kLongAnalyze + 1;
@@ -2229,6 +2298,13 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     if (replay && plan->dense_temp && !dtemp.active)
         return set_error(h, RMCM_ENOMEM, "replay: dense temporary could not be allocated");
     if (record) plan->dense_temp = dtemp.active;
+    {
+        int32_t risky_rows = 0;
+        if (replay) risky_rows = plan->risky_rows;
+        else risky_rows = ((int32_t *)h->h_pinned)[56];
+        if (record) plan->risky_rows = risky_rows;
+        dtemp.no_risky = risky_rows == 0;
+    }
     // Dense rows with far more products than a fair share of the device are
     // split over several CTAs (k_dense_split).
     int64_t max_dense_f = 0;
