@@ -1216,7 +1216,7 @@ __global__ void __launch_bounds__(1024) k_split_tasks(const int32_t *parts, cons
 
 // One CTA per task (slot, part): the part's A-entry range into the shared
 // window, then its nonzero counters into the slot's global accumulator.
-template <typename V>
+template <typename V, bool PRES = true>
 __global__ void __launch_bounds__(kSplitThreads) k_dense_split(DevCsr A, DevCsr B, const int32_t *rows,
                                                                const int32_t *row_of_slot, const int32_t *parts,
                                                                const int32_t *task_start, const int32_t *nslots,
@@ -1231,13 +1231,16 @@ __global__ void __launch_bounds__(kSplitThreads) k_dense_split(DevCsr A, DevCsr 
     const V *Aval = (const V *)A.val;
     const V *Bval = (const V *)B.val;
     extern __shared__ __align__(16) unsigned char smem[];
+    // PRES = false (every value >= 1, no row can overflow): counters alone
+    // mark presence and the window holds only them
     uint8_t *present = smem;
-    V *acc = (V *)(smem + (((size_t)W + 15) & ~(size_t)15));
+    V *acc = (V *)(PRES ? smem + (((size_t)W + 15) & ~(size_t)15) : smem);
     __shared__ ChunkStage<V> sg;
     const int tid = threadIdx.x, lane = tid & 31;
     const int ns = min(*nslots, max_slots);
     const int ntasks = task_start[ns];
-    for (int i = tid; i < W / 16; i += NT) ((uint4 *)present)[i] = make_uint4(0, 0, 0, 0);
+    if (PRES)
+        for (int i = tid; i < W / 16; i += NT) ((uint4 *)present)[i] = make_uint4(0, 0, 0, 0);
     for (int i = tid; i < W; i += NT) acc[i] = 0;
     bool ovf = false;
     __syncthreads();
@@ -1287,7 +1290,7 @@ __global__ void __launch_bounds__(kSplitThreads) k_dense_split(DevCsr A, DevCsr 
             if (full) sg.flist[pf + __popc(fb & ((1u << lane) - 1u))] = tid;
             __syncthreads();
             stream_chunk<NT, V, true>(sg, n, B, checked, ovf, [&](int32_t c, V p) {
-                present[c] = 1;
+                if (PRES) present[c] = 1;
                 if (checked) add_shared_chk(acc + c, p, ovf);
                 else atomicAdd((AtomV *)(acc + c), (AtomV)p);
             });
@@ -1326,7 +1329,7 @@ __global__ void __launch_bounds__(kSplitThreads) k_dense_split(DevCsr A, DevCsr 
                 if (c < wc) {
                     if (checked) ovf |= acc[c] > (V)~(V)0 - preg[j];
                     acc[c] += preg[j];
-                    present[c] = 1;
+                    if (PRES) present[c] = 1;
                 }
             }
             __syncthreads();
@@ -1335,7 +1338,7 @@ __global__ void __launch_bounds__(kSplitThreads) k_dense_split(DevCsr A, DevCsr 
         unsigned long long *g = G + (int64_t)slot * W;
         uint32_t *gb = Gbits + (int64_t)slot * (W / 32);
         for (int c = tid; c < W; c += NT) {
-            const bool here = present[c] != 0;
+            const bool here = PRES ? present[c] != 0 : acc[c] != 0;
             const unsigned bits = __ballot_sync(kFull, here);
             if (here) {
                 const unsigned long long v = (unsigned long long)acc[c];
@@ -1343,7 +1346,7 @@ __global__ void __launch_bounds__(kSplitThreads) k_dense_split(DevCsr A, DevCsr 
                     const unsigned long long old = atomicAdd(g + c, v);
                     ovf |= old > ~0ull - v;
                 }
-                present[c] = 0;
+                if (PRES) present[c] = 0;
                 acc[c] = 0;
             }
             if (lane == 0 && bits) atomicOr(gb + (c >> 5), bits);
@@ -2043,11 +2046,14 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                         T.val = temp->val;
                         if (temp->split) {
                             // the split rows run on the second stream, beside the dense bin
-                            auto ks = k_dense_split<V>;
-                            RMCM_TRY(set_smem(h, ks, sm));
+                            const bool slite = positive && temp->no_risky;
+                            const int64_t ssm = slite ? sm_lite : sm_full;
+                            auto ks = slite ? k_dense_split<V, false> : k_dense_split<V, true>;
+                            RMCM_TRY(set_smem(h, ks, ssm));
                             RMCM_CUDA(h, cudaEventRecord(h->ev_fork, s));
                             RMCM_CUDA(h, cudaStreamWaitEvent(h->aux, h->ev_fork, 0));
-                            k_dense_split<V><<<(int)((int64_t)h->sm_count * per_sm), kSplitThreads, sm, h->aux>>>(
+                            const int sper = (int)std::max<int64_t>(1, std::min<int64_t>(4, (200 * 1024) / std::max<int64_t>(ssm, 1)));
+                            ks<<<(int)((int64_t)h->sm_count * sper), kSplitThreads, ssm, h->aux>>>(
                                 A, B, temp->perm, temp->row_of_slot, temp->parts, temp->task_start, temp->nslots,
                                 temp->max_slots, (int32_t)W, temp->G, temp->Gbits, bin_of, st, (int32_t)ncols,
                                 b_distinct && ncols <= 4 * kSplitThreads);
