@@ -12,8 +12,9 @@ SpGEMM chain) over all four chains, results computed in full and freed.
 * e2e: the same chains through the C ABI from pinned HOST buffers: per step
   every leaf CSR is uploaded (rmcm_mat_upload), the chain runs, and every
   result CSR (rowptr, columns, counts) is copied back to pinned host memory
-  (rmcm_mat_download_async: a result's copy overlaps the next chain's upload
-  and work; the step ends when every copy has landed).
+  (rmcm_mat_download_async: a result's copy overlaps the next chain's work,
+  and a loader handle on a helper thread uploads the next chain's leaves
+  meanwhile; the step ends when every copy has landed).
 * roofline: the dominant numeric SpGEMM pass (largest event time), its
   algorithmic bytes (A + touched B rows + C) over its event-timed duration,
   against the measured HBM copy bandwidth.
@@ -501,25 +502,38 @@ def main():
                                       pin_memory=True))
             d2h += (rows + 1) * 8 + nnz * 4 + nnz * (8 if vt == rg.VAL_U64 else 4)
 
+        # a loader handle uploads (and validates) the next chain's leaves on a
+        # helper thread while this one multiplies the current chain
+        loader = rg.Engine(device=local, valtype=rg.VAL_AUTO)
+        from concurrent.futures import ThreadPoolExecutor
+        pool = ThreadPoolExecutor(max_workers=1)
+
         def upload(mp):
-            return [eng.upload_ptr(trp.data_ptr(), tcol.data_ptr(), trp.numel() - 1, cols)
+            mats = [loader.upload_ptr(trp.data_ptr(), tcol.data_ptr(), trp.numel() - 1, cols)
                     for trp, tcol, cols in host[mp]]
+            loader.synchronize()
+            return mats
 
         def e2e_step():
             # a chain's result travels to the host on the transfer stream while
             # the next chain's leaves are uploaded and multiplied
-            nxt = upload(mps[0])
+            fut = pool.submit(upload, mps[0])
             for i, mp in enumerate(mps):
-                mats = nxt
+                mats = fut.result()
+                if i + 1 < len(mps):
+                    fut = pool.submit(upload, mps[i + 1])
                 Cm, _, _ = eng.chain(mats)
                 rp_b, col_b, val_b = outbuf[mp]
                 eng.download_async(Cm, rp_b.data_ptr(), col_b.data_ptr(), val_b.data_ptr())
                 Cm.free()
+                done.append(mats)
+            eng.transfers_wait()
+            for mats in done:
                 for m in mats:
                     m.free()
-                if i + 1 < len(mps):
-                    nxt = upload(mps[i + 1])
-            eng.transfers_wait()
+            done.clear()
+
+        done = []
 
         for _ in range(max(1, min(args.warmup, 2))):
             e2e_step()
@@ -532,6 +546,8 @@ def main():
         barrier()
         e2e_s = (time.perf_counter() - t0) / args.steps
         e2e_s = max_over_ranks(e2e_s, ws)
+        pool.shutdown()
+        loader.close()
         e2e = {"value": replica_value(len(mps), ws, e2e_s), "unit": "chains/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3}
 

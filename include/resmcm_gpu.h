@@ -180,6 +180,11 @@ RMCM_API int32_t rmcm_mat_free(rmcm_handle *h, rmcm_mat *m);
 RMCM_API int32_t rmcm_mat_download_async(rmcm_handle *h, rmcm_mat *m, int64_t *rowptr, int32_t *col, void *val);
 /* Waits for every asynchronous download of the handle. */
 RMCM_API int32_t rmcm_transfers_wait(rmcm_handle *h);
+/* Waits for all work of the handle (its stream and its transfer stream).
+ * Matrices made on one handle may be read by another handle's operations
+ * once this has returned (a loader thread can upload the next chain on its
+ * own handle while this one multiplies). */
+RMCM_API int32_t rmcm_synchronize(rmcm_handle *h);
 
 /* ---- stage (a): RES estimator ---------------------------------------------
  * Replaces the estimator loop of rows_sparse_optimal_matrix_chain_order

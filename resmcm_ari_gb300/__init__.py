@@ -151,6 +151,7 @@ def lib():
         "rmcm_mat_free": ([vp, vp], i32),
         "rmcm_mat_download_async": ([vp, vp, vp, vp, vp], i32),
         "rmcm_transfers_wait": ([vp], i32),
+        "rmcm_synchronize": ([vp], i32),
         "rmcm_estimate": ([vp, vp, i32, vp], i32),
         "rmcm_order": ([vp, vp, i32, vp, vp, vp], i32),
         "rmcm_spgemm": ([vp, vp, vp, pp], i32),
@@ -647,6 +648,10 @@ class Engine:
 
     def transfers_wait(self):
         self._check(lib().rmcm_transfers_wait(self._h))
+
+    def synchronize(self):
+        """rmcm_synchronize: all work of this handle is done."""
+        self._check(lib().rmcm_synchronize(self._h))
 
     def digest(self, m: Matrix) -> tuple:
         """(nnz, digest) of a device matrix (rmcm_mat_digest)."""

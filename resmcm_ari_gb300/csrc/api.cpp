@@ -1349,6 +1349,14 @@ RMCM_API int32_t rmcm_mat_download_async(rmcm_handle *h, rmcm_mat *m, int64_t *r
     return RMCM_OK;
 }
 
+RMCM_API int32_t rmcm_synchronize(rmcm_handle *h) {
+    if (!h) return RMCM_EINVAL;
+    RMCM_CUDA(h, cudaStreamSynchronize(h->stream));
+    RMCM_CUDA(h, cudaStreamSynchronize(h->xfer));
+    release_deferred(h, true);
+    return RMCM_OK;
+}
+
 RMCM_API int32_t rmcm_transfers_wait(rmcm_handle *h) {
     if (!h) return RMCM_EINVAL;
     RMCM_CUDA(h, cudaStreamSynchronize(h->xfer));

@@ -534,3 +534,29 @@ def test_heavy_rank_rows_are_split_over_ctas(native):
         st = eng.product_stats()[0]
         assert st["bin_rows"][5] > 0
         eng.close()
+
+
+def test_matrices_of_one_handle_feed_another_after_synchronize(native, engine):
+    """A loader handle uploads a chain's leaves; after rmcm_synchronize the
+    compute handle multiplies them: same result as with its own uploads."""
+    g = synth.tiny_dblp()
+    hg = native.HeteroGraph.from_synthetic(engine, g)
+    mp = "1-3-0-1-2-4-0-0-1"
+    want, _, _ = engine.run_metapath(hg, mp)
+    want_arrays = want.download()
+    want.free()
+    loader = native.Engine(device=0)
+    mats = []
+    for leaf in hg.leaves(mp):
+        rp, col, _ = leaf.download(values=False)
+        mats.append(loader.upload(rp, col, cols=leaf.shape[1]))
+    loader.synchronize()
+    C, _, rc = engine.chain(mats)
+    got = C.download()
+    C.free()
+    for a, b in zip(got, want_arrays):
+        assert np.array_equal(a, b)
+    for m in mats:
+        m.free()
+    loader.close()
+    hg.close()
