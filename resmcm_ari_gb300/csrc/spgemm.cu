@@ -351,7 +351,7 @@ __global__ void k_rowsum(DevCsr M, uint64_t *out) {
 
 // Row ids into per-bin lists laid out back to back (offsets from bin_count).
 __global__ void k_scatter(int64_t m, const uint8_t *bin_of, const int32_t *bin_count, int32_t *bin_cursor,
-                          int32_t *lists) {
+                          int32_t *lists, int64_t *cnt) {
     __shared__ int32_t off[kNumBins];
     if (threadIdx.x == 0) {
         int32_t s = 0;
@@ -360,16 +360,16 @@ __global__ void k_scatter(int64_t m, const uint8_t *bin_of, const int32_t *bin_c
     __syncthreads();
     for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x) {
         const int b = bin_of[r] & ~kRiskyBit;
-        if (b == kEmptyBin) continue;
+        if (b == kEmptyBin) {
+            cnt[r] = 0;   // rows without products have no entries
+            continue;
+        }
         const int32_t pos = atomicAdd(bin_cursor + b, 1);
         lists[off[b] + pos] = (int32_t)r;
     }
 }
 
-__global__ void k_zero_counts(int64_t m, const uint8_t *bin_of, int64_t *cnt) {
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x)
-        if ((bin_of[r] & ~kRiskyBit) == kEmptyBin) cnt[r] = 0;
-}
+
 
 // ------------------------------------------------------------------------
 // tiny bin: one warp per row, <= 32 products held one per lane
@@ -1738,7 +1738,8 @@ __device__ __forceinline__ int64_t block_scan_i64(int64_t v, int64_t *s_warp, in
 
 // rowptr[i+1] = inclusive partial sums within a tile; tile sums to tile_sum.
 __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int64_t *cnt, int64_t m, int64_t *rowptr,
-                                                             int64_t *tile_sum, unsigned long long *row_max) {
+                                                             int64_t *tile_sum, unsigned long long *row_max,
+                                                             int64_t expect, int *st) {
     __shared__ int64_t s_warp[32];
     const int64_t t0 = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
     int64_t v[kScanItems];
@@ -1760,8 +1761,11 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int64_t *cnt,
     for (int i = 0; i < kScanItems; i++) {
         run += v[i];
         if (t0 + i < m) rowptr[t0 + i + 1] = run;
+        // one tile: the scan is complete here (a replay checks its size)
+        if (gridDim.x == 1 && t0 + i == m - 1 && expect >= 0 && run != expect) raise_status(st, kInvariant);
     }
     if (threadIdx.x == 0) tile_sum[blockIdx.x] = tot;
+    if (gridDim.x == 1 && threadIdx.x == 0) rowptr[0] = 0;
 }
 
 // One block: exclusive scan of the tile sums in place.
@@ -1784,13 +1788,19 @@ __global__ void __launch_bounds__(1024) k_scan_sums(int64_t *tile_sum, int64_t n
     if (threadIdx.x == 0) rowptr[0] = 0;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_add(int64_t m, int64_t *rowptr, const int64_t *tile_sum) {
+__global__ void __launch_bounds__(kScanThreads) k_scan_add(int64_t m, int64_t *rowptr, const int64_t *tile_sum,
+                                                           int64_t expect, int *st) {
     const int64_t t0 = (int64_t)blockIdx.x * kScanTile;
     const int64_t add = tile_sum[blockIdx.x];
-    if (add == 0) return;
+    if (add == 0 && (expect < 0 || t0 + kScanTile < m)) return;
     for (int i = threadIdx.x; i < kScanTile; i += kScanThreads) {
         const int64_t r = t0 + i;
-        if (r < m) rowptr[r + 1] += add;
+        if (r < m) {
+            const int64_t v = rowptr[r + 1] + add;
+            if (add) rowptr[r + 1] = v;
+            // the last row's end is the product's size (a replay checks it)
+            if (r == m - 1 && expect >= 0 && v != expect) raise_status(st, kInvariant);
+        }
     }
 }
 
@@ -2105,29 +2115,27 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
     return RMCM_OK;
 }
 
+// Exclusive scan of the row lengths into rowptr (rowptr[0] = 0); one tile
+// needs one launch.  expect >= 0 checks the total (replays).
 int32_t scan_rowptr(rmcm_handle *h, const int64_t *cnt, int64_t m, int64_t *rowptr, int64_t *tile_sum,
-                    unsigned long long *row_max) {
+                    unsigned long long *row_max, int64_t expect) {
     cudaStream_t s = h->stream;
     const int64_t ntiles = std::max<int64_t>(1, (m + kScanTile - 1) / kScanTile);
-    if (m > 0) {
-        k_scan_tiles<<<(unsigned)ntiles, kScanThreads, 0, s>>>(cnt, m, rowptr, tile_sum, row_max);
-        h->launches++;
-    } else {
-        RMCM_CUDA(h, cudaMemsetAsync(tile_sum, 0, sizeof(int64_t), s));
+    if (m == 0) {
+        RMCM_CUDA(h, cudaMemsetAsync(rowptr, 0, sizeof(int64_t), s));
+        return RMCM_OK;
     }
-    k_scan_sums<<<1, 1024, 0, s>>>(tile_sum, ntiles, rowptr);
+    k_scan_tiles<<<(unsigned)ntiles, kScanThreads, 0, s>>>(cnt, m, rowptr, tile_sum, row_max, expect, h->d_status);
     h->launches++;
-    if (m > 0) {
-        k_scan_add<<<(unsigned)ntiles, kScanThreads, 0, s>>>(m, rowptr, tile_sum);
-        h->launches++;
+    if (ntiles > 1) {
+        k_scan_sums<<<1, 1024, 0, s>>>(tile_sum, ntiles, rowptr);
+        k_scan_add<<<(unsigned)ntiles, kScanThreads, 0, s>>>(m, rowptr, tile_sum, expect, h->d_status);
+        h->launches += 2;
     }
     RMCM_CUDA(h, cudaGetLastError());
     return RMCM_OK;
 }
 
-__global__ void k_check_nnz(const int64_t *nnz_dev, int64_t expect, int *st) {
-    if (threadIdx.x == 0 && *nnz_dev != expect) raise_status(st, kInvariant);
-}
 
 template <typename V>
 int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_mat **Cout, int64_t *flops_out,
@@ -2223,9 +2231,8 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
             k_analyze_long_finish<V><<<4, 256, 0, s>>>(A, B, bp, ao, llist, nlong, acc_f, acc_s, lsat);
             h->launches += 2;
         }
-        k_scatter<<<grid_for(h, m, 256, 8), 256, 0, s>>>(m, bin_of, small, small + 8, lists);
-        k_zero_counts<<<grid_for(h, m, 256, 8), 256, 0, s>>>(m, bin_of, cnt);
-        h->launches += 2;
+        k_scatter<<<grid_for(h, m, 256, 8), 256, 0, s>>>(m, bin_of, small, small + 8, lists, cnt);
+        h->launches += 1;
         if (long_mem) {
             dev_free(h, long_mem, long_bytes);
             long_mem = nullptr;
@@ -2463,7 +2470,8 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     }
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[2], s);
     rc = launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap, &dtemp, bin_of, positive, Bm->distinct, &rsplit);
-    if (rc == RMCM_OK) rc = scan_rowptr(h, cnt, m, C->d.rowptr, tiles, (unsigned long long *)(small + 44));
+    if (rc == RMCM_OK)
+        rc = scan_rowptr(h, cnt, m, C->d.rowptr, tiles, (unsigned long long *)(small + 44), replay ? plan->nnz : -1);
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[3], s);
     // nnz to the host, then the output arrays
     int64_t *hp = h->h_pinned;
@@ -2472,12 +2480,6 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         if (e == cudaSuccess) e = cudaMemcpyAsync(hp + 1, small + 44, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) rc = cuda_error(h, e, "spgemm nnz download");
-    }
-    if (rc == RMCM_OK && replay) {
-        // the replayed symbolic pass must find the recorded size
-        k_check_nnz<<<1, 32, 0, s>>>(C->d.rowptr + m, plan->nnz, h->d_status);
-        h->launches++;
-        if (cudaGetLastError() != cudaSuccess) rc = set_error(h, RMCM_ECUDA, "replay nnz check launch");
     }
     const int64_t nnz = replay ? plan->nnz : hp[0];
     const int64_t c_max_row = replay ? plan->c_max_row : hp[1];
