@@ -718,6 +718,61 @@ __device__ __forceinline__ void stream_long(ChunkStage<V> &sg, int cnt, const De
     }
 }
 
+// Shared-memory add at a 32-bit shared address (no value returned).
+__device__ __forceinline__ void red_shared_add(uint32_t addr, uint32_t v) {
+    asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(addr), "r"(v));
+}
+__device__ __forceinline__ void red_shared_add(uint32_t addr, uint64_t v) {
+    asm volatile("red.shared.add.u64 [%0], %1;" ::"r"(addr), "l"(v));
+}
+
+// stream_long for rows that need neither overflow checks nor presence bytes:
+// add(col, product) only.  Each lane keeps one pointer pair into the B
+// segment; whole blocks of 128 positions run unpredicated (eight loads per
+// lane in flight, immediate offsets), the remainder once with predicates.
+template <typename V, typename Add>
+__device__ __forceinline__ void stream_long_plain(ChunkStage<V> &sg, int cnt, const DevCsr B, Add add) {
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        int i = 0;
+        if (lane == 0) i = atomicAdd(&sg.ctr, 1);
+        i = __shfl_sync(kFull, i, 0);
+        if (i >= cnt) break;
+        const int t = sg.llist[i];
+        const int32_t L = sg.len[t];
+        const int64_t q0 = sg.bs[t] + lane;
+        const int32_t *pc = B.col + q0;
+        const V *pv = (const V *)B.val + q0;
+        const V a = sg.va[t];
+        for (int32_t nb = L >> 7; nb > 0; nb--, pc += 128, pv += 128) {
+            int32_t c[4];
+            V v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                c[u] = __ldg(pc + 32 * u);
+                v[u] = __ldg(pv + 32 * u);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) add(c[u], (V)(a * v[u]));
+        }
+        const int32_t rest = (L & 127) - lane;   // this lane's positions: lane, lane + 32, ...
+        int32_t c[4];
+        V v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            c[u] = 0;
+            v[u] = 0;
+            if (32 * u < rest) {
+                c[u] = __ldg(pc + 32 * u);
+                v[u] = __ldg(pv + 32 * u);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (32 * u < rest) add(c[u], (V)(a * v[u]));
+    }
+}
+
 // ------------------------------------------------------------------------
 // hash bins: one CTA per row, shared-memory linear probing
 // ------------------------------------------------------------------------
@@ -1049,8 +1104,17 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                     }
                 }
                 __syncthreads();
-                if (sg.nlong) stream_long<V, NUMERIC>(sg, sg.nlong, B, checked, ovf, visit);
-                stream_chunk<NT, V, NUMERIC>(sg, n, B, checked, ovf, visit);
+                if (NUMERIC && !checked && !track) {
+                    // counters only: 32-bit shared addresses, no flag tests per product
+                    const uint32_t acc_s =
+                        (uint32_t)__cvta_generic_to_shared(acc) - (uint32_t)w0 * (uint32_t)sizeof(V);
+                    auto add = [&](int32_t c, V p) { red_shared_add(acc_s + (uint32_t)c * (uint32_t)sizeof(V), p); };
+                    if (sg.nlong) stream_long_plain<V>(sg, sg.nlong, B, add);
+                    stream_chunk<NT, V, NUMERIC>(sg, n, B, false, ovf, add);
+                } else {
+                    if (sg.nlong) stream_long<V, NUMERIC>(sg, sg.nlong, B, checked, ovf, visit);
+                    stream_chunk<NT, V, NUMERIC>(sg, n, B, checked, ovf, visit);
+                }
                 const int nfull = sg.nfull;
                 for (int i0 = 0; i0 < nfull; i0 += 4) {
                     // four full entries per step: sixteen independent loads per thread
