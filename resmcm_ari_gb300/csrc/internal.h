@@ -86,6 +86,7 @@ struct ProductPlan {
     bool rank_split = false;
     int32_t rank_n_front = 0;
     int64_t scratch_bytes = 0;
+    int32_t pack_cbits = 0;          // column bits of the packed copy of B (0: not packed)
 };
 
 }  // namespace rmcm
@@ -97,7 +98,7 @@ struct rmcm_mat {
     bool ones = false;                  // every value is 1 (leaves): row sums are row lengths
     bool positive = false;              // every value is >= 1 (a counter > 0 then marks presence)
     bool distinct = false;              // no column repeats within a row
-    uint64_t *rowsum = nullptr;         // lazily computed row sums (device), owned
+    uint64_t *rowsum = nullptr;         // lazily computed row sums (device, rows + 1: the largest value last), owned
     int64_t max_row = -1;               // longest row (entries); -1 when unknown
     // rows longer than kEstLongRow entries, ascending (device), when known:
     // the estimator gives each a whole CTA

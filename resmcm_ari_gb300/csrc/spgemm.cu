@@ -55,6 +55,9 @@ constexpr int32_t kDenseWinU32 = 40960;       // 160 KB counters + 40 KB presenc
 constexpr int32_t kDenseWinU64 = 22528;       // 176 KB counters + 22 KB presence bytes
 constexpr int32_t kDenseWinSym = 196608;      // presence bytes only: 192 KB
 constexpr int kDenseThreads = 512;
+// B is packed for the dense bin when the product has at least this many
+// multiply-adds per entry of B.
+constexpr int64_t kPackReuse = 64;
 
 __device__ __forceinline__ void raise_status(int *st, int word) { atomicOr(st + word, 1); }
 
@@ -334,18 +337,83 @@ __global__ void __launch_bounds__(256) k_analyze_long_finish(DevCsr A, DevCsr B,
     analyze_shared_flush(sh, o);
 }
 
-// Saturating row sums of a matrix's values (warp per row).
+// Saturating row sums of a matrix's values (warp per row); out[M.rows]
+// (zeroed by the caller) receives the largest value.
 template <typename V>
 __global__ void k_rowsum(DevCsr M, uint64_t *out) {
     const int lane = threadIdx.x & 31;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const V *v = (const V *)M.val;
+    unsigned long long vmax = 0;
     for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < M.rows; r += nwarps) {
         unsigned long long sum = 0;
-        for (int64_t q = M.rowptr[r] + lane; q < M.rowptr[r + 1]; q += 32) sum = sat_add(sum, (unsigned long long)v[q]);
+        for (int64_t q = M.rowptr[r] + lane; q < M.rowptr[r + 1]; q += 32) {
+            const unsigned long long x = (unsigned long long)v[q];
+            sum = sat_add(sum, x);
+            vmax = x > vmax ? x : vmax;
+        }
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) sum = sat_add(sum, __shfl_xor_sync(kFull, sum, d));
         if (lane == 0) out[r] = sum;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(kFull, vmax, d);
+        vmax = o > vmax ? o : vmax;
+    }
+    if (lane == 0 && vmax) atomicMax((unsigned long long *)out + M.rows, vmax);
+}
+
+// Packed copy of B for the dense bin's plain path: entry q becomes
+// (value << cbits) | column at a position of its own row such that the r-th
+// entry of every shared-memory bank (column mod 32) lands in group r, groups
+// in order and banks ascending within a group.  Any 32 consecutive positions
+// then touch each bank at most twice (once per group they straddle), where
+// the sorted order puts several columns of a sparse row on one bank.  Ranks
+// within a bank follow the sorted order, so the layout is deterministic.
+__global__ void __launch_bounds__(256) k_pack_banked(DevCsr B, int32_t cbits, uint32_t *pk, int *st) {
+    __shared__ int32_t s_cnt[8][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int32_t *cnt = s_cnt[warp];
+    const uint32_t *bv = (const uint32_t *)B.val;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < B.rows; r += nwarps) {
+        const int64_t q0 = B.rowptr[r], q1 = B.rowptr[r + 1];
+        cnt[lane] = 0;
+        __syncwarp();
+        for (int64_t q = q0 + lane; q < q1; q += 32) atomicAdd(&cnt[B.col[q] & 31], 1);
+        __syncwarp();
+        const int32_t total = cnt[lane];   // entries of bank `lane`
+        __syncwarp();
+        cnt[lane] = 0;                     // running rank per bank
+        __syncwarp();
+        for (int64_t base = q0; base < q1; base += 32) {
+            const int64_t q = base + lane;
+            const bool ok = q < q1;
+            const int32_t c = ok ? B.col[q] : 0;
+            const int32_t bank = ok ? (c & 31) : 32 + lane;
+            const unsigned peers = __match_any_sync(kFull, bank);
+            const int32_t rank = ok ? cnt[bank] + __popc(peers & lt_mask) : 0;
+            __syncwarp();
+            if (ok && lane == 31 - __clz(peers)) cnt[bank] += __popc(peers);
+            __syncwarp();
+            // entries before (rank, bank): min(total_b, rank) of every bank,
+            // plus one of each lower bank that reaches this rank
+            int32_t pos = 0;
+#pragma unroll 8
+            for (int b = 0; b < 32; b++) {
+                const int32_t t = __shfl_sync(kFull, total, b);
+                pos += min(t, rank) + ((b < bank && t > rank) ? 1 : 0);
+            }
+            if (ok) {
+                const uint32_t x = bv[q];
+                // the host checked the largest value; a replay on other values would not fit
+                if (x >> (32 - cbits)) raise_status(st, kInvariant);
+                pk[q0 + pos] = (x << cbits) | (uint32_t)c;
+            }
+        }
+        __syncwarp();
     }
 }
 
@@ -773,6 +841,39 @@ __device__ __forceinline__ void stream_long_plain(ChunkStage<V> &sg, int cnt, co
     }
 }
 
+// stream_long_plain over the packed copy of B (k_pack_banked): one load per
+// position, column and value split from the word.
+template <typename Add>
+__device__ __forceinline__ void stream_long_packed(ChunkStage<uint32_t> &sg, int cnt, const uint32_t *pk,
+                                                   int32_t cbits, Add add) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t cmask = (1u << cbits) - 1u;
+    while (true) {
+        int i = 0;
+        if (lane == 0) i = atomicAdd(&sg.ctr, 1);
+        i = __shfl_sync(kFull, i, 0);
+        if (i >= cnt) break;
+        const int t = sg.llist[i];
+        const int32_t L = sg.len[t];
+        const uint32_t *pw = pk + sg.bs[t] + lane;
+        const uint32_t a = sg.va[t];
+        for (int32_t nb = L >> 7; nb > 0; nb--, pw += 128) {
+            uint32_t w[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) w[u] = __ldg(pw + 32 * u);
+#pragma unroll
+            for (int u = 0; u < 4; u++) add((int32_t)(w[u] & cmask), a * (w[u] >> cbits));
+        }
+        const int32_t rest = (L & 127) - lane;
+        uint32_t w[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) w[u] = 32 * u < rest ? __ldg(pw + 32 * u) : 0u;
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (32 * u < rest) add((int32_t)(w[u] & cmask), a * (w[u] >> cbits));
+    }
+}
+
 // ------------------------------------------------------------------------
 // hash bins: one CTA per row, shared-memory linear probing
 // ------------------------------------------------------------------------
@@ -976,7 +1077,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                                                          int32_t nrows, int64_t *cnt, int32_t *cursors,
                                                          int64_t cur_stride, int32_t W, int *st, int64_t tstride,
                                                          const uint8_t *bin_of, bool positive, bool b_distinct,
-                                                         bool abort_mode) {
+                                                         bool abort_mode, const uint32_t *pk, int32_t cbits) {
     constexpr int NT = kDenseThreads;
     constexpr int kPull = 4;   // register accumulators per thread: windows of up to 4 * NT columns
     static_assert(kChunk == NT, "the dense kernel stages one A entry per thread");
@@ -1104,14 +1205,27 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                     }
                 }
                 __syncthreads();
-                if (NUMERIC && !checked && !track) {
-                    // counters only: 32-bit shared addresses, no flag tests per product
-                    const uint32_t acc_s =
-                        (uint32_t)__cvta_generic_to_shared(acc) - (uint32_t)w0 * (uint32_t)sizeof(V);
-                    auto add = [&](int32_t c, V p) { red_shared_add(acc_s + (uint32_t)c * (uint32_t)sizeof(V), p); };
-                    if (sg.nlong) stream_long_plain<V>(sg, sg.nlong, B, add);
-                    stream_chunk<NT, V, NUMERIC>(sg, n, B, false, ovf, add);
-                } else {
+                bool plain = false;
+                if constexpr (NUMERIC && sizeof(V) == 4) {
+                    // uint32 counters only: 32-bit shared addresses, no flag tests per
+                    // product (the uint64 kernel keeps the general path: the plain one
+                    // costs it registers and spills)
+                    plain = !checked && !track;
+                    if (plain) {
+                        const uint32_t acc_s =
+                            (uint32_t)__cvta_generic_to_shared(acc) - (uint32_t)w0 * (uint32_t)sizeof(V);
+                        auto add = [&](int32_t c, V p) {
+                            red_shared_add(acc_s + (uint32_t)c * (uint32_t)sizeof(V), p);
+                        };
+                        if (sg.nlong) {
+                            // pk: packed copy of B (single window only)
+                            if (pk) stream_long_packed(sg, sg.nlong, pk, cbits, add);
+                            else stream_long_plain<V>(sg, sg.nlong, B, add);
+                        }
+                        stream_chunk<NT, V, NUMERIC>(sg, n, B, false, ovf, add);
+                    }
+                }
+                if (!plain) {
                     if (sg.nlong) stream_long<V, NUMERIC>(sg, sg.nlong, B, checked, ovf, visit);
                     stream_chunk<NT, V, NUMERIC>(sg, n, B, checked, ovf, visit);
                 }
@@ -1957,6 +2071,11 @@ struct DenseTemp {
     int64_t stride = 0;
     int64_t bytes = 0;
     bool no_risky = false;            // no row can overflow: with positive inputs, no presence bytes
+    // packed copy of B (k_pack_banked) for the plain path of single-window rows
+    const uint32_t *pk = nullptr;
+    int32_t cbits = 0;
+    void *pk_mem = nullptr;
+    int64_t pk_bytes = 0;
     // split rows
     bool split = false;
     const int64_t *flops = nullptr;   // per-row products (scratch)
@@ -2143,7 +2262,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                         if (dn > 0)
                             kern<<<std::max(1, std::min(grid, dn)), kDenseThreads, sm, s>>>(
                                 A, B, T, dl, dn, cnt, nullptr, 0, (int32_t)W, st, temp->stride, bin_of, positive,
-                                b_distinct, h->abort_on_certain_overflow);
+                                b_distinct, h->abort_on_certain_overflow, temp->pk, temp->cbits);
                         if (temp->split) {
                             RMCM_CUDA(h, cudaEventRecord(h->ev_join, h->aux));
                             RMCM_CUDA(h, cudaStreamWaitEvent(s, h->ev_join, 0));
@@ -2169,7 +2288,9 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                     grid = (int)std::max<int64_t>(1, cursor_cap / stride);
                 }
                 kern<<<grid, kDenseThreads, sm, s>>>(A, B, C, list, n, cnt, cursor_base, stride, (int32_t)W, st, 0, bin_of,
-                                                     positive, b_distinct, h->abort_on_certain_overflow);
+                                                     positive, b_distinct, h->abort_on_certain_overflow,
+                                                     NUMERIC && !multi && temp ? temp->pk : nullptr,
+                                                     temp ? temp->cbits : 0);
                 break;
             }
         }
@@ -2210,7 +2331,8 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     // row sums of B bound the counts of every output row (computed once per matrix)
     if (!Bm->ones && !Bm->rowsum && Bm->d.rows > 0) {
         rmcm_mat *Bw = const_cast<rmcm_mat *>(Bm);
-        RMCM_TRY(dev_alloc(h, (void **)&Bw->rowsum, 8 * Bm->d.rows));
+        RMCM_TRY(dev_alloc(h, (void **)&Bw->rowsum, 8 * (Bm->d.rows + 1)));
+        RMCM_CUDA(h, cudaMemsetAsync(Bw->rowsum + Bm->d.rows, 0, 8, s));
         k_rowsum<V><<<grid_for(h, Bm->d.rows * 32, 256, 8), 256, 0, s>>>(Bm->d, Bw->rowsum);
         h->launches++;
         RMCM_CUDA(h, cudaGetLastError());
@@ -2246,9 +2368,14 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     // [40] overflow certain, [42] dense split slots, [43] long A rows,
     // [44..45] longest C row (u64), [46] unsplit dense rows, [48..51]
     // profiling sums, [52] rank split slots, [53] unsplit rank rows,
-    // [54..55] largest rank-row flops (u64), [56] rows that may overflow
+    // [54..55] largest rank-row flops (u64), [56] rows that may overflow,
+    // [58..59] largest value of B (u64, when B may be packed)
     int32_t *small = (int32_t *)(sc + o_small);
     RMCM_CUDA(h, cudaMemsetAsync(small, 0, 256, s));
+    // B may be packed for the dense bin (uint32, positive, one window)
+    const bool pack_cand = sizeof(V) == 4 && positive && B.cols >= 2 && B.cols <= kDenseWinU32 && B.nnz > 0;
+    if (pack_cand && !Bm->ones && !replay)
+        RMCM_CUDA(h, cudaMemcpyAsync(small + 58, Bm->rowsum + Bm->d.rows, 8, cudaMemcpyDeviceToDevice, s));
 
     ProdRecord *rec = nullptr;
     size_t rec_idx = 0;
@@ -2381,6 +2508,37 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         else risky_rows = ((int32_t *)h->h_pinned)[56];
         if (record) plan->risky_rows = risky_rows;
         dtemp.no_risky = risky_rows == 0;
+    }
+    {
+        // Pack B when the dense bin reuses its entries many times and every
+        // value fits beside the column bits.
+        int32_t cbits = 0;
+        if (replay) {
+            cbits = plan->pack_cbits;
+        } else if (pack_cand && counts[kBinDense] > 0 && flops_total >= kPackReuse * B.nnz) {
+            uint64_t bmax = 1;
+            if (!Bm->ones) memcpy(&bmax, (int32_t *)h->h_pinned + 58, sizeof(uint64_t));
+            const int32_t cb = 32 - __builtin_clz((uint32_t)(B.cols - 1));
+            if (cb < 32 && bmax < (1ull << (32 - cb))) cbits = cb;
+        }
+        if (cbits > 0) {
+            void *p = nullptr;
+            if (dev_alloc(h, &p, 4 * B.nnz) == RMCM_OK) {
+                dtemp.pk = (const uint32_t *)p;
+                dtemp.cbits = cbits;
+                dtemp.pk_mem = p;
+                dtemp.pk_bytes = 4 * B.nnz;
+                k_pack_banked<<<grid_for(h, B.rows * 32, 256, 8), 256, 0, s>>>(B, cbits, (uint32_t *)p, h->d_status);
+                h->launches++;
+                RMCM_CUDA(h, cudaGetLastError());
+            } else if (replay) {
+                return set_error(h, RMCM_ENOMEM, "replay: packed copy of B could not be allocated");
+            } else {
+                h->last_error.clear();
+                cbits = 0;
+            }
+        }
+        if (record) plan->pack_cbits = cbits;
     }
     // Dense rows with far more products than a fair share of the device are
     // split over several CTAs (k_dense_split).
@@ -2517,6 +2675,9 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         rsplit.active = false;
     };
     auto drop_temp = [&]() {
+        if (dtemp.pk_mem) dev_free(h, dtemp.pk_mem, dtemp.pk_bytes);
+        dtemp.pk_mem = nullptr;
+        dtemp.pk = nullptr;
         if (dtemp.active) dev_free(h, dtemp.col, dtemp.bytes);
         if (dtemp.split) dev_free(h, dtemp.split_mem, dtemp.split_bytes);
         dtemp.active = false;

@@ -560,3 +560,64 @@ def test_matrices_of_one_handle_feed_another_after_synchronize(native, engine):
         m.free()
     loader.close()
     hg.close()
+
+
+def _heavy_reuse(rng, m, k, n, big=None):
+    """A (m x k) with every row long, B (k x n) rows of 40..n entries: the
+    product has hundreds of multiply-adds per entry of B (B is packed for the
+    dense bin).  ``big``: one entry per B row set to this value."""
+    A = _random_csr(rng, m, k, rng.integers(k // 2, k + 1, m), vmax=5)
+    B = _random_csr(rng, k, n, rng.integers(40, n + 1, k), vmax=5).tocsr()
+    if big is not None:
+        B.data[B.indptr[:-1][np.diff(B.indptr) > 0]] = big
+    return A, B
+
+
+@pytest.mark.parametrize("n", [1500, 2047, 2048, 2049])
+def test_packed_b_for_heavy_reuse(native, engine, n):
+    """Dense rows whose B entries are reused many times read a packed copy of
+    B ((value << column bits) | column, rows reordered by shared-memory bank);
+    column counts at the edges of the column bits."""
+    rng = np.random.default_rng(40 + n)
+    A, B = _heavy_reuse(rng, 300, 60, n)
+    for vt in (native.VAL_U32, native.VAL_U64):
+        _check_product(native, engine, A, B, vt)
+
+
+def test_values_too_large_to_pack(native, engine):
+    """A B value at 2^21 + 5 does not fit beside 11 column bits: B stays
+    unpacked and the product is still exact."""
+    rng = np.random.default_rng(44)
+    A, B = _heavy_reuse(rng, 300, 60, 1500, big=(1 << 21) + 5)
+    A.data[:] = 1
+    _check_product(native, engine, A, B, native.VAL_U32)
+
+
+def test_packed_b_replays_in_a_batch(native):
+    """A meta-path whose product packs B gives the same (nnz, digest) when
+    replayed from a batch's CUDA graph."""
+    rng = np.random.default_rng(45)
+    nx, ny, nz = 400, 60, 1500
+    xs = np.repeat(np.arange(nx), 45)
+    xy = rng.integers(0, ny, xs.size)
+    src01, dst01 = synth.dedup_pairs_keep_order(xs, xy, ny)
+    ys = np.repeat(np.arange(ny), 700)
+    yz = rng.integers(0, nz, ys.size)
+    src12, dst12 = synth.dedup_pairs_keep_order(ys, yz, nz)
+    g = synth.SyntheticHIN("reuse", [nx, ny, nz], [synth.Relation(0, 1, 0, 1, src01, dst01),
+                                                   synth.Relation(1, 2, 2, 3, src12, dst12)])
+    eng = native.Engine(device=0)
+    hg = native.HeteroGraph.from_synthetic(eng, g)
+    paths = ["0-0-1-2-2", "2-3-1-1-0-0-1-2-2"]
+    plain = []
+    for mp in paths:
+        C, _, _ = eng.run_metapath(hg, mp)
+        plain.append(eng.digest(C))
+        C.free()
+    b = eng.batch(hg, paths, lanes=2)
+    for _ in range(2):
+        nnz, dig, _ = b.run()
+        assert [(int(a), int(x)) for a, x in zip(nnz, dig)] == plain
+    b.free()
+    hg.close()
+    eng.close()
