@@ -371,15 +371,26 @@ __global__ void k_rowsum(DevCsr M, uint64_t *out) {
 // then touch each bank at most twice (once per group they straddle), where
 // the sorted order puts several columns of a sparse row on one bank.  Ranks
 // within a bank follow the sorted order, so the layout is deterministic.
-__global__ void __launch_bounds__(256) k_pack_banked(DevCsr B, int32_t cbits, uint32_t *pk, int *st) {
-    __shared__ int32_t s_cnt[8][32];
+// An entry's position is start[rank] + (banks below its own in group rank),
+// from per-rank tables (group masks and starts) when no bank holds more than
+// kPackRanks entries of the row, else from the bank totals directly.
+constexpr int kPackWarps = 4;
+constexpr int kPackRanks = 1024;
+
+__global__ void __launch_bounds__(kPackWarps * 32) k_pack_banked(DevCsr B, int32_t cbits, uint32_t *pk, int *st) {
+    __shared__ int32_t s_cnt[kPackWarps][32];
+    __shared__ uint32_t s_mask[kPackWarps][kPackRanks];   // banks with more than r entries
+    __shared__ int32_t s_start[kPackWarps][kPackRanks];   // first position of group r
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int32_t *cnt = s_cnt[warp];
+    uint32_t *gmask = s_mask[warp];
+    int32_t *gstart = s_start[warp];
     const uint32_t *bv = (const uint32_t *)B.val;
     const unsigned lt_mask = (1u << lane) - 1u;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < B.rows; r += nwarps) {
         const int64_t q0 = B.rowptr[r], q1 = B.rowptr[r + 1];
+        if (q0 == q1) continue;
         cnt[lane] = 0;
         __syncwarp();
         for (int64_t q = q0 + lane; q < q1; q += 32) atomicAdd(&cnt[B.col[q] & 31], 1);
@@ -387,6 +398,19 @@ __global__ void __launch_bounds__(256) k_pack_banked(DevCsr B, int32_t cbits, ui
         const int32_t total = cnt[lane];   // entries of bank `lane`
         __syncwarp();
         cnt[lane] = 0;                     // running rank per bank
+        const int32_t max_total = __reduce_max_sync(kFull, total);
+        const bool tab = max_total <= kPackRanks;
+        if (tab) {
+            int32_t run = 0;
+            for (int32_t g = 0; g < max_total; g++) {
+                const uint32_t m = __ballot_sync(kFull, total > g);
+                if (lane == 0) {
+                    gmask[g] = m;
+                    gstart[g] = run;
+                }
+                run += __popc(m);
+            }
+        }
         __syncwarp();
         for (int64_t base = q0; base < q1; base += 32) {
             const int64_t q = base + lane;
@@ -398,13 +422,17 @@ __global__ void __launch_bounds__(256) k_pack_banked(DevCsr B, int32_t cbits, ui
             __syncwarp();
             if (ok && lane == 31 - __clz(peers)) cnt[bank] += __popc(peers);
             __syncwarp();
-            // entries before (rank, bank): min(total_b, rank) of every bank,
-            // plus one of each lower bank that reaches this rank
             int32_t pos = 0;
+            if (tab) {
+                if (ok) pos = gstart[rank] + __popc(gmask[rank] & ((1u << bank) - 1u));
+            } else {
+                // entries before (rank, bank): min(total_b, rank) of every
+                // bank, plus one of each lower bank that reaches this rank
 #pragma unroll 8
-            for (int b = 0; b < 32; b++) {
-                const int32_t t = __shfl_sync(kFull, total, b);
-                pos += min(t, rank) + ((b < bank && t > rank) ? 1 : 0);
+                for (int b = 0; b < 32; b++) {
+                    const int32_t t = __shfl_sync(kFull, total, b);
+                    pos += min(t, rank) + ((b < bank && t > rank) ? 1 : 0);
+                }
             }
             if (ok) {
                 const uint32_t x = bv[q];
@@ -957,6 +985,96 @@ __device__ __forceinline__ void stage_full_rows(ChunkStage<V> &sg, const DevCsr 
         }
     }
     stage_scan<NT>(len, sg.pre, sg.warp_tot);
+}
+
+// stage_full_rows that also lists the entries whose B rows have at least
+// kLongRow positions (sg.llist / sg.nlong, sg.ctr zeroed): their length in
+// the flattened stream is 0, stream_long_fast takes them a warp at a time.
+// One entry per thread (NT == kChunk).
+template <int NT, typename V, bool NUMERIC>
+__device__ __forceinline__ void stage_rows_split(ChunkStage<V> &sg, const DevCsr A, const DevCsr B, int64_t k0,
+                                                 int cnt) {
+    static_assert(kChunk == NT, "one A entry per thread");
+    constexpr int NW = NT / 32;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    int64_t len[1] = {0};
+    bool lng = false;
+    if (t < cnt) {
+        const int32_t a = A.col[k0 + t];
+        const int64_t b0 = B.rowptr[a];
+        const int64_t L = B.rowptr[a + 1] - b0;
+        sg.bs[t] = b0;
+        sg.len[t] = (int32_t)L;
+        if (NUMERIC) sg.va[t] = ((const V *)A.val)[k0 + t];
+        lng = L >= kLongRow;
+        len[0] = lng ? 0 : L;
+    }
+    const unsigned lb = __ballot_sync(kFull, lng);
+    if (lane == 0) sg.wl[warp] = __popc(lb);
+    if (t == 0) sg.ctr = 0;
+    stage_scan<NT>(len, sg.pre, sg.warp_tot);
+    int pl = 0, tl = 0;
+#pragma unroll
+    for (int w = 0; w < NW; w++) {
+        const int x = sg.wl[w];
+        if (w < warp) pl += x;
+        tl += x;
+    }
+    if (lng) sg.llist[pl + __popc(lb & ((1u << lane) - 1u))] = t;
+    if (t == 0) sg.nlong = tl;
+    __syncthreads();
+}
+
+// Products of the listed long entries: a warp per entry (taken from sg.ctr),
+// whole blocks of 128 positions unpredicated, the rest once with predicates;
+// visit(col, product).  CHECKED records overflowing products in ovf.
+template <typename V, bool NUMERIC, bool CHECKED, typename Visit>
+__device__ __forceinline__ void stream_long_fast(ChunkStage<V> &sg, int cnt, const DevCsr B, bool &ovf,
+                                                 Visit visit) {
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        int i = 0;
+        if (lane == 0) i = atomicAdd(&sg.ctr, 1);
+        i = __shfl_sync(kFull, i, 0);
+        if (i >= cnt) break;
+        const int t = sg.llist[i];
+        const int32_t L = sg.len[t];
+        const int64_t q0 = sg.bs[t] + lane;
+        const int32_t *pc = B.col + q0;
+        const V *pv = (const V *)B.val + q0;
+        const V a = NUMERIC ? sg.va[t] : (V)0;
+        auto prod = [&](V b) -> V {
+            if (!NUMERIC) return (V)0;
+            if (CHECKED) return mul_chk(a, b, ovf);
+            return (V)(a * b);
+        };
+        for (int32_t nb = L >> 7; nb > 0; nb--, pc += 128, pv += 128) {
+            int32_t c[4];
+            V v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                c[u] = __ldg(pc + 32 * u);
+                v[u] = NUMERIC ? __ldg(pv + 32 * u) : (V)0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) visit(c[u], prod(v[u]));
+        }
+        const int32_t rest = (L & 127) - lane;
+        int32_t c[4];
+        V v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            c[u] = 0;
+            v[u] = 0;
+            if (32 * u < rest) {
+                c[u] = __ldg(pc + 32 * u);
+                if (NUMERIC) v[u] = __ldg(pv + 32 * u);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (32 * u < rest) visit(c[u], prod(v[u]));
+    }
 }
 
 template <typename V, bool NUMERIC, int S, int NT>
@@ -1624,7 +1742,8 @@ __global__ void __launch_bounds__(kRankThreads) k_rank(DevCsr A, DevCsr B, DevCs
         auto set_bit = [&](int32_t c, V) { atomicOr(bits + (c >> 5), 1u << (c & 31)); };
         for (int64_t k0 = a0; k0 < a1; k0 += kChunk) {
             const int n = (int)(a1 - k0 < (int64_t)kChunk ? a1 - k0 : (int64_t)kChunk);
-            stage_full_rows<NT, V, false>(sg, A, B, k0, n);
+            stage_rows_split<NT, V, false>(sg, A, B, k0, n);
+            if (sg.nlong) stream_long_fast<V, false, false>(sg, sg.nlong, B, ovf, set_bit);
             stream_chunk<NT, V, false>(sg, n, B, false, ovf, set_bit);
             __syncthreads();
         }
@@ -1681,22 +1800,32 @@ __global__ void __launch_bounds__(kRankThreads) k_rank(DevCsr A, DevCsr B, DevCs
         __syncthreads();
         // values: every product lands on its column's rank
         V *vals = (V *)C.val + base;
-        auto add_val = [&](int32_t c, V p) {
+        auto rank_of = [&](int32_t c) -> int64_t {
             const int w = c >> 5;
-            const int64_t pos = (int64_t)bpre[w >> 5] + wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u));
+            return (int64_t)bpre[w >> 5] + wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u));
+        };
+        auto add_plain = [&](int32_t c, V p) {
+            const int64_t pos = rank_of(c);
+            if (pos < rlen) atomicAdd((AtomV *)(vals + pos), (AtomV)p);
+        };
+        auto add_chk = [&](int32_t c, V p) {
+            const int64_t pos = rank_of(c);
             if (pos < rlen) {
-                if (checked) {
-                    const AtomV old = atomicAdd((AtomV *)(vals + pos), (AtomV)p);
-                    ovf |= old > (AtomV)~(AtomV)0 - (AtomV)p;
-                } else {
-                    atomicAdd((AtomV *)(vals + pos), (AtomV)p);
-                }
+                const AtomV old = atomicAdd((AtomV *)(vals + pos), (AtomV)p);
+                ovf |= old > (AtomV)~(AtomV)0 - (AtomV)p;
             }
         };
+        // the overflow test is chosen once per row, not per product
         for (int64_t k0 = a0; k0 < a1; k0 += kChunk) {
             const int n = (int)(a1 - k0 < (int64_t)kChunk ? a1 - k0 : (int64_t)kChunk);
-            stage_full_rows<NT, V, true>(sg, A, B, k0, n);
-            stream_chunk<NT, V, true>(sg, n, B, checked, ovf, add_val);
+            stage_rows_split<NT, V, true>(sg, A, B, k0, n);
+            if (checked) {
+                if (sg.nlong) stream_long_fast<V, true, true>(sg, sg.nlong, B, ovf, add_chk);
+                stream_chunk<NT, V, true>(sg, n, B, true, ovf, add_chk);
+            } else {
+                if (sg.nlong) stream_long_fast<V, true, false>(sg, sg.nlong, B, ovf, add_plain);
+                stream_chunk<NT, V, true>(sg, n, B, false, ovf, add_plain);
+            }
             __syncthreads();
         }
 
@@ -1750,7 +1879,8 @@ __global__ void __launch_bounds__(kRankThreads) k_rank_split_sym(DevCsr A, DevCs
         auto set_bit = [&](int32_t c, V) { atomicOr(bits + (c >> 5), 1u << (c & 31)); };
         for (int64_t k0 = ka; k0 < kb; k0 += kChunk) {
             const int n = (int)(kb - k0 < (int64_t)kChunk ? kb - k0 : (int64_t)kChunk);
-            stage_full_rows<NT, V, false>(sg, A, B, k0, n);
+            stage_rows_split<NT, V, false>(sg, A, B, k0, n);
+            if (sg.nlong) stream_long_fast<V, false, false>(sg, sg.nlong, B, ovf, set_bit);
             stream_chunk<NT, V, false>(sg, n, B, false, ovf, set_bit);
             __syncthreads();
         }
@@ -1846,22 +1976,31 @@ __global__ void __launch_bounds__(kRankThreads) k_rank_split_val(DevCsr A, DevCs
         const int64_t base = C.rowptr[r];
         const int64_t rlen = C.rowptr[r + 1] - base;
         V *vals = (V *)C.val + base;
-        auto add_val = [&](int32_t c, V p) {
+        auto rank_of = [&](int32_t c) -> int64_t {
             const int w = c >> 5;
-            const int64_t pos = (int64_t)pre[w] + __popc(g[w] & ((1u << (c & 31)) - 1u));
+            return (int64_t)pre[w] + __popc(g[w] & ((1u << (c & 31)) - 1u));
+        };
+        auto add_plain = [&](int32_t c, V p) {
+            const int64_t pos = rank_of(c);
+            if (pos < rlen) atomicAdd((AtomV *)(vals + pos), (AtomV)p);
+        };
+        auto add_chk = [&](int32_t c, V p) {
+            const int64_t pos = rank_of(c);
             if (pos < rlen) {
-                if (checked) {
-                    const AtomV old = atomicAdd((AtomV *)(vals + pos), (AtomV)p);
-                    ovf |= old > (AtomV)~(AtomV)0 - (AtomV)p;
-                } else {
-                    atomicAdd((AtomV *)(vals + pos), (AtomV)p);
-                }
+                const AtomV old = atomicAdd((AtomV *)(vals + pos), (AtomV)p);
+                ovf |= old > (AtomV)~(AtomV)0 - (AtomV)p;
             }
         };
         for (int64_t k0 = ka; k0 < kb; k0 += kChunk) {
             const int n = (int)(kb - k0 < (int64_t)kChunk ? kb - k0 : (int64_t)kChunk);
-            stage_full_rows<NT, V, true>(sg, A, B, k0, n);
-            stream_chunk<NT, V, true>(sg, n, B, checked, ovf, add_val);
+            stage_rows_split<NT, V, true>(sg, A, B, k0, n);
+            if (checked) {
+                if (sg.nlong) stream_long_fast<V, true, true>(sg, sg.nlong, B, ovf, add_chk);
+                stream_chunk<NT, V, true>(sg, n, B, true, ovf, add_chk);
+            } else {
+                if (sg.nlong) stream_long_fast<V, true, false>(sg, sg.nlong, B, ovf, add_plain);
+                stream_chunk<NT, V, true>(sg, n, B, false, ovf, add_plain);
+            }
             __syncthreads();
         }
     }
@@ -2528,7 +2667,8 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
                 dtemp.cbits = cbits;
                 dtemp.pk_mem = p;
                 dtemp.pk_bytes = 4 * B.nnz;
-                k_pack_banked<<<grid_for(h, B.rows * 32, 256, 8), 256, 0, s>>>(B, cbits, (uint32_t *)p, h->d_status);
+                k_pack_banked<<<grid_for(h, B.rows * 32, kPackWarps * 32, 6), kPackWarps * 32, 0, s>>>(
+                    B, cbits, (uint32_t *)p, h->d_status);
                 h->launches++;
                 RMCM_CUDA(h, cudaGetLastError());
             } else if (replay) {
