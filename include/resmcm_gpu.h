@@ -104,7 +104,7 @@ typedef struct rmcm_product_stats {
     int64_t bytes_a, bytes_b_touched, bytes_c;   /* level 2 only */
     double analyze_ms, symbolic_ms, numeric_ms;  /* CUDA-event times on the handle's stream */
     int32_t valtype;
-    int32_t bin_rows[7];                /* rows per bin: tiny, hash512, hash2k, hash8k, dense, rank, micro */
+    int32_t bin_rows[8];                /* rows per bin: tiny, hash512, hash2k, hash8k, dense, rank, micro, warp */
 } rmcm_product_stats;
 
 /* ---- handle -------------------------------------------------------------- */
@@ -266,14 +266,19 @@ RMCM_API int32_t rmcm_estimate_metapath(rmcm_handle *h, rmcm_graph *g, const cha
  *                    dense / rank bins (32 .. 1048576)
  *   dense_ratio      a row whose products x dense_ratio reach the output
  *                    width goes to the dense bin (>= 1)
+ *   warp_max_flops   rows of an output at most 2048 columns wide with more
+ *                    products than the short-row bins take and at most this
+ *                    many get a warp each with a window of its own
+ *                    (0 .. 65536; 0 = none)
  *   hash_load        hash tables get at least min(products, width) / load
  *                    slots (0.1 .. 0.75)
- * Defaults: 32, 4096, 16, 0.5.  A batch keeps the values it was created with. */
+ * Defaults: 32, 4096, 16, 2048, 0.5.  A batch keeps the values it was created
+ * with. */
 typedef struct rmcm_tuning {
     int32_t threads_per_row;
     int32_t hash_max_flops;
     int32_t dense_ratio;
-    int32_t reserved;
+    int32_t warp_max_flops;
     double hash_load;
 } rmcm_tuning;
 RMCM_API int32_t rmcm_set_tuning(rmcm_handle *h, const rmcm_tuning *t);

@@ -61,10 +61,10 @@ class Timings(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("threads_per_row", C.c_int32), ("hash_max_flops", C.c_int32), ("dense_ratio", C.c_int32),
-                ("reserved", C.c_int32), ("hash_load", C.c_double)]
+                ("warp_max_flops", C.c_int32), ("hash_load", C.c_double)]
 
     def as_dict(self) -> dict:
-        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class ServerOpts(C.Structure):
@@ -99,7 +99,7 @@ class ProductStats(C.Structure):
                 ("touched_rows", C.c_int64), ("touched_nnz", C.c_int64),
                 ("bytes_a", C.c_int64), ("bytes_b_touched", C.c_int64), ("bytes_c", C.c_int64),
                 ("analyze_ms", C.c_double), ("symbolic_ms", C.c_double), ("numeric_ms", C.c_double),
-                ("valtype", C.c_int32), ("bin_rows", C.c_int32 * 7)]
+                ("valtype", C.c_int32), ("bin_rows", C.c_int32 * 8)]
 
     def as_dict(self) -> dict:
         d = {f: getattr(self, f) for f, _ in self._fields_ if f != "bin_rows"}
@@ -627,14 +627,14 @@ class Engine:
         return t.as_dict()
 
     def set_tuning(self, **kw):
-        """Change some of threads_per_row, hash_max_flops, dense_ratio, hash_load."""
+        """Change some of threads_per_row, hash_max_flops, dense_ratio, warp_max_flops, hash_load."""
         cur = self.get_tuning()
         bad = set(kw) - set(cur)
         if bad:
             raise ValueError(f"unknown tunables {sorted(bad)}")
         cur.update(kw)
-        t = Tuning(int(cur["threads_per_row"]), int(cur["hash_max_flops"]), int(cur["dense_ratio"]), 0,
-                   float(cur["hash_load"]))
+        t = Tuning(int(cur["threads_per_row"]), int(cur["hash_max_flops"]), int(cur["dense_ratio"]),
+                   int(cur["warp_max_flops"]), float(cur["hash_load"]))
         self._check(lib().rmcm_set_tuning(self._h, C.byref(t)))
 
     def batch(self, graph: HeteroGraph, paths: list, lanes: int = 8) -> Batch:

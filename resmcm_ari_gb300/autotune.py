@@ -6,13 +6,15 @@ The search space is the row-binning tunables of a handle (rmcm_set_tuning):
   dense / rank bins: {32, 128, 512, 2048, 8192}
 * ``hash_load``       hash-table load factor bound: {0.5, 0.7}
 * ``threads_per_row`` threads on one short row (<= 32 products): {1, 4, 32, 128}
+* ``warp_max_flops``  largest row (products) of an output at most 2048
+  columns wide that gets a warp of its own: {0, 512, 2048, 8192}
 
 Each candidate is measured the way the meta-paths are served: recorded as a
 batch (rmcm_batch_create) and replayed as one CUDA graph, best of ``reps``
 replays.  Every candidate's per-path (nnz, digest) must equal the default
 tuning's — tunables move rows between kernels, never change a result — and a
 mismatch raises.  ``coordinate`` mode sweeps one tunable at a time from the
-current best (5 + 2 + 4 candidates); ``grid`` mode tries all 40.
+current best (5 + 2 + 4 + 4 candidates); ``grid`` mode tries all 160.
 """
 from __future__ import annotations
 
@@ -23,6 +25,7 @@ SPACE = {
     "hash_max_flops": [32, 128, 512, 2048, 8192],
     "hash_load": [0.5, 0.7],
     "threads_per_row": [1, 4, 32, 128],
+    "warp_max_flops": [0, 512, 2048, 8192],
 }
 
 

@@ -1684,7 +1684,10 @@ RMCM_API int32_t rmcm_set_tuning(rmcm_handle *h, const rmcm_tuning *t) {
     if (t->dense_ratio < 1) return set_error(h, RMCM_EINVAL, "tuning: dense_ratio must be >= 1");
     if (!(t->hash_load >= 0.1 && t->hash_load <= 0.75))
         return set_error(h, RMCM_EINVAL, "tuning: hash_load must be in 0.1 .. 0.75");
+    if (t->warp_max_flops < 0 || t->warp_max_flops > 65536)
+        return set_error(h, RMCM_EINVAL, "tuning: warp_max_flops must be in 0 .. 65536");
     h->tune.threads_per_row = g;
+    h->tune.warp_max_flops = t->warp_max_flops;
     h->tune.hash_max_flops = t->hash_max_flops;
     h->tune.dense_ratio = t->dense_ratio;
     h->tune.hash_load = t->hash_load;
@@ -1696,7 +1699,7 @@ RMCM_API int32_t rmcm_get_tuning(const rmcm_handle *h, rmcm_tuning *t) {
     t->threads_per_row = h->tune.threads_per_row;
     t->hash_max_flops = h->tune.hash_max_flops;
     t->dense_ratio = h->tune.dense_ratio;
-    t->reserved = 0;
+    t->warp_max_flops = h->tune.warp_max_flops;
     t->hash_load = h->tune.hash_load;
     return RMCM_OK;
 }

@@ -44,7 +44,8 @@ enum Bin {
     kBinDense = 4,     // windowed dense accumulator (presence + counters) in shared memory
     kBinRank = 5,      // whole-row bitmap in shared memory, counts by rank with global atomics
     kBinMicro = 6,     // flops <= G (1, 2, 4, 8 or 16): G lanes per row, one product per lane
-    kNumBins = 7
+    kBinWarp = 7,      // output width <= 2048, few products: a warp per row with its own window
+    kNumBins = 8
 };
 
 // Tunables of the SpGEMM row binning (the autotuner searches these).
@@ -56,6 +57,7 @@ struct Tuning {
     int32_t threads_per_row = 32;
     int32_t hash_max_flops = 4096;  // rows above go to the dense / rank bins
     int32_t dense_ratio = 16;       // dense when flops * dense_ratio >= cols (and one window covers cols)
+    int32_t warp_max_flops = 2048;  // output width <= 2048 and at most this many flops: warp bin (0: none)
     double hash_load = 0.5;         // hash table load factor bound: slots >= min(f, cols) / load, load <= 0.75
     bool dense_single_pass = true;  // dense rows in one window: one pass into a padded temporary
     int64_t dense_temp_max_bytes = 8LL << 30;

@@ -99,6 +99,10 @@ __device__ __forceinline__ int32_t warp_min(int32_t v) {
 // 1. analysis and binning
 // ------------------------------------------------------------------------
 
+// Warp bin: output rows of at most kWarpCols columns, kWarpWarps rows per CTA.
+constexpr int kWarpCols = 2048;
+constexpr int kWarpWarps = 4;
+
 struct BinParams {
     int64_t dense_win;      // columns one numeric dense window covers
     int32_t hash_max;       // flops above -> dense or rank
@@ -106,6 +110,7 @@ struct BinParams {
     int32_t micro_max;      // flops <= micro_max -> micro bin (0: none)
     int32_t tiny_max;       // flops <= tiny_max -> tiny bin (32, or 0: none)
     int32_t inv_load_q8;    // 256 / hash load factor, rounded up
+    int32_t warp_max;       // flops <= warp_max and cols <= kWarpCols -> warp bin (0: none)
 };
 
 // Widest output row the rank bin holds in shared memory (bitmap + prefixes).
@@ -115,6 +120,7 @@ __device__ __forceinline__ int classify(int64_t f, int64_t ncols, const BinParam
     if (f == 0) return kEmptyBin;
     if (f <= bp.micro_max) return kBinMicro;
     if (f <= bp.tiny_max) return kBinTiny;
+    if (ncols <= kWarpCols && f <= bp.warp_max) return kBinWarp;
     const bool one_window = ncols <= bp.dense_win;
     if (f > bp.hash_max) return (!one_window && ncols <= kRankCols) ? kBinRank : kBinDense;
     if (one_window && f * (int64_t)bp.dense_ratio >= ncols) return kBinDense;
@@ -575,6 +581,160 @@ __global__ void __launch_bounds__(256) k_tiny(DevCsr A, DevCsr B, DevCsr C, cons
                 }
             }
         }
+    }
+    if (__any_sync(kFull, ovf) && lane == 0) raise_status(st, kOverflow);
+}
+
+// Warp bin: rows whose output has at most kWarpCols columns and whose
+// products are few (bounded by a tunable): a warp per row with a window of
+// its own in shared memory (presence bytes; counters in the numeric pass), so
+// a CTA carries several rows at once with no block barrier.  Per chunk of 32
+// A entries the warp scans their B row lengths and lane l takes the
+// flattened products l, l + 32, ... (four loads in flight); every product
+// marks its column's 32-column group in a per-lane mask, and the output pass
+// visits only the groups the row touched, 32 columns per ballot, writing the
+// columns in order (coalesced) and clearing the window behind it.
+template <typename V, bool NUMERIC, bool CHECKED, typename Visit>
+__device__ __forceinline__ void warp_row_products(const DevCsr A, const DevCsr B, int64_t a0, int64_t a1,
+                                                  int32_t *wpre, int64_t *wbs, V *wva, bool &ovf, Visit visit) {
+    const int lane = threadIdx.x & 31;
+    const V *Aval = (const V *)A.val;
+    const V *Bval = (const V *)B.val;
+    for (int64_t k0 = a0; k0 < a1; k0 += 32) {
+        const int64_t k = k0 + lane;
+        int32_t len = 0;
+        int64_t bs = 0;
+        V va = 0;
+        if (k < a1) {
+            const int32_t a = A.col[k];
+            bs = B.rowptr[a];
+            len = (int32_t)(B.rowptr[a + 1] - bs);
+            if (NUMERIC) va = Aval[k];
+        }
+        int32_t incl = len;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int32_t o = __shfl_up_sync(kFull, incl, d);
+            if (lane >= d) incl += o;
+        }
+        const int32_t tot = __shfl_sync(kFull, incl, 31);
+        __syncwarp();   // the previous chunk is done with the staging arrays
+        wpre[lane] = incl - len;
+        wbs[lane] = bs;
+        if (NUMERIC) wva[lane] = va;
+        if (lane == 31) wpre[32] = tot;
+        __syncwarp();
+        int e = 0;
+        for (int32_t p0 = 0; p0 < tot; p0 += 128) {
+            int32_t c[4];
+            V v[4], av[4];
+            bool ok[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int32_t p = p0 + 32 * u + lane;
+                ok[u] = p < tot;
+                c[u] = 0;
+                v[u] = 0;
+                av[u] = 0;
+                if (ok[u]) {
+                    while (wpre[e + 1] <= p) e++;
+                    const int64_t q = wbs[e] + (p - wpre[e]);
+                    c[u] = __ldg(B.col + q);
+                    if (NUMERIC) {
+                        v[u] = __ldg(Bval + q);
+                        av[u] = wva[e];
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                if (!ok[u]) continue;
+                V prod = 0;
+                if (NUMERIC) prod = CHECKED ? mul_chk(av[u], v[u], ovf) : (V)(av[u] * v[u]);
+                visit(c[u], prod);
+            }
+        }
+    }
+}
+
+template <typename V, bool NUMERIC>
+__global__ void __launch_bounds__(kWarpWarps * 32) k_warp(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows,
+                                                          int32_t nrows, int64_t *cnt, int *st,
+                                                          const uint8_t *bin_of) {
+    using AtomV = typename std::conditional<sizeof(V) == 4, unsigned int, unsigned long long>::type;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int32_t s_pre[kWarpWarps][33];
+    __shared__ int64_t s_bs[kWarpWarps][32];
+    __shared__ V s_va[kWarpWarps][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    constexpr int W = kWarpCols;
+    constexpr int64_t per_warp = W + (NUMERIC ? (int64_t)W * sizeof(V) : 0);
+    uint8_t *pres = smem + warp * per_warp;
+    V *acc = (V *)(pres + W);
+    for (int i = lane; i < (int)(per_warp / 16); i += 32) ((uint4 *)pres)[i] = make_uint4(0, 0, 0, 0);
+    __syncwarp();
+    bool ovf = false;
+    for (int64_t wi = (int64_t)blockIdx.x * kWarpWarps + warp; wi < nrows; wi += (int64_t)gridDim.x * kWarpWarps) {
+        const int32_t r = rows[wi];
+        const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
+        const bool checked = NUMERIC && (bin_of[r] & kRiskyBit) != 0;
+        uint32_t glo = 0, ghi = 0;   // 32-column groups this lane touched
+        auto mark = [&](int32_t c) {
+            pres[c] = 1;
+            const int g = c >> 5;
+            if (g < 32) glo |= 1u << g;
+            else ghi |= 1u << (g - 32);
+        };
+        if (!NUMERIC) {
+            warp_row_products<V, false, false>(A, B, a0, a1, s_pre[warp], s_bs[warp], s_va[warp], ovf,
+                                               [&](int32_t c, V) { mark(c); });
+        } else if (checked) {
+            warp_row_products<V, true, true>(A, B, a0, a1, s_pre[warp], s_bs[warp], s_va[warp], ovf,
+                                             [&](int32_t c, V p) {
+                                                 mark(c);
+                                                 add_shared_chk(acc + c, p, ovf);
+                                             });
+        } else {
+            warp_row_products<V, true, false>(A, B, a0, a1, s_pre[warp], s_bs[warp], s_va[warp], ovf,
+                                              [&](int32_t c, V p) {
+                                                  mark(c);
+                                                  atomicAdd((AtomV *)(acc + c), (AtomV)p);
+                                              });
+        }
+        glo = __reduce_or_sync(kFull, glo);
+        ghi = __reduce_or_sync(kFull, ghi);
+        __syncwarp();   // every product has landed in the window
+        const int64_t base = NUMERIC ? C.rowptr[r] : 0;
+        const int64_t rlen = NUMERIC ? C.rowptr[r + 1] - base : 0;
+        int64_t pos = 0;
+        for (int half = 0; half < 2; half++) {
+            uint32_t gm = half ? ghi : glo;
+            while (gm) {
+                const int g = __ffs(gm) - 1 + 32 * half;
+                gm &= gm - 1;
+                const int lc = g * 32 + lane;
+                const bool here = pres[lc] != 0;
+                const unsigned bits = __ballot_sync(kFull, here);
+                if (here) {
+                    if (NUMERIC) {
+                        const int64_t o = pos + __popc(bits & lt_mask);
+                        if (o < rlen) {
+                            C.col[base + o] = lc;
+                            ((V *)C.val)[base + o] = acc[lc];
+                        }
+                        acc[lc] = 0;
+                    }
+                    pres[lc] = 0;
+                }
+                pos += __popc(bits);
+            }
+        }
+        if (lane == 0) {
+            if (!NUMERIC) cnt[r] = pos;
+            else if (pos != rlen) raise_status(st, kInvariant);
+        }
+        __syncwarp();
     }
     if (__any_sync(kFull, ovf) && lane == 0) raise_status(st, kOverflow);
 }
@@ -2269,6 +2429,15 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
         off += n;
         if (n == 0) continue;
         switch (b) {
+            case kBinWarp: {
+                const int64_t sm = (int64_t)kWarpWarps * (kWarpCols + (NUMERIC ? (int64_t)kWarpCols * sizeof(V) : 0));
+                auto kern = k_warp<V, NUMERIC>;
+                RMCM_TRY(set_smem(h, kern, sm));
+                const int per_sm = std::max(1, occupancy(h, kern, kWarpWarps * 32, sm));
+                const int grid = grid_for(h, (int64_t)n * 32, kWarpWarps * 32, per_sm);
+                kern<<<grid, kWarpWarps * 32, sm, s>>>(A, B, C, list, n, cnt, st, bin_of);
+                break;
+            }
             case kBinTiny: {
                 const int grid = grid_for(h, (int64_t)n * 32, 256, 8);
                 k_tiny<V, NUMERIC><<<grid, 256, 0, s>>>(A, B, C, list, n, cnt, st);
@@ -2536,6 +2705,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         bp.micro_max = tpr < 32 ? tpr : 0;
         bp.tiny_max = tpr <= 32 ? 32 : 0;
         bp.inv_load_q8 = (int32_t)std::ceil(256.0 / h->tune.hash_load);
+        bp.warp_max = h->tune.warp_max_flops;
     }
     if (m > 0) {
         AnalyzeOut ao{flops, bin_of, small, small + 16, (unsigned long long *)(small + 32), small + 40,

@@ -151,8 +151,9 @@ def test_autotuner_keeps_results_and_picks_a_measured_best(native):
 
 
 def test_bad_tuning_is_rejected(native, engine):
-    for kw in ({"threads_per_row": 3}, {"hash_max_flops": 8}, {"hash_load": 0.9}, {"dense_ratio": 0}):
+    for kw in ({"threads_per_row": 3}, {"hash_max_flops": 8}, {"hash_load": 0.9}, {"dense_ratio": 0},
+               {"warp_max_flops": -1}, {"warp_max_flops": 70000}):
         with pytest.raises(native.RmcmError):
             engine.set_tuning(**kw)
     assert engine.get_tuning() == {"threads_per_row": 32, "hash_max_flops": 4096, "dense_ratio": 16,
-                                   "hash_load": 0.5}
+                                   "warp_max_flops": 2048, "hash_load": 0.5}

@@ -621,3 +621,50 @@ def test_packed_b_replays_in_a_batch(native):
     b.free()
     hg.close()
     eng.close()
+
+
+@pytest.mark.parametrize("n", [300, 2000, 2048, 2049])
+def test_warp_bin_rows(native, n):
+    """Rows of an output at most 2048 columns wide with 33..2048 products get
+    a warp each with its own window; equal to scipy in uint32 and uint64, and
+    to the same product with the warp bin turned off.  A 2049-column output
+    never uses it."""
+    rng = np.random.default_rng(50 + n)
+    m, k = 1500, 3000
+    A = _random_csr(rng, m, k, rng.integers(0, 24, m), vmax=5)
+    B = _random_csr(rng, k, n, rng.integers(0, min(n, 150), k), vmax=5)
+    for vt in (native.VAL_U32, native.VAL_U64):
+        eng = native.Engine(device=0)
+        _check_product(native, eng, A, B, vt)
+        eng.set_tuning(warp_max_flops=0)
+        _check_product(native, eng, A, B, vt)
+        eng.close()
+
+
+def test_warp_bin_risky_rows(native, engine):
+    """Rows whose count bound exceeds uint32 take the checked adds of the warp
+    bin: exact when no entry overflows, EOVERFLOW (and exact in uint64) when
+    one does."""
+    rng = np.random.default_rng(60)
+    m, k, n = 400, 800, 1000
+    A = _random_csr(rng, m, k, rng.integers(1, 20, m), vmax=1)
+    B = _random_csr(rng, k, n, rng.integers(50, 100, k), vmax=1).tocsr()
+    B.data[:] = rng.integers(1 << 26, 1 << 27, B.nnz)
+    _check_product(native, engine, A, B, native.VAL_U32)
+    # 33 products (warp bin) all on column 0 at 2^27: 33 * 2^27 > 2^32
+    A2 = A.tolil()
+    A2[0, :] = 0
+    A2[0, :33] = 1
+    A2 = A2.tocsr()
+    B2 = B.tolil()
+    B2[:33, :] = 0
+    B2[:33, 0] = 1 << 27
+    B2 = B2.tocsr()
+    B2.eliminate_zeros()
+    import ctypes
+    Am = engine.upload(A2.indptr, A2.indices, cols=k, val=A2.data.astype(np.uint64), valtype=native.VAL_U32)
+    Bm = engine.upload(B2.indptr, B2.indices, cols=n, val=B2.data.astype(np.uint64), valtype=native.VAL_U32)
+    h = ctypes.c_void_p()
+    assert native.lib().rmcm_spgemm(engine._h, Am._h, Bm._h, ctypes.byref(h)) == native.EOVERFLOW
+    native.lib().rmcm_mat_free(engine._h, h)
+    _check_product(native, engine, A2, B2, native.VAL_U64)
