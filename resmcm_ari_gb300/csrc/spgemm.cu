@@ -1679,7 +1679,7 @@ __global__ void __launch_bounds__(kSplitThreads) k_dense_split(DevCsr A, DevCsr 
                                                                int32_t max_slots, int32_t W,
                                                                unsigned long long *G, uint32_t *Gbits,
                                                                const uint8_t *bin_of, int *st, int32_t wc,
-                                                               bool pull_ok) {
+                                                               bool pull_ok, const uint32_t *pk, int32_t cbits) {
     constexpr int NT = kSplitThreads;
     constexpr int kPull = 4;   // register accumulators per thread: rows of up to 4 * NT columns
     static_assert(kChunk == NT, "one staged A entry per thread");
@@ -1692,7 +1692,8 @@ __global__ void __launch_bounds__(kSplitThreads) k_dense_split(DevCsr A, DevCsr 
     uint8_t *present = smem;
     V *acc = (V *)(PRES ? smem + (((size_t)W + 15) & ~(size_t)15) : smem);
     __shared__ ChunkStage<V> sg;
-    const int tid = threadIdx.x, lane = tid & 31;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
     const int ns = min(*nslots, max_slots);
     const int ntasks = task_start[ns];
     if (PRES)
@@ -1724,32 +1725,75 @@ __global__ void __launch_bounds__(kSplitThreads) k_dense_split(DevCsr A, DevCsr 
         for (int64_t k0 = ka; k0 < kb; k0 += kChunk) {
             const int n = (int)(kb - k0 < (int64_t)kChunk ? kb - k0 : (int64_t)kChunk);
             int64_t len1[1] = {0};
-            bool full = false;
+            bool full = false, lng = false;
             if (tid < n) {
                 const int32_t a = A.col[k0 + tid];
                 const int64_t b0 = B.rowptr[a];
                 const int64_t len = B.rowptr[a + 1] - b0;
                 full = pull_ok && len == wc;
+                lng = sizeof(V) == 4 && !full && len >= kLongRow;   // uint64: flattened stream only
                 sg.bs[tid] = b0;
                 sg.len[tid] = (int32_t)len;
                 sg.va[tid] = Aval[k0 + tid];
-                len1[0] = full ? 0 : len;
+                len1[0] = (full || lng) ? 0 : len;
             }
-            const unsigned fb = __ballot_sync(kFull, full);
-            if (lane == 0) sg.wf[tid >> 5] = __popc(fb);
+            // lists of full entries (register path) and long ones (a warp each)
+            const unsigned fb = __ballot_sync(kFull, full), lb = __ballot_sync(kFull, lng);
+            if (lane == 0) {
+                sg.wf[warp] = __popc(fb);
+                sg.wl[warp] = __popc(lb);
+            }
+            if (tid == 0) sg.ctr = 0;
             stage_scan<NT>(len1, sg.pre, sg.warp_tot);
-            int pf = 0, tf = 0;
+            int pf = 0, tf = 0, pl = 0, tl = 0;
             for (int w = 0; w < NT / 32; w++) {
-                if (w < (tid >> 5)) pf += sg.wf[w];
+                if (w < warp) {
+                    pf += sg.wf[w];
+                    pl += sg.wl[w];
+                }
                 tf += sg.wf[w];
+                tl += sg.wl[w];
             }
-            if (full) sg.flist[pf + __popc(fb & ((1u << lane) - 1u))] = tid;
+            if (full) sg.flist[pf + __popc(fb & lt_mask)] = tid;
+            if (lng) sg.llist[pl + __popc(lb & lt_mask)] = tid;
             __syncthreads();
-            stream_chunk<NT, V, true>(sg, n, B, checked, ovf, [&](int32_t c, V p) {
-                if (PRES) present[c] = 1;
-                if (checked) add_shared_chk(acc + c, p, ovf);
-                else atomicAdd((AtomV *)(acc + c), (AtomV)p);
-            });
+            // the row's overflow test is chosen here, not per product (uint64
+            // keeps the single flattened stream: the split costs it spills)
+            if constexpr (sizeof(V) == 8) {
+                stream_chunk<NT, V, true>(sg, n, B, checked, ovf, [&](int32_t c, V p) {
+                    if (PRES) present[c] = 1;
+                    if (checked) add_shared_chk(acc + c, p, ovf);
+                    else atomicAdd((AtomV *)(acc + c), (AtomV)p);
+                });
+            } else if (checked) {
+                auto vis = [&](int32_t c, V p) {
+                    if (PRES) present[c] = 1;
+                    add_shared_chk(acc + c, p, ovf);
+                };
+                if (tl) stream_long_fast<V, true, true>(sg, tl, B, ovf, vis);
+                stream_chunk<NT, V, true>(sg, n, B, true, ovf, vis);
+            } else {
+                bool done = false;
+                if constexpr (sizeof(V) == 4 && !PRES) {
+                    // uint32 counters alone: 32-bit shared addresses, packed B when given
+                    const uint32_t acc_s = (uint32_t)__cvta_generic_to_shared(acc);
+                    auto add = [&](int32_t c, V p) { red_shared_add(acc_s + (uint32_t)c * 4u, p); };
+                    if (tl) {
+                        if (pk) stream_long_packed(sg, tl, pk, cbits, add);
+                        else stream_long_fast<V, true, false>(sg, tl, B, ovf, add);
+                    }
+                    stream_chunk<NT, V, true>(sg, n, B, false, ovf, add);
+                    done = true;
+                }
+                if (!done) {
+                    auto vis = [&](int32_t c, V p) {
+                        if (PRES) present[c] = 1;
+                        atomicAdd((AtomV *)(acc + c), (AtomV)p);
+                    };
+                    if (tl) stream_long_fast<V, true, false>(sg, tl, B, ovf, vis);
+                    stream_chunk<NT, V, true>(sg, n, B, false, ovf, vis);
+                }
+            }
             for (int i0 = 0; i0 < tf; i0 += 4) {
                 pulled = true;
                 V bvals[4][kPull];
@@ -2557,7 +2601,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                             ks<<<(int)((int64_t)h->sm_count * sper), kSplitThreads, ssm, h->aux>>>(
                                 A, B, temp->perm, temp->row_of_slot, temp->parts, temp->task_start, temp->nslots,
                                 temp->max_slots, (int32_t)W, temp->G, temp->Gbits, bin_of, st, (int32_t)ncols,
-                                b_distinct && ncols <= 4 * kSplitThreads);
+                                b_distinct && ncols <= 4 * kSplitThreads, temp->pk, temp->cbits);
                             k_split_finish<V><<<temp->max_slots, kSplitThreads, 0, h->aux>>>(
                                 T, temp->perm, temp->row_of_slot, temp->nslots, temp->max_slots, ncols, (int32_t)W,
                                 temp->G, temp->Gbits, temp->stride, cnt, st);
