@@ -41,9 +41,55 @@ struct LevelArgs {
     int32_t i;              // level
     int32_t nj;             // number of j > i (len - 1 - i)
     int32_t jp;             // lanes per group (power of two >= nj, >= 1)
+    int32_t tile;           // rows a warp takes per step (1 .. 32)
     double dim_leaf;        // dim(vts[i+1]) = cols of M_i
     double dims[kMaxLen];   // dims[j] = cols of M_j
 };
+
+// prod over entries k = k0, k0 + G, ... < k1 of (1 - r_next[col_k][j]).
+// A lane with at least four entries keeps four independent partial products
+// (entries taken in turn) so four gathers and multiply chains are in flight,
+// combined in a fixed order ((p0 p1)(p2 p3)); a shorter run multiplies
+// serially (no combining multiplies).  Reproducible run to run.
+__device__ __forceinline__ double factor_product(const DevCsr &M, const double *r_next, int32_t len, int j,
+                                                 int64_t k0, int64_t k1, int G) {
+    int64_t k = k0;
+    if (k + 3 * (int64_t)G < k1) {
+        double p[4] = {1.0, 1.0, 1.0, 1.0};
+        for (; k + 3 * (int64_t)G < k1; k += 4 * (int64_t)G) {
+            int32_t v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] = M.col[k + u * G];
+            double r[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) r[u] = r_next[(int64_t)v[u] * len + j];
+#pragma unroll
+            for (int u = 0; u < 4; u++) p[u] = __dmul_rn(p[u], __dsub_rn(1.0, r[u]));
+        }
+        // the last 0..3 entries, into p[0], p[1], p[2] in turn
+#pragma unroll
+        for (int u = 0; u < 3; u++) {
+            if (k < k1) {
+                const double r = r_next[(int64_t)M.col[k] * len + j];
+                p[u] = __dmul_rn(p[u], __dsub_rn(1.0, r));
+                k += G;
+            }
+        }
+        return __dmul_rn(__dmul_rn(p[0], p[1]), __dmul_rn(p[2], p[3]));
+    }
+    double p = 1.0;
+    for (; k < k1; k += G) p = __dmul_rn(p, __dsub_rn(1.0, r_next[(int64_t)M.col[k] * len + j]));
+    return p;
+}
+
+// Rows per warp step: 32 when every warp of a full grid (blocks_cap CTAs)
+// still gets several steps, fewer for short matrices so that warps stay busy.
+inline int32_t level_tile(int64_t rows, int64_t blocks_cap) {
+    const int64_t warps = blocks_cap * (kEstThreads / 32);
+    int32_t t = 32;
+    while (t > 1 && rows < warps * t * 4) t >>= 1;
+    return t;
+}
 
 __global__ void __launch_bounds__(kEstThreads) k_res_level(DevCsr M, const double *r_next, double *r_cur,
                                                            LevelArgs la, double *partial, bool skip_long) {
@@ -55,32 +101,39 @@ __global__ void __launch_bounds__(kEstThreads) k_res_level(DevCsr M, const doubl
     const int j = la.i + 1 + jo;
     const double dimj = active_j ? la.dims[j] : 0.0;
     double term_sum = 0.0;                       // held by group-0 lanes
+    const int T = la.tile;                       // rows per warp step (1 .. 32)
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < M.rows; u += nwarps) {
-        const int64_t a0 = M.rowptr[u], a1 = M.rowptr[u + 1];
-        if (lane == 0) {
-            const double s = __ddiv_rn((double)(a1 - a0), la.dim_leaf);
-            r_cur[u * la.len + la.i] = s > 1.0 ? 1.0 : s;
+    for (int64_t t0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * T; t0 < M.rows;
+         t0 += nwarps * T) {
+        // r_ii of the tile's rows, a lane each (one division for T rows)
+        int64_t my_a0 = 0, my_len = 0;
+        if (lane < T && t0 + lane < M.rows) {
+            const int64_t ul = t0 + lane;
+            my_a0 = M.rowptr[ul];
+            my_len = M.rowptr[ul + 1] - my_a0;
+            const double s = __ddiv_rn((double)my_len, la.dim_leaf);
+            r_cur[ul * la.len + la.i] = s > 1.0 ? 1.0 : s;
         }
         if (la.nj == 0) continue;
-        if (skip_long && a1 - a0 > kEstLongRow) continue;   // a CTA of k_res_long takes it
-        double prod = 1.0;
-        if (active_j) {
-            for (int64_t k = a0 + g; k < a1; k += G) {
-                const int32_t v = M.col[k];
-                const double rv = r_next[(int64_t)v * la.len + j];
-                prod = __dmul_rn(prod, __dsub_rn(1.0, rv));
+        const int nrow = M.rows - t0 < (int64_t)T ? (int)(M.rows - t0) : T;
+        for (int t = 0; t < nrow; t++) {
+            const int64_t u = t0 + t;
+            const int64_t a0 = __shfl_sync(kFull, my_a0, t), rl = __shfl_sync(kFull, my_len, t);
+            if (skip_long && rl > kEstLongRow) continue;   // a CTA of k_res_long takes it
+            double prod = 1.0;
+            if (active_j) prod = factor_product(M, r_next, la.len, j, a0 + g, a0 + rl, G);
+            // combine the group products (fixed butterfly order); groups past
+            // the row's entries hold exactly 1.0, so those steps are skipped
+            const int ng = rl < (int64_t)G ? (int)rl : G;
+            for (int d = la.jp; d < 32 && d < la.jp * ng; d <<= 1) {
+                const double o = __shfl_xor_sync(kFull, prod, d);
+                prod = __dmul_rn(prod, o);
             }
-        }
-        // combine the G group products (fixed butterfly order)
-        for (int d = la.jp; d < 32; d <<= 1) {
-            const double o = __shfl_xor_sync(kFull, prod, d);
-            prod = __dmul_rn(prod, o);
-        }
-        if (g == 0 && active_j) {
-            const double s = __dsub_rn(1.0, prod);
-            r_cur[u * la.len + j] = s;
-            term_sum = __dadd_rn(term_sum, __dmul_rn(s, dimj));
+            if (g == 0 && active_j) {
+                const double s = __dsub_rn(1.0, prod);
+                r_cur[u * la.len + j] = s;
+                term_sum = __dadd_rn(term_sum, __dmul_rn(s, dimj));
+            }
         }
     }
     // block partials: partial[block * len + j]
@@ -115,13 +168,7 @@ __global__ void __launch_bounds__(kEstLongThreads) k_res_long(DevCsr M, const do
     const int64_t a0 = M.rowptr[u], len = M.rowptr[u + 1] - a0;
     const int64_t k0 = a0 + len * warp / (kEstLongThreads / 32), k1 = a0 + len * (warp + 1) / (kEstLongThreads / 32);
     double prod = 1.0;
-    if (active_j) {
-        for (int64_t k = k0 + g; k < k1; k += G) {
-            const int32_t v = M.col[k];
-            const double rv = r_next[(int64_t)v * la.len + j];
-            prod = __dmul_rn(prod, __dsub_rn(1.0, rv));
-        }
-    }
+    if (active_j) prod = factor_product(M, r_next, la.len, j, k0 + g, k1, G);
     for (int d = la.jp; d < 32; d <<= 1) {
         const double o = __shfl_xor_sync(kFull, prod, d);
         prod = __dmul_rn(prod, o);
@@ -191,7 +238,8 @@ int32_t estimate(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, double *c_
         la.jp = jp;
         la.dim_leaf = (double)M.cols;
         for (int j = 0; j < len; j++) la.dims[j] = (double)chain[j]->d.cols;
-        int64_t blocks = (M.rows * 32 + kEstThreads - 1) / kEstThreads;
+        la.tile = level_tile(M.rows, blocks_cap);
+        int64_t blocks = (M.rows + (int64_t)la.tile * (kEstThreads / 32) - 1) / ((int64_t)la.tile * (kEstThreads / 32));
         blocks = std::max<int64_t>(1, std::min(blocks, blocks_cap));
         // rows of more than kEstLongRow entries (known for uploaded matrices)
         // get a whole CTA each
@@ -312,7 +360,8 @@ extern "C" RMCM_API int32_t rmcm_estimate_noalloc(int32_t len, const int64_t *ro
         la.jp = jp;
         la.dim_leaf = (double)M.cols;
         for (int j = 0; j < len; j++) la.dims[j] = (double)cols[j];
-        int64_t blocks = (M.rows * 32 + kEstThreads - 1) / kEstThreads;
+        la.tile = level_tile(M.rows, blocks_cap);
+        int64_t blocks = (M.rows + (int64_t)la.tile * (kEstThreads / 32) - 1) / ((int64_t)la.tile * (kEstThreads / 32));
         blocks = std::max<int64_t>(1, std::min(blocks, blocks_cap));
         k_res_level<<<(unsigned)blocks, kEstThreads, 0, s>>>(M, r_next, r_cur, la, part, false);
         if (la.nj > 0) k_res_reduce<<<1, 256, 0, s>>>(part, (int32_t)blocks, la, c_dev);
