@@ -9,8 +9,10 @@
 // for i = len-1 .. 0.  dim(vts[j+1]) is the column count of M_j.
 //
 // One launch per level i computes every j > i at once, so each M_i is read
-// once: the sparsities of a level are stored row-major as r[v * len + j], and
-// a row's gathers for all j are one contiguous run of doubles.
+// once: a level stores q = 1 - r (r rounded first, then 1 - r rounded, the
+// value the reference's next level forms) row-major as q[v * len + j], so
+// the next level multiplies the gathered q directly and a row's gathers for
+// all j are one contiguous run of doubles.
 // Mapping: a warp per row; the warp is split into G groups of JP lanes
 // (JP = next power of two >= number of j), lane (g, j) multiplies the factors
 // of entries g, g+G, ... for target j, and the G partial products are
@@ -46,12 +48,12 @@ struct LevelArgs {
     double dims[kMaxLen];   // dims[j] = cols of M_j
 };
 
-// prod over entries k = k0, k0 + G, ... < k1 of (1 - r_next[col_k][j]).
+// prod over entries k = k0, k0 + G, ... < k1 of q_next[col_k][j] (= 1 - r).
 // A lane with at least four entries keeps four independent partial products
 // (entries taken in turn) so four gathers and multiply chains are in flight,
 // combined in a fixed order ((p0 p1)(p2 p3)); a shorter run multiplies
 // serially (no combining multiplies).  Reproducible run to run.
-__device__ __forceinline__ double factor_product(const DevCsr &M, const double *r_next, int32_t len, int j,
+__device__ __forceinline__ double factor_product(const DevCsr &M, const double *q_next, int32_t len, int j,
                                                  int64_t k0, int64_t k1, int G) {
     int64_t k = k0;
     if (k + 3 * (int64_t)G < k1) {
@@ -60,25 +62,24 @@ __device__ __forceinline__ double factor_product(const DevCsr &M, const double *
             int32_t v[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) v[u] = M.col[k + u * G];
-            double r[4];
+            double q[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) r[u] = r_next[(int64_t)v[u] * len + j];
+            for (int u = 0; u < 4; u++) q[u] = q_next[(int64_t)v[u] * len + j];
 #pragma unroll
-            for (int u = 0; u < 4; u++) p[u] = __dmul_rn(p[u], __dsub_rn(1.0, r[u]));
+            for (int u = 0; u < 4; u++) p[u] = __dmul_rn(p[u], q[u]);
         }
         // the last 0..3 entries, into p[0], p[1], p[2] in turn
 #pragma unroll
         for (int u = 0; u < 3; u++) {
             if (k < k1) {
-                const double r = r_next[(int64_t)M.col[k] * len + j];
-                p[u] = __dmul_rn(p[u], __dsub_rn(1.0, r));
+                p[u] = __dmul_rn(p[u], q_next[(int64_t)M.col[k] * len + j]);
                 k += G;
             }
         }
         return __dmul_rn(__dmul_rn(p[0], p[1]), __dmul_rn(p[2], p[3]));
     }
     double p = 1.0;
-    for (; k < k1; k += G) p = __dmul_rn(p, __dsub_rn(1.0, r_next[(int64_t)M.col[k] * len + j]));
+    for (; k < k1; k += G) p = __dmul_rn(p, q_next[(int64_t)M.col[k] * len + j]);
     return p;
 }
 
@@ -91,17 +92,19 @@ inline int32_t level_tile(int64_t rows, int64_t blocks_cap) {
     return t;
 }
 
-__global__ void __launch_bounds__(kEstThreads) k_res_level(DevCsr M, const double *r_next, double *r_cur,
+__global__ void __launch_bounds__(kEstThreads) k_res_level(DevCsr M, const double *q_next, double *q_cur,
                                                            LevelArgs la, double *partial, bool skip_long) {
+    __shared__ double s_tp[kEstThreads / 32][32 * kMaxLen];   // tile products: [t * jp + jo]
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int G = 32 / la.jp;
     const int g = lane / la.jp;
     const int jo = lane % la.jp;                 // offset of j above i+1
-    const bool active_j = jo < la.nj && g < G;
+    const bool active_j = jo < la.nj;
     const int j = la.i + 1 + jo;
     const double dimj = active_j ? la.dims[j] : 0.0;
-    double term_sum = 0.0;                       // held by group-0 lanes
+    double term_sum = 0.0;                       // this lane's rows of target j
     const int T = la.tile;                       // rows per warp step (1 .. 32)
+    double *tp = s_tp[warp];
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t t0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * T; t0 < M.rows;
          t0 += nwarps * T) {
@@ -111,17 +114,21 @@ __global__ void __launch_bounds__(kEstThreads) k_res_level(DevCsr M, const doubl
             const int64_t ul = t0 + lane;
             my_a0 = M.rowptr[ul];
             my_len = M.rowptr[ul + 1] - my_a0;
-            const double s = __ddiv_rn((double)my_len, la.dim_leaf);
-            r_cur[ul * la.len + la.i] = s > 1.0 ? 1.0 : s;
+            double r = __ddiv_rn((double)my_len, la.dim_leaf);
+            r = r > 1.0 ? 1.0 : r;
+            q_cur[ul * la.len + la.i] = __dsub_rn(1.0, r);
         }
         if (la.nj == 0) continue;
         const int nrow = M.rows - t0 < (int64_t)T ? (int)(M.rows - t0) : T;
+        uint32_t skipped = 0;
         for (int t = 0; t < nrow; t++) {
-            const int64_t u = t0 + t;
             const int64_t a0 = __shfl_sync(kFull, my_a0, t), rl = __shfl_sync(kFull, my_len, t);
-            if (skip_long && rl > kEstLongRow) continue;   // a CTA of k_res_long takes it
+            if (skip_long && rl > kEstLongRow) {   // a CTA of k_res_long takes it
+                skipped |= 1u << t;
+                continue;
+            }
             double prod = 1.0;
-            if (active_j) prod = factor_product(M, r_next, la.len, j, a0 + g, a0 + rl, G);
+            if (active_j) prod = factor_product(M, q_next, la.len, j, a0 + g, a0 + rl, G);
             // combine the group products (fixed butterfly order); groups past
             // the row's entries hold exactly 1.0, so those steps are skipped
             const int ng = rl < (int64_t)G ? (int)rl : G;
@@ -129,13 +136,23 @@ __global__ void __launch_bounds__(kEstThreads) k_res_level(DevCsr M, const doubl
                 const double o = __shfl_xor_sync(kFull, prod, d);
                 prod = __dmul_rn(prod, o);
             }
-            if (g == 0 && active_j) {
-                const double s = __dsub_rn(1.0, prod);
-                r_cur[u * la.len + j] = s;
-                term_sum = __dadd_rn(term_sum, __dmul_rn(s, dimj));
+            if (g == 0 && active_j) tp[t * la.jp + jo] = prod;
+        }
+        __syncwarp();
+        // per (row, target): r = 1 - prod, its term r * dim_j, and q = 1 - r
+        // for the next level; lane (g, jo) takes rows g, g + G, ...
+        if (active_j) {
+            for (int t = g; t < nrow; t += G) {
+                if ((skipped >> t) & 1u) continue;
+                const double r = __dsub_rn(1.0, tp[t * la.jp + jo]);
+                q_cur[(t0 + t) * la.len + j] = __dsub_rn(1.0, r);
+                term_sum = __dadd_rn(term_sum, __dmul_rn(r, dimj));
             }
         }
+        __syncwarp();
     }
+    // this warp's sums per target, over the groups in a fixed order
+    for (int d = la.jp; d < 32; d <<= 1) term_sum = __dadd_rn(term_sum, __shfl_xor_sync(kFull, term_sum, d));
     // block partials: partial[block * len + j]
     __shared__ double s_part[kEstThreads / 32][kMaxLen];
     if (g == 0 && active_j) s_part[warp][jo] = term_sum;
@@ -154,7 +171,7 @@ __global__ void __launch_bounds__(kEstThreads) k_res_level(DevCsr M, const doubl
 // reduction still adds them in a fixed order.
 constexpr int kEstLongThreads = 1024;
 
-__global__ void __launch_bounds__(kEstLongThreads) k_res_long(DevCsr M, const double *r_next, double *r_cur,
+__global__ void __launch_bounds__(kEstLongThreads) k_res_long(DevCsr M, const double *q_next, double *q_cur,
                                                               LevelArgs la, const int32_t *long_rows,
                                                               double *partial) {
     __shared__ double s_prod[kEstLongThreads / 32][kMaxLen];
@@ -168,7 +185,7 @@ __global__ void __launch_bounds__(kEstLongThreads) k_res_long(DevCsr M, const do
     const int64_t a0 = M.rowptr[u], len = M.rowptr[u + 1] - a0;
     const int64_t k0 = a0 + len * warp / (kEstLongThreads / 32), k1 = a0 + len * (warp + 1) / (kEstLongThreads / 32);
     double prod = 1.0;
-    if (active_j) prod = factor_product(M, r_next, la.len, j, k0 + g, k1, G);
+    if (active_j) prod = factor_product(M, q_next, la.len, j, k0 + g, k1, G);
     for (int d = la.jp; d < 32; d <<= 1) {
         const double o = __shfl_xor_sync(kFull, prod, d);
         prod = __dmul_rn(prod, o);
@@ -180,7 +197,7 @@ __global__ void __launch_bounds__(kEstLongThreads) k_res_long(DevCsr M, const do
         for (int w = 0; w < kEstLongThreads / 32; w++) p = __dmul_rn(p, s_prod[w][threadIdx.x]);
         const int jj = la.i + 1 + threadIdx.x;
         const double sv = __dsub_rn(1.0, p);
-        r_cur[u * la.len + jj] = sv;
+        q_cur[u * la.len + jj] = __dsub_rn(1.0, sv);   // q = 1 - r for the next level
         partial[(int64_t)blockIdx.x * kMaxLen + threadIdx.x] = __dmul_rn(sv, la.dims[jj]);
     }
 }
