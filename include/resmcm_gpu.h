@@ -272,14 +272,23 @@ RMCM_API int32_t rmcm_estimate_metapath(rmcm_handle *h, rmcm_graph *g, const cha
  *                    (0 .. 65536; 0 = none)
  *   hash_load        hash tables get at least min(products, width) / load
  *                    slots (0.1 .. 0.75)
- * Defaults: 32, 4096, 16, 2048, 0.5.  A batch keeps the values it was created
- * with. */
+ *   gemm_inv_density uint32 products whose rows all take the single-pass dense
+ *                    path: inner indices with (A column count / rows) x
+ *                    (B row length / cols) >= 1 / gemm_inv_density are
+ *                    multiplied as a dense FP16 GEMM on the tensor cores
+ *                    (exact: see dense_gemm.cu); 0 = never (0 .. 65536)
+ *   gemm_min_mflops  products with fewer multiply-adds (millions) never try
+ *                    it (>= 0)
+ * Defaults: 32, 4096, 16, 2048, 0.5, 256, 512.  A batch keeps the values it
+ * was created with (its recorded products never use the GEMM). */
 typedef struct rmcm_tuning {
     int32_t threads_per_row;
     int32_t hash_max_flops;
     int32_t dense_ratio;
     int32_t warp_max_flops;
     double hash_load;
+    int32_t gemm_inv_density;
+    int32_t gemm_min_mflops;
 } rmcm_tuning;
 RMCM_API int32_t rmcm_set_tuning(rmcm_handle *h, const rmcm_tuning *t);
 RMCM_API int32_t rmcm_get_tuning(const rmcm_handle *h, rmcm_tuning *t);

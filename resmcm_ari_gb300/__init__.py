@@ -61,7 +61,8 @@ class Timings(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("threads_per_row", C.c_int32), ("hash_max_flops", C.c_int32), ("dense_ratio", C.c_int32),
-                ("warp_max_flops", C.c_int32), ("hash_load", C.c_double)]
+                ("warp_max_flops", C.c_int32), ("hash_load", C.c_double),
+                ("gemm_inv_density", C.c_int32), ("gemm_min_mflops", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -627,14 +628,16 @@ class Engine:
         return t.as_dict()
 
     def set_tuning(self, **kw):
-        """Change some of threads_per_row, hash_max_flops, dense_ratio, warp_max_flops, hash_load."""
+        """Change some of threads_per_row, hash_max_flops, dense_ratio, warp_max_flops, hash_load,
+        gemm_inv_density, gemm_min_mflops."""
         cur = self.get_tuning()
         bad = set(kw) - set(cur)
         if bad:
             raise ValueError(f"unknown tunables {sorted(bad)}")
         cur.update(kw)
         t = Tuning(int(cur["threads_per_row"]), int(cur["hash_max_flops"]), int(cur["dense_ratio"]),
-                   int(cur["warp_max_flops"]), float(cur["hash_load"]))
+                   int(cur["warp_max_flops"]), float(cur["hash_load"]), int(cur["gemm_inv_density"]),
+                   int(cur["gemm_min_mflops"]))
         self._check(lib().rmcm_set_tuning(self._h, C.byref(t)))
 
     def batch(self, graph: HeteroGraph, paths: list, lanes: int = 8) -> Batch:

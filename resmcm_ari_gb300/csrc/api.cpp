@@ -1048,6 +1048,7 @@ RMCM_API int32_t rmcm_destroy(rmcm_handle *h) {
         for (auto &e : r.ev)
             if (e) cudaEventDestroy(e);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    cublas_destroy(h);
     if (h->scratch) dev_free(h, h->scratch, h->scratch_bytes);
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->d_status) cudaFree(h->d_status);
@@ -1686,6 +1687,11 @@ RMCM_API int32_t rmcm_set_tuning(rmcm_handle *h, const rmcm_tuning *t) {
         return set_error(h, RMCM_EINVAL, "tuning: hash_load must be in 0.1 .. 0.75");
     if (t->warp_max_flops < 0 || t->warp_max_flops > 65536)
         return set_error(h, RMCM_EINVAL, "tuning: warp_max_flops must be in 0 .. 65536");
+    if (t->gemm_inv_density < 0 || t->gemm_inv_density > 65536)
+        return set_error(h, RMCM_EINVAL, "tuning: gemm_inv_density must be in 0 .. 65536");
+    if (t->gemm_min_mflops < 0) return set_error(h, RMCM_EINVAL, "tuning: gemm_min_mflops must be >= 0");
+    h->tune.gemm_inv_density = t->gemm_inv_density;
+    h->tune.gemm_min_mflops = t->gemm_min_mflops;
     h->tune.threads_per_row = g;
     h->tune.warp_max_flops = t->warp_max_flops;
     h->tune.hash_max_flops = t->hash_max_flops;
@@ -1701,6 +1707,8 @@ RMCM_API int32_t rmcm_get_tuning(const rmcm_handle *h, rmcm_tuning *t) {
     t->dense_ratio = h->tune.dense_ratio;
     t->warp_max_flops = h->tune.warp_max_flops;
     t->hash_load = h->tune.hash_load;
+    t->gemm_inv_density = h->tune.gemm_inv_density;
+    t->gemm_min_mflops = h->tune.gemm_min_mflops;
     return RMCM_OK;
 }
 

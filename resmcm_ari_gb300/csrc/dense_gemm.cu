@@ -1,0 +1,292 @@
+// Tensor-core part of dense-bin products (sm_103a; cuBLAS FP16 GEMM, FP32
+// accumulation, exact integer results).
+//
+// A product C = A B whose output rows all sit in the dense bin often has a
+// few inner indices u (columns of A, rows of B) that carry most of its
+// multiply-adds: A's column u is nearly full and so is B's row u (in the
+// retail workload, the heaviest users of T x U . U x C).  For those, the
+// sub-product A[:, H] B[H, :] is dense work: it runs as a GEMM on the tensor
+// cores, and the dense-bin kernel streams only the remaining entries of A
+// into counters seeded with the GEMM's rows.
+//
+// Exactness.  A's heavy values (<= 2048) and B's heavy values split into L
+// limbs of `bits` bits (each <= 2047) are integers that FP16 holds exactly;
+// their products and every partial sum of a GEMM output are non-negative
+// integers no larger than S_A * (2^bits - 1) <= 2^24, S_A being the largest
+// sum of a row's heavy A values, so FP32 holds each of them exactly in any
+// summation order.  The row's counter then takes sum_l G_l << (bits * l)
+// modulo 2^32, the uint32 value of the exact product (rows that could
+// overflow uint32 never come here).
+//
+// The heavy set: an inner index is heavy when (A column count / rows) x
+// (B row length / cols) reaches 1 / inv_density, the point where a dense
+// multiply-add on the tensor cores costs less than the sparse ones it
+// replaces; column counts are sampled (every 8th entry of A).  Which indices
+// are heavy only moves work between the two parts, never changes a result.
+#include <cublas_v2.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "internal.h"
+
+namespace rmcm {
+namespace {
+
+constexpr int kSample = 8;            // A entries per counted one (column counts)
+constexpr int64_t kMaxHeavy = 65536;  // heavy indices at most (A panel row in shared memory)
+constexpr int kGatherThreads = 256;
+
+// Sampled column counts of A: cnt[u] += 1 for every kSample-th entry.
+__global__ void k_col_sample(DevCsr A, uint32_t *cnt) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x * kSample;
+    for (int64_t k = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kSample; k < A.nnz; k += stride)
+        atomicAdd(cnt + A.col[k], 1u);
+}
+
+// heavy[u] = score threshold met; slot[u] = its index in the heavy list
+// (order of discovery: the list order never changes a result), list[slot] = u.
+__global__ void k_heavy_select(int64_t nin, const uint32_t *cnt, const int64_t *browptr, double thr,
+                               uint8_t *heavy, int32_t *slot, int32_t *list, int32_t *nheavy, int32_t cap) {
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t u0 = (int64_t)blockIdx.x * blockDim.x; u0 < nin; u0 += stride) {
+        const int64_t u = u0 + threadIdx.x;
+        bool hv = false;
+        if (u < nin) {
+            const double score = (double)cnt[u] * kSample * (double)(browptr[u + 1] - browptr[u]);
+            hv = score >= thr;
+        }
+        const unsigned b = __ballot_sync(0xffffffffu, hv);
+        int base = 0;
+        if (lane == 0 && b) base = atomicAdd(nheavy, __popc(b));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (u < nin) {
+            int32_t s = -1;
+            if (hv) {
+                s = base + __popc(b & ((1u << lane) - 1u));
+                if (s < cap) list[s] = (int32_t)u;
+                else s = -1;
+            }
+            heavy[u] = s >= 0;
+            slot[u] = s;
+        }
+    }
+}
+
+// Row panel of A over the heavy indices: Ad[r][slot[u]] = A[r][u] as FP16
+// (ld columns, zero elsewhere), built in shared memory and written whole.
+// stats[0] = largest row sum of heavy values, stats[1] = largest heavy value.
+__global__ void __launch_bounds__(kGatherThreads) k_gather_a(DevCsr A, const int32_t *slot, int32_t ld, __half *Ad,
+                                                             unsigned long long *stats) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __half *row = (__half *)smem;
+    __shared__ unsigned long long s_sum, s_max;
+    const uint32_t *av = (const uint32_t *)A.val;
+    for (int64_t r = blockIdx.x; r < A.rows; r += gridDim.x) {
+        for (int i = threadIdx.x; i < ld / 8; i += kGatherThreads) ((uint4 *)row)[i] = make_uint4(0, 0, 0, 0);
+        if (threadIdx.x == 0) {
+            s_sum = 0;
+            s_max = 0;
+        }
+        __syncthreads();
+        unsigned long long sum = 0, mx = 0;
+        for (int64_t k = A.rowptr[r] + threadIdx.x; k < A.rowptr[r + 1]; k += kGatherThreads) {
+            const int32_t s = slot[A.col[k]];
+            if (s >= 0) {
+                const uint32_t v = av[k];
+                row[s] = __uint2half_rn(v);
+                sum += v;
+                mx = v > mx ? v : mx;
+            }
+        }
+        if (sum) atomicAdd(&s_sum, sum);
+        if (mx) atomicMax(&s_max, mx);
+        __syncthreads();
+        uint4 *dst = (uint4 *)(Ad + r * (int64_t)ld);
+        for (int i = threadIdx.x; i < ld / 8; i += kGatherThreads) dst[i] = ((const uint4 *)row)[i];
+        if (threadIdx.x == 0) {
+            if (s_sum) atomicMax(stats, s_sum);
+            if (s_max) atomicMax(stats + 1, s_max);
+        }
+        __syncthreads();
+    }
+}
+
+// Limb l of the heavy rows of B: Bd[l][h][c] = (B[list[h]][c] >> (bits l)) &
+// (2^bits - 1) as FP16 (ld columns, zero elsewhere).  stats[2] = largest
+// value seen (checked against the limbs).
+__global__ void __launch_bounds__(kGatherThreads) k_gather_b(DevCsr B, const int32_t *list, int32_t nh, int32_t ld,
+                                                             int32_t limbs, int32_t bits, __half *Bd,
+                                                             int64_t limb_stride, unsigned long long *stats) {
+    const uint32_t *bv = (const uint32_t *)B.val;
+    const uint32_t mask = (1u << bits) - 1u;
+    unsigned long long mx = 0;
+    for (int64_t h = blockIdx.x; h < nh; h += gridDim.x) {
+        const int32_t u = list[h];
+        for (int l = 0; l < limbs; l++) {
+            uint4 *dst = (uint4 *)(Bd + l * limb_stride + h * (int64_t)ld);
+            for (int i = threadIdx.x; i < ld / 8; i += kGatherThreads) dst[i] = make_uint4(0, 0, 0, 0);
+        }
+        __syncthreads();
+        for (int64_t k = B.rowptr[u] + threadIdx.x; k < B.rowptr[u + 1]; k += kGatherThreads) {
+            const uint32_t v = bv[k];
+            const int32_t c = B.col[k];
+            mx = v > mx ? v : mx;
+            for (int l = 0; l < limbs; l++)
+                Bd[l * limb_stride + h * (int64_t)ld + c] = __uint2half_rn((v >> (bits * l)) & mask);
+        }
+        __syncthreads();
+    }
+    if (mx) atomicMax(stats + 2, mx);
+}
+
+}  // namespace
+
+// Builds the tensor-core part of C = A B (uint32, single-window dense rows):
+// on success dp.G holds L limb panels (rows x ld floats each) and dp.skip
+// flags the heavy inner indices; otherwise dp stays empty (and the product
+// runs sparse).  bmax: an upper bound on B's values.
+int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint64_t bmax, DensePart &dp) {
+    dp = DensePart{};
+    const int32_t inv_density = h->tune.gemm_inv_density;
+    if (inv_density <= 0 || A.rows == 0 || B.cols == 0 || A.cols == 0) return RMCM_OK;
+    cudaStream_t s = h->stream;
+    const int64_t M = A.rows, N = B.cols, K = A.cols;
+    const int64_t ldn = (N + 7) / 8 * 8;
+    const double thr = (double)M * (double)N / (double)inv_density;
+    // heavy-set scratch: counts, flags, slots, list, counters/stats
+    auto al = [](int64_t x) { return (x + 255) & ~255LL; };
+    const int64_t o_cnt = 0, o_flag = o_cnt + al(4 * K), o_slot = o_flag + al(K), o_list = o_slot + al(4 * K);
+    const int64_t o_small = o_list + al(4 * kMaxHeavy), sel_bytes = o_small + 256;
+    char *sel = nullptr;
+    RMCM_TRY(dev_alloc(h, (void **)&sel, sel_bytes));
+    uint32_t *cnt = (uint32_t *)(sel + o_cnt);
+    uint8_t *flag = (uint8_t *)(sel + o_flag);
+    int32_t *slot = (int32_t *)(sel + o_slot), *list = (int32_t *)(sel + o_list);
+    int32_t *nheavy = (int32_t *)(sel + o_small);
+    unsigned long long *stats = (unsigned long long *)(sel + o_small + 64);
+    auto fail = [&](int32_t rc) {
+        dev_free(h, sel, sel_bytes);
+        dp = DensePart{};
+        return rc;
+    };
+    RMCM_CUDA(h, cudaMemsetAsync(cnt, 0, 4 * K, s));
+    RMCM_CUDA(h, cudaMemsetAsync(sel + o_small, 0, 256, s));
+    k_col_sample<<<h->sm_count * 8, 256, 0, s>>>(A, cnt);
+    k_heavy_select<<<h->sm_count * 8, 256, 0, s>>>(K, cnt, B.rowptr, thr, flag, slot, list, nheavy,
+                                                  (int32_t)kMaxHeavy);
+    h->launches += 2;
+    RMCM_CUDA(h, cudaGetLastError());
+    RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned + 8, nheavy, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    RMCM_CUDA(h, cudaStreamSynchronize(s));
+    const int64_t nh = std::min<int64_t>(((int32_t *)(h->h_pinned + 8))[0], kMaxHeavy);
+    // worth a GEMM only when the heavy part is a real share of the work
+    if (nh < 64) return fail(RMCM_OK);
+    const int64_t ldk = (nh + 63) / 64 * 64;
+    // dense panels: A (M x ldk) and up to 3 limbs of B (ldk x ldn), FP16; G (L x M x ldn), FP32
+    const int64_t a_bytes = al(2 * M * ldk), b_limb = ldk * ldn, g_limb = M * ldn;
+    const int64_t max_bytes = (h->budget - h->in_use) / 3;
+    if (a_bytes + al(2 * 3 * b_limb) + al(4 * 3 * g_limb) > max_bytes) return fail(RMCM_OK);
+    if (ldk * 2 > 160 * 1024) return fail(RMCM_OK);
+    __half *Ad = nullptr;
+    RMCM_TRY(dev_alloc(h, (void **)&Ad, a_bytes));
+    auto fail2 = [&](int32_t rc) {
+        dev_free(h, Ad, a_bytes);
+        return fail(rc);
+    };
+    {
+        const int64_t smem = ldk * 2;
+        if (smem > 48 * 1024 &&
+            cudaFuncSetAttribute(k_gather_a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+            cudaGetLastError();
+            return fail2(RMCM_OK);
+        }
+        const int grid = (int)std::min<int64_t>(M, (int64_t)h->sm_count * 8);
+        k_gather_a<<<grid, kGatherThreads, smem, s>>>(A, slot, (int32_t)ldk, Ad, stats);
+        h->launches++;
+        RMCM_CUDA(h, cudaGetLastError());
+    }
+    RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned + 8, stats, 2 * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    RMCM_CUDA(h, cudaStreamSynchronize(s));
+    const uint64_t s_a = ((uint64_t *)(h->h_pinned + 8))[0], a_max = ((uint64_t *)(h->h_pinned + 8))[1];
+    if (s_a == 0 || a_max > 2048) return fail2(RMCM_OK);
+    // limb width: S_A * (2^bits - 1) <= 2^24 and 2^bits - 1 <= 2047
+    int32_t bits = 0;
+    while (bits < 11 && (double)s_a * (double)((1ull << (bits + 1)) - 1) <= 16777216.0) bits++;
+    if (bits == 0) return fail2(RMCM_OK);
+    int32_t bbits = 0;
+    while (bbits < 64 && (bmax >> bbits) != 0) bbits++;
+    const int32_t limbs = std::max(1, (bbits + bits - 1) / bits);
+    if (limbs > 3 || bits * (limbs - 1) >= 32) return fail2(RMCM_OK);
+    const int64_t bd_bytes = al(2 * limbs * b_limb), g_bytes = al(4 * limbs * g_limb);
+    char *mem = nullptr;
+    if (dev_alloc(h, (void **)&mem, bd_bytes + g_bytes) != RMCM_OK) {
+        h->last_error.clear();
+        return fail2(RMCM_OK);
+    }
+    __half *Bd = (__half *)mem;
+    float *G = (float *)(mem + bd_bytes);
+    auto fail3 = [&](int32_t rc) {
+        dev_free(h, mem, bd_bytes + g_bytes);
+        return fail2(rc);
+    };
+    k_gather_b<<<(int)std::min<int64_t>(nh, (int64_t)h->sm_count * 8), kGatherThreads, 0, s>>>(
+        B, list, (int32_t)nh, (int32_t)ldn, limbs, bits, Bd, b_limb, stats);
+    h->launches++;
+    if (ldk > nh) {
+        // padding rows of B's panels (heavy slots past nh) are zero
+        for (int l = 0; l < limbs; l++)
+            RMCM_CUDA(h, cudaMemsetAsync(Bd + l * b_limb + nh * ldn, 0, 2 * (ldk - nh) * ldn, s));
+    }
+    RMCM_CUDA(h, cudaGetLastError());
+    if (!h->cublas) {
+        cublasHandle_t cb = nullptr;
+        if (cublasCreate(&cb) != CUBLAS_STATUS_SUCCESS) return fail3(RMCM_OK);
+        h->cublas = cb;
+    }
+    cublasHandle_t cb = (cublasHandle_t)h->cublas;
+    if (cublasSetStream(cb, s) != CUBLAS_STATUS_SUCCESS) return fail3(set_error(h, RMCM_ECUDA, "cublasSetStream"));
+    // row-major G_l (M x N) = Ad (M x ldk) Bd_l (ldk x N): column-major G_l^T = Bd_l^T Ad^T
+    const float one = 1.0f, zero = 0.0f;
+    for (int l = 0; l < limbs; l++) {
+        const cublasStatus_t st = cublasGemmEx(cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)N, (int)M, (int)ldk, &one,
+                                               Bd + l * b_limb, CUDA_R_16F, (int)ldn, Ad, CUDA_R_16F, (int)ldk,
+                                               &zero, G + l * g_limb, CUDA_R_32F, (int)ldn, CUBLAS_COMPUTE_32F,
+                                               CUBLAS_GEMM_DEFAULT);
+        if (st != CUBLAS_STATUS_SUCCESS) return fail3(set_error(h, RMCM_ECUDA, "dense part: cublasGemmEx failed"));
+    }
+    // the B gather saw no value wider than the limbs
+    RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned + 8, stats + 2, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    RMCM_CUDA(h, cudaStreamSynchronize(s));
+    const uint64_t seen = ((uint64_t *)(h->h_pinned + 8))[0];
+    if (bits * limbs < 64 && (seen >> (bits * limbs)) != 0) return fail3(RMCM_OK);
+    dev_free(h, Ad, a_bytes);
+    dp.mem = mem;
+    dp.bytes = bd_bytes + g_bytes;
+    dp.G = G;
+    dp.ld = ldn;
+    dp.limb_stride = g_limb;
+    dp.limbs = limbs;
+    dp.bits = bits;
+    dp.heavy = nh;
+    dp.sel = sel;
+    dp.sel_bytes = sel_bytes;
+    dp.skip = flag;
+    return RMCM_OK;
+}
+
+void dense_part_release(rmcm_handle *h, DensePart &dp) {
+    if (dp.mem) dev_free(h, dp.mem, dp.bytes);
+    if (dp.sel) dev_free(h, dp.sel, dp.sel_bytes);
+    dp = DensePart{};
+}
+
+void cublas_destroy(rmcm_handle *h) {
+    if (h->cublas) cublasDestroy((cublasHandle_t)h->cublas);
+    h->cublas = nullptr;
+}
+
+}  // namespace rmcm

@@ -58,6 +58,10 @@ struct Tuning {
     int32_t hash_max_flops = 4096;  // rows above go to the dense / rank bins
     int32_t dense_ratio = 16;       // dense when flops * dense_ratio >= cols (and one window covers cols)
     int32_t warp_max_flops = 2048;  // output width <= 2048 and at most this many flops: warp bin (0: none)
+    // dense-bin products: inner indices whose A-column x B-row density reaches
+    // 1 / gemm_inv_density go to a tensor-core GEMM (0: never)
+    int32_t gemm_inv_density = 256;
+    int32_t gemm_min_mflops = 512;   // products with fewer multiply-adds (millions) stay sparse
     double hash_load = 0.5;         // hash table load factor bound: slots >= min(f, cols) / load, load <= 0.75
     bool dense_single_pass = true;  // dense rows in one window: one pass into a padded temporary
     int64_t dense_temp_max_bytes = 8LL << 30;
@@ -143,6 +147,7 @@ struct rmcm_handle {
     std::set<rmcm_batch *> batches;  // batches recorded on this handle
     bool abort_on_certain_overflow = false;   // spgemm returns EOVERFLOW before computing when sure
     int32_t order_mode = RMCM_ORDER_RES;
+    void *cublas = nullptr;          // cuBLAS handle of the dense-bin GEMMs (created on first use)
 };
 
 struct rmcm_graph {
@@ -200,6 +205,21 @@ int32_t spgemm(rmcm_handle *h, const rmcm_mat *A, const rmcm_mat *B, rmcm_mat **
                ProductPlan *plan = nullptr);
 int32_t fill_ones(rmcm_handle *h, void *val, int64_t nnz, int32_t valtype);
 int32_t convert_values(rmcm_handle *h, const rmcm_mat *src, int32_t valtype, rmcm_mat **out);
+// dense_gemm.cu: tensor-core part of a uint32 dense-bin product.  G holds
+// `limbs` FP32 panels (A.rows x ld, limb_stride apart); row r's uint32 part is
+// sum_l G_l[r][c] << (bits * l).  skip[u] flags the inner indices it covers.
+struct DensePart {
+    const float *G = nullptr;
+    int64_t ld = 0, limb_stride = 0;
+    int32_t limbs = 0, bits = 0;
+    int64_t heavy = 0;
+    const uint8_t *skip = nullptr;
+    void *mem = nullptr, *sel = nullptr;
+    int64_t bytes = 0, sel_bytes = 0;
+};
+int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint64_t bmax, DensePart &dp);
+void dense_part_release(rmcm_handle *h, DensePart &dp);
+void cublas_destroy(rmcm_handle *h);
 // estimator.cu: c_dev[len*len] on the device
 int32_t estimate(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, double *c_dev);
 // chain_dp.cu: split/cost/pairs on the device

@@ -1350,12 +1350,25 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
 // to slot ri of a row-padded temporary (C.col / C.val point at it, slot
 // stride `tstride` entries) and its length goes to cnt[r]; the symbolic pass
 // is skipped for these rows and k_copy_rows compacts the slots into C.
+// Per-product extras of the dense bin (single-window rows only): the packed
+// copy of B (k_pack_banked) and the tensor-core part of the product (G panels
+// of uint32 limbs; skip[u] flags the inner indices it covers, whose A entries
+// the kernel leaves out).
+struct DenseExtra {
+    const uint32_t *pk = nullptr;
+    int32_t cbits = 0;
+    int32_t glimbs = 0, gbits = 0;
+    const float *G = nullptr;
+    int64_t gld = 0, gstride = 0;
+    const uint8_t *skip = nullptr;
+};
+
 template <typename V, bool NUMERIC, bool TEMP, bool PRES = true>
 __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, DevCsr C, const int32_t *rows,
                                                          int32_t nrows, int64_t *cnt, int32_t *cursors,
                                                          int64_t cur_stride, int32_t W, int *st, int64_t tstride,
                                                          const uint8_t *bin_of, bool positive, bool b_distinct,
-                                                         bool abort_mode, const uint32_t *pk, int32_t cbits) {
+                                                         bool abort_mode, DenseExtra ex) {
     constexpr int NT = kDenseThreads;
     constexpr int kPull = 4;   // register accumulators per thread: windows of up to 4 * NT columns
     static_assert(kChunk == NT, "the dense kernel stages one A entry per thread");
@@ -1410,6 +1423,19 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                 else atomicAdd((AtomV *)(acc + lc), (AtomV)p);
             }
         };
+        if constexpr (NUMERIC && sizeof(V) == 4) {
+            if (ex.G) {
+                // the row's tensor-core part seeds the counters (one window)
+                const float *g = ex.G + (int64_t)r * ex.gld;
+                for (int c = tid; c < (int)B.cols; c += NT) {
+                    uint32_t v = 0;
+                    for (int l = 0; l < ex.glimbs; l++)
+                        v += __float2uint_rn(g[l * ex.gstride + c]) << (ex.gbits * l);
+                    acc[c] = v;
+                }
+                __syncthreads();
+            }
+        }
         while (true) {
             const int64_t w1 = min(w0 + (int64_t)W, B.cols);
             if (tid == 0) s_next = INT_MAX;
@@ -1433,7 +1459,9 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                     if (t < n) {
                         const int64_t k = k0 + t;
                         const int32_t a = A.col[k];
-                        const int64_t bs = B.rowptr[a], be = B.rowptr[a + 1];
+                        const int64_t bs = B.rowptr[a];
+                        // inner indices of the tensor-core part contribute through G
+                        const int64_t be = (ex.skip && ex.skip[a]) ? bs : B.rowptr[a + 1];
                         int64_t lo = bs, hi = be;
                         if (multi) {
                             if (!first) lo = bs + cur[k - a0];
@@ -1497,7 +1525,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                         };
                         if (sg.nlong) {
                             // pk: packed copy of B (single window only)
-                            if (pk) stream_long_packed(sg, sg.nlong, pk, cbits, add);
+                            if (ex.pk) stream_long_packed(sg, sg.nlong, ex.pk, ex.cbits, add);
                             else stream_long_plain<V>(sg, sg.nlong, B, add);
                         }
                         stream_chunk<NT, V, NUMERIC>(sg, n, B, false, ovf, add);
@@ -2419,6 +2447,7 @@ struct DenseTemp {
     int32_t cbits = 0;
     void *pk_mem = nullptr;
     int64_t pk_bytes = 0;
+    DensePart dpart;                  // tensor-core part of the product (single-pass rows)
     // split rows
     bool split = false;
     const int64_t *flops = nullptr;   // per-row products (scratch)
@@ -2456,6 +2485,24 @@ constexpr int64_t kSplitMinFlops = 1 << 20;
 
 // A rows with more entries than this are analysed by the whole grid.
 constexpr int64_t kLongAnalyze = 16384;
+
+// Extras of a dense-bin launch: the packed copy of B, and (single-pass rows
+// only) the tensor-core part.
+DenseExtra dense_extra(const DenseTemp *t, bool single_pass) {
+    DenseExtra e;
+    if (!t) return e;
+    e.pk = t->pk;
+    e.cbits = t->cbits;
+    if (single_pass && t->dpart.G) {
+        e.G = t->dpart.G;
+        e.gld = t->dpart.ld;
+        e.gstride = t->dpart.limb_stride;
+        e.glimbs = t->dpart.limbs;
+        e.gbits = t->dpart.bits;
+        e.skip = t->dpart.skip;
+    }
+    return e;
+}
 
 template <typename V, bool NUMERIC>
 int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevCsr &C, const int32_t *lists,
@@ -2614,7 +2661,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                         if (dn > 0)
                             kern<<<std::max(1, std::min(grid, dn)), kDenseThreads, sm, s>>>(
                                 A, B, T, dl, dn, cnt, nullptr, 0, (int32_t)W, st, temp->stride, bin_of, positive,
-                                b_distinct, h->abort_on_certain_overflow, temp->pk, temp->cbits);
+                                b_distinct, h->abort_on_certain_overflow, dense_extra(temp, true));
                         if (temp->split) {
                             RMCM_CUDA(h, cudaEventRecord(h->ev_join, h->aux));
                             RMCM_CUDA(h, cudaStreamWaitEvent(s, h->ev_join, 0));
@@ -2641,8 +2688,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                 }
                 kern<<<grid, kDenseThreads, sm, s>>>(A, B, C, list, n, cnt, cursor_base, stride, (int32_t)W, st, 0, bin_of,
                                                      positive, b_distinct, h->abort_on_certain_overflow,
-                                                     NUMERIC && !multi && temp ? temp->pk : nullptr,
-                                                     temp ? temp->cbits : 0);
+                                                     NUMERIC && !multi ? dense_extra(temp, false) : DenseExtra{});
                 break;
             }
         }
@@ -2894,13 +2940,34 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         }
         if (record) plan->pack_cbits = cbits;
     }
+    {
+        // Tensor-core part (dense_gemm.cu): every row with products in the
+        // single-pass dense bin, uint32, positive, no row able to overflow, a
+        // large product; not inside a batch recording (plain runs only).
+        bool want = sizeof(V) == 4 && !plan && dtemp.active && positive && dtemp.no_risky &&
+                    flops_total >= (int64_t)h->tune.gemm_min_mflops * 1000000 && h->tune.gemm_inv_density > 0;
+        for (int b = 0; b < kNumBins && want; b++)
+            if (b != kBinDense && counts[b] > 0) want = false;
+        if (want) {
+            uint64_t bmax = 1;
+            if (!Bm->ones) memcpy(&bmax, (int32_t *)h->h_pinned + 58, sizeof(uint64_t));
+            const int32_t drc = dense_part_build(h, A, B, bmax, dtemp.dpart);
+            if (drc != RMCM_OK) {
+                dense_part_release(h, dtemp.dpart);
+                if (dtemp.pk_mem) dev_free(h, dtemp.pk_mem, dtemp.pk_bytes);
+                if (dtemp.active) dev_free(h, dtemp.col, dtemp.bytes);
+                return drc;
+            }
+        }
+    }
     // Dense rows with far more products than a fair share of the device are
     // split over several CTAs (k_dense_split).
     int64_t max_dense_f = 0;
     if (replay) max_dense_f = plan->max_dense_flops;
     else memcpy(&max_dense_f, (int32_t *)h->h_pinned + 36, sizeof(int64_t));
     if (record) plan->max_dense_flops = max_dense_f;
-    if (dtemp.active) {
+    if (dtemp.active && !dtemp.dpart.G) {
+        // (with a tensor-core part the heaviest work is in the GEMM: no split)
         const int64_t fpart = std::max<int64_t>(kSplitMinFlops, flops_total / ((int64_t)h->sm_count * 4));
         if (max_dense_f > fpart) {
             const int32_t nd = counts[kBinDense];
@@ -3029,6 +3096,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         rsplit.active = false;
     };
     auto drop_temp = [&]() {
+        dense_part_release(h, dtemp.dpart);
         if (dtemp.pk_mem) dev_free(h, dtemp.pk_mem, dtemp.pk_bytes);
         dtemp.pk_mem = nullptr;
         dtemp.pk = nullptr;

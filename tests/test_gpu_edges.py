@@ -668,3 +668,83 @@ def test_warp_bin_risky_rows(native, engine):
     assert native.lib().rmcm_spgemm(engine._h, Am._h, Bm._h, ctypes.byref(h)) == native.EOVERFLOW
     native.lib().rmcm_mat_free(engine._h, h)
     _check_product(native, engine, A2, B2, native.VAL_U64)
+
+
+def _heavy_inner(rng, m, k, n, nheavy, bbig=None):
+    """A (m x k) with `nheavy` nearly full columns and sparse others, B (k x n)
+    whose rows for those columns are half full: the product's heavy inner
+    indices go to the tensor-core GEMM, the rest stays sparse.  ``bbig``: a
+    few B values that need more than one limb."""
+    dense_a = (rng.random((m, nheavy)) < 0.8) * rng.integers(1, 4, (m, nheavy))
+    light_a = sp.random(m, k - nheavy, density=0.03, random_state=rng, format="csr")
+    light_a.data[:] = rng.integers(1, 4, light_a.nnz)
+    A = sp.hstack([sp.csr_matrix(dense_a), light_a]).tocsr()
+    dense_b = (rng.random((nheavy, n)) < 0.5) * rng.integers(1, 4, (nheavy, n))
+    light_b = sp.random(k - nheavy, n, density=0.02, random_state=rng, format="csr")
+    light_b.data[:] = rng.integers(1, 4, light_b.nnz)
+    B = sp.vstack([sp.csr_matrix(dense_b), light_b]).tocsr()
+    if bbig is not None:
+        B = B.tolil()
+        for u in range(0, nheavy, 7):
+            B[u, (u * 13) % n] = bbig
+        B = B.tocsr()
+    A.eliminate_zeros()
+    B.eliminate_zeros()
+    return A, B
+
+
+@pytest.mark.parametrize("bbig", [None, 5000, 200000])
+def test_tensor_core_part_of_dense_rows(native, bbig):
+    """Heavy inner indices multiplied as an FP16 GEMM with FP32 accumulation
+    (B split into limbs when its values are wide): the product equals scipy's
+    and the same product with the GEMM turned off, bit for bit."""
+    rng = np.random.default_rng(70 if bbig is None else bbig)
+    A, B = _heavy_inner(rng, 1200, 2500, 1500, 300, bbig)
+    eng = native.Engine(device=0)
+    eng.set_tuning(gemm_min_mflops=0)
+    _check_product(native, eng, A, B, native.VAL_U32)
+    eng.set_tuning(gemm_inv_density=0)
+    _check_product(native, eng, A, B, native.VAL_U32)
+    eng.close()
+
+
+def test_tensor_core_part_in_a_chain_and_batch(native):
+    """A meta-path whose product takes the tensor-core part gives the same
+    (nnz, digest) run plainly (GEMM) and replayed from a batch (no GEMM)."""
+    rng = np.random.default_rng(71)
+    nx, ny, nz = 800, 1500, 1200
+    heavy = 200
+    xs, ys = [], []
+    for x in range(nx):
+        cols = np.concatenate([np.nonzero(rng.random(heavy) < 0.8)[0],
+                               heavy + rng.choice(ny - heavy, 40, replace=False)])
+        xs += [x] * cols.size
+        ys += cols.tolist()
+    src01, dst01 = synth.dedup_pairs_keep_order(np.array(xs), np.array(ys), ny)
+    ys2, zs = [], []
+    for y in range(ny):
+        k = nz // 2 if y < heavy else 20
+        cols = rng.choice(nz, k, replace=False)
+        ys2 += [y] * k
+        zs += cols.tolist()
+    src12, dst12 = synth.dedup_pairs_keep_order(np.array(ys2), np.array(zs), nz)
+    g = synth.SyntheticHIN("gemm", [nx, ny, nz], [synth.Relation(0, 1, 0, 1, src01, dst01),
+                                                  synth.Relation(1, 2, 2, 3, src12, dst12)])
+    eng = native.Engine(device=0)
+    eng.set_tuning(gemm_min_mflops=0)
+    hg = native.HeteroGraph.from_synthetic(eng, g)
+    paths = ["0-0-1-2-2"]
+    C, _, _ = eng.run_metapath(hg, paths[0])
+    plain = [eng.digest(C)]
+    C.free()
+    eng.set_tuning(gemm_inv_density=0)
+    C, _, _ = eng.run_metapath(hg, paths[0])
+    assert eng.digest(C) == plain[0]
+    C.free()
+    eng.set_tuning(gemm_inv_density=256)
+    b = eng.batch(hg, paths, lanes=1)
+    nnz, dig, _ = b.run()
+    assert [(int(a), int(x)) for a, x in zip(nnz, dig)] == plain
+    b.free()
+    hg.close()
+    eng.close()
