@@ -451,7 +451,8 @@ def main():
                 "peak_kind": f"of {peak_kind}",
                 "traffic": (alg * tr["bytes_per_alg_byte"]) if tr else None,
                 "kernel": "SpGEMM product with the largest time per step (all its passes)",
-                "product": {k: b[k] for k in ("rows", "inner", "cols", "nnz_a", "nnz_c", "flops", "bin_rows")},
+                "product": {k: b[k] for k in ("rows", "inner", "cols", "nnz_a", "nnz_c", "flops", "bin_rows",
+                                              "gemm_inner", "gemm_limbs")},
                 "algorithmic_bytes": alg, "launch_ms": avg_ms[dom],
                 "multiply_adds_per_s": b["flops"] / (avg_ms[dom] / 1e3)}
         tot_alg = sum(s_["bytes_a"] + s_["bytes_b_touched"] + s_["bytes_c"] for s_ in bytes_stats)
@@ -462,7 +463,7 @@ def main():
     if args.detail and rank == 0:
         for i, b in enumerate(bytes_stats):
             row = {k: b[k] for k in ("rows", "inner", "cols", "nnz_a", "nnz_b", "nnz_c", "flops", "bin_rows",
-                                      "valtype", "touched_rows", "touched_nnz")}
+                                      "valtype", "touched_rows", "touched_nnz", "gemm_inner", "gemm_limbs")}
             reps = [st for j, st in enumerate(timed_stats) if j % nprod == i]
             for key in ("analyze_ms", "symbolic_ms", "numeric_ms"):
                 row[key] = sum(st[key] for st in reps) / max(1, len(reps))

@@ -105,6 +105,8 @@ typedef struct rmcm_product_stats {
     double analyze_ms, symbolic_ms, numeric_ms;  /* CUDA-event times on the handle's stream */
     int32_t valtype;
     int32_t bin_rows[8];                /* rows per bin: tiny, hash512, hash2k, hash8k, dense, rank, micro, warp */
+    int32_t gemm_limbs;                 /* limbs of B in the tensor-core GEMM (0: no GEMM part) */
+    int64_t gemm_inner;                 /* inner indices multiplied by that GEMM */
 } rmcm_product_stats;
 
 /* ---- handle -------------------------------------------------------------- */
@@ -279,7 +281,7 @@ RMCM_API int32_t rmcm_estimate_metapath(rmcm_handle *h, rmcm_graph *g, const cha
  *                    (exact: see dense_gemm.cu); 0 = never (0 .. 65536)
  *   gemm_min_mflops  products with fewer multiply-adds (millions) never try
  *                    it (>= 0)
- * Defaults: 32, 4096, 16, 2048, 0.5, 256, 512.  A batch keeps the values it
+ * Defaults: 32, 4096, 16, 2048, 0.5, 512, 512.  A batch keeps the values it
  * was created with (its recorded products never use the GEMM). */
 typedef struct rmcm_tuning {
     int32_t threads_per_row;

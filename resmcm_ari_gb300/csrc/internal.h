@@ -60,7 +60,7 @@ struct Tuning {
     int32_t warp_max_flops = 2048;  // output width <= 2048 and at most this many flops: warp bin (0: none)
     // dense-bin products: inner indices whose A-column x B-row density reaches
     // 1 / gemm_inv_density go to a tensor-core GEMM (0: never)
-    int32_t gemm_inv_density = 256;
+    int32_t gemm_inv_density = 512;
     int32_t gemm_min_mflops = 512;   // products with fewer multiply-adds (millions) stay sparse
     double hash_load = 0.5;         // hash table load factor bound: slots >= min(f, cols) / load, load <= 0.75
     bool dense_single_pass = true;  // dense rows in one window: one pass into a padded temporary

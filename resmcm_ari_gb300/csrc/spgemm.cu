@@ -2943,9 +2943,14 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     {
         // Tensor-core part (dense_gemm.cu): every row with products in the
         // single-pass dense bin, uint32, positive, no row able to overflow, a
-        // large product; not inside a batch recording (plain runs only).
+        // large product whose rows need no split over CTAs (skewed rows keep
+        // the split kernels); not inside a batch recording (plain runs only).
+        int64_t mdf = 0;
+        if (!replay) memcpy(&mdf, (int32_t *)h->h_pinned + 36, sizeof(int64_t));
+        const int64_t fpart0 = std::max<int64_t>(kSplitMinFlops, flops_total / ((int64_t)h->sm_count * 4));
         bool want = sizeof(V) == 4 && !plan && dtemp.active && positive && dtemp.no_risky &&
-                    flops_total >= (int64_t)h->tune.gemm_min_mflops * 1000000 && h->tune.gemm_inv_density > 0;
+                    flops_total >= (int64_t)h->tune.gemm_min_mflops * 1000000 && h->tune.gemm_inv_density > 0 &&
+                    mdf <= fpart0;
         for (int b = 0; b < kNumBins && want; b++)
             if (b != kBinDense && counts[b] > 0) want = false;
         if (want) {
@@ -3156,6 +3161,8 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     if (rc == RMCM_OK) rc = mat_alloc(h, m, B.cols, nnz, Am->valtype, &C);
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[4], s);
     if (rc == RMCM_OK) rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap, &dtemp, bin_of, positive, Bm->distinct, &rsplit);
+    const int32_t gemm_limbs = dtemp.dpart.G ? dtemp.dpart.limbs : 0;
+    const int64_t gemm_inner = dtemp.dpart.G ? dtemp.dpart.heavy : 0;
     drop_cursors();
     drop_temp();
     drop_rank();
@@ -3176,6 +3183,8 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         st.flops = flops_total;
         st.valtype = Am->valtype;
         for (int b = 0; b < kNumBins; b++) st.bin_rows[b] = counts[b];
+        st.gemm_limbs = gemm_limbs;
+        st.gemm_inner = gemm_inner;
         if (h->prof_level >= 2 && A.cols > 0) {
             // after the numeric pass: the row lists are no longer needed, reuse them
             uint8_t *mark = (uint8_t *)lists;

@@ -156,5 +156,5 @@ def test_bad_tuning_is_rejected(native, engine):
         with pytest.raises(native.RmcmError):
             engine.set_tuning(**kw)
     assert engine.get_tuning() == {"threads_per_row": 32, "hash_max_flops": 4096, "dense_ratio": 16,
-                                   "warp_max_flops": 2048, "hash_load": 0.5, "gemm_inv_density": 256,
+                                   "warp_max_flops": 2048, "hash_load": 0.5, "gemm_inv_density": 512,
                                    "gemm_min_mflops": 512}

@@ -702,9 +702,13 @@ def test_tensor_core_part_of_dense_rows(native, bbig):
     A, B = _heavy_inner(rng, 1200, 2500, 1500, 300, bbig)
     eng = native.Engine(device=0)
     eng.set_tuning(gemm_min_mflops=0)
+    eng.set_profiling(1)
     _check_product(native, eng, A, B, native.VAL_U32)
+    st = eng.product_stats()[-1]
+    assert st["gemm_inner"] >= 250 and st["gemm_limbs"] == (1 if bbig is None else 2)
     eng.set_tuning(gemm_inv_density=0)
     _check_product(native, eng, A, B, native.VAL_U32)
+    assert eng.product_stats()[-1]["gemm_inner"] == 0
     eng.close()
 
 
@@ -732,9 +736,11 @@ def test_tensor_core_part_in_a_chain_and_batch(native):
                                                   synth.Relation(1, 2, 2, 3, src12, dst12)])
     eng = native.Engine(device=0)
     eng.set_tuning(gemm_min_mflops=0)
+    eng.set_profiling(1)
     hg = native.HeteroGraph.from_synthetic(eng, g)
     paths = ["0-0-1-2-2"]
     C, _, _ = eng.run_metapath(hg, paths[0])
+    assert eng.product_stats()[-1]["gemm_inner"] >= 150
     plain = [eng.digest(C)]
     C.free()
     eng.set_tuning(gemm_inv_density=0)
