@@ -78,28 +78,57 @@ __global__ void k_heavy_select(int64_t nin, const uint32_t *cnt, const int64_t *
 
 // Row panel of A over the heavy indices: Ad[r][slot[u]] = A[r][u] as FP16
 // (ld columns, zero elsewhere), built in shared memory and written whole.
-// stats[0] = largest row sum of heavy values, stats[1] = largest heavy value.
+// The row's other (light) entries go, in any order, to the front of its
+// segment of (lcol, lval); lcnt[r] = their number.  stats[0] = largest row
+// sum of heavy values, stats[1] = largest heavy value.
 __global__ void __launch_bounds__(kGatherThreads) k_gather_a(DevCsr A, const int32_t *slot, int32_t ld, __half *Ad,
+                                                             int32_t *lcol, uint32_t *lval, int32_t *lcnt,
                                                              unsigned long long *stats) {
     extern __shared__ __align__(16) unsigned char smem[];
     __half *row = (__half *)smem;
     __shared__ unsigned long long s_sum, s_max;
+    __shared__ int32_t s_light;
+    const int lane = threadIdx.x & 31;
     const uint32_t *av = (const uint32_t *)A.val;
     for (int64_t r = blockIdx.x; r < A.rows; r += gridDim.x) {
         for (int i = threadIdx.x; i < ld / 8; i += kGatherThreads) ((uint4 *)row)[i] = make_uint4(0, 0, 0, 0);
         if (threadIdx.x == 0) {
             s_sum = 0;
             s_max = 0;
+            s_light = 0;
         }
         __syncthreads();
+        const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
         unsigned long long sum = 0, mx = 0;
-        for (int64_t k = A.rowptr[r] + threadIdx.x; k < A.rowptr[r + 1]; k += kGatherThreads) {
-            const int32_t s = slot[A.col[k]];
-            if (s >= 0) {
-                const uint32_t v = av[k];
-                row[s] = __uint2half_rn(v);
-                sum += v;
-                mx = v > mx ? v : mx;
+        // four entries per thread per step: their gathers overlap
+        for (int64_t k0 = a0; k0 < a1; k0 += 4 * kGatherThreads) {
+            int32_t c[4], sl[4];
+            uint32_t v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int64_t k = k0 + u * kGatherThreads + threadIdx.x;
+                c[u] = k < a1 ? A.col[k] : -1;
+                v[u] = k < a1 ? av[k] : 0u;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) sl[u] = c[u] >= 0 ? slot[c[u]] : -1;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                if (sl[u] >= 0) {
+                    row[sl[u]] = __uint2half_rn(v[u]);
+                    sum += v[u];
+                    mx = v[u] > mx ? v[u] : mx;
+                }
+                const bool light = c[u] >= 0 && sl[u] < 0;
+                const unsigned lb = __ballot_sync(0xffffffffu, light);
+                int base = 0;
+                if (lane == 0 && lb) base = atomicAdd(&s_light, __popc(lb));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (light) {
+                    const int64_t o = a0 + base + __popc(lb & ((1u << lane) - 1u));
+                    lcol[o] = c[u];
+                    lval[o] = v[u];
+                }
             }
         }
         if (sum) atomicAdd(&s_sum, sum);
@@ -108,6 +137,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather_a(DevCsr A, const int
         uint4 *dst = (uint4 *)(Ad + r * (int64_t)ld);
         for (int i = threadIdx.x; i < ld / 8; i += kGatherThreads) dst[i] = ((const uint4 *)row)[i];
         if (threadIdx.x == 0) {
+            lcnt[r] = s_light;
             if (s_sum) atomicMax(stats, s_sum);
             if (s_max) atomicMax(stats + 1, s_max);
         }
@@ -189,12 +219,25 @@ int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint6
     // dense panels: A (M x ldk) and up to 3 limbs of B (ldk x ldn), FP16; G (L x M x ldn), FP32
     const int64_t a_bytes = al(2 * M * ldk), b_limb = ldk * ldn, g_limb = M * ldn;
     const int64_t max_bytes = (h->budget - h->in_use) / 3;
-    if (a_bytes + al(2 * 3 * b_limb) + al(4 * 3 * g_limb) > max_bytes) return fail(RMCM_OK);
+    const int64_t l_bytes = al(8 * A.nnz) + al(4 * M);
+    if (a_bytes + l_bytes + al(2 * 3 * b_limb) + al(4 * 3 * g_limb) > max_bytes) return fail(RMCM_OK);
     if (ldk * 2 > 160 * 1024) return fail(RMCM_OK);
+    // A panel (freed once the GEMMs are queued); A's light entries
+    // (compacted per row) and their counts (kept for the dense kernel)
     __half *Ad = nullptr;
+    char *amem = nullptr;
     RMCM_TRY(dev_alloc(h, (void **)&Ad, a_bytes));
+    if (dev_alloc(h, (void **)&amem, l_bytes) != RMCM_OK) {
+        dev_free(h, Ad, a_bytes);
+        h->last_error.clear();
+        return fail(RMCM_OK);
+    }
+    int32_t *lcol = (int32_t *)amem;
+    uint32_t *lval = (uint32_t *)(lcol + A.nnz);
+    int32_t *lcnt = (int32_t *)(amem + al(8 * A.nnz));
     auto fail2 = [&](int32_t rc) {
         dev_free(h, Ad, a_bytes);
+        dev_free(h, amem, l_bytes);
         return fail(rc);
     };
     {
@@ -205,7 +248,7 @@ int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint6
             return fail2(RMCM_OK);
         }
         const int grid = (int)std::min<int64_t>(M, (int64_t)h->sm_count * 8);
-        k_gather_a<<<grid, kGatherThreads, smem, s>>>(A, slot, (int32_t)ldk, Ad, stats);
+        k_gather_a<<<grid, kGatherThreads, smem, s>>>(A, slot, (int32_t)ldk, Ad, lcol, lval, lcnt, stats);
         h->launches++;
         RMCM_CUDA(h, cudaGetLastError());
     }
@@ -264,6 +307,11 @@ int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint6
     const uint64_t seen = ((uint64_t *)(h->h_pinned + 8))[0];
     if (bits * limbs < 64 && (seen >> (bits * limbs)) != 0) return fail3(RMCM_OK);
     dev_free(h, Ad, a_bytes);
+    dp.amem = amem;
+    dp.abytes = l_bytes;
+    dp.lcol = lcol;
+    dp.lval = lval;
+    dp.lcnt = lcnt;
     dp.mem = mem;
     dp.bytes = bd_bytes + g_bytes;
     dp.G = G;
@@ -279,6 +327,7 @@ int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint6
 }
 
 void dense_part_release(rmcm_handle *h, DensePart &dp) {
+    if (dp.amem) dev_free(h, dp.amem, dp.abytes);
     if (dp.mem) dev_free(h, dp.mem, dp.bytes);
     if (dp.sel) dev_free(h, dp.sel, dp.sel_bytes);
     dp = DensePart{};

@@ -207,15 +207,20 @@ int32_t fill_ones(rmcm_handle *h, void *val, int64_t nnz, int32_t valtype);
 int32_t convert_values(rmcm_handle *h, const rmcm_mat *src, int32_t valtype, rmcm_mat **out);
 // dense_gemm.cu: tensor-core part of a uint32 dense-bin product.  G holds
 // `limbs` FP32 panels (A.rows x ld, limb_stride apart); row r's uint32 part is
-// sum_l G_l[r][c] << (bits * l).  skip[u] flags the inner indices it covers.
+// sum_l G_l[r][c] << (bits * l).  skip[u] flags the inner indices it covers;
+// the entries of A on the others are listed per row (lcol, lval, lcnt).
 struct DensePart {
     const float *G = nullptr;
     int64_t ld = 0, limb_stride = 0;
     int32_t limbs = 0, bits = 0;
     int64_t heavy = 0;
     const uint8_t *skip = nullptr;
-    void *mem = nullptr, *sel = nullptr;
-    int64_t bytes = 0, sel_bytes = 0;
+    // A's light entries: row r's are lcol/lval[rowptr[r] .. + lcnt[r])
+    const int32_t *lcol = nullptr;
+    const uint32_t *lval = nullptr;
+    const int32_t *lcnt = nullptr;
+    void *mem = nullptr, *sel = nullptr, *amem = nullptr;
+    int64_t bytes = 0, sel_bytes = 0, abytes = 0;
 };
 int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint64_t bmax, DensePart &dp);
 void dense_part_release(rmcm_handle *h, DensePart &dp);

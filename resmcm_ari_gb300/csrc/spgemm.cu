@@ -1361,6 +1361,7 @@ struct DenseExtra {
     const float *G = nullptr;
     int64_t gld = 0, gstride = 0;
     const uint8_t *skip = nullptr;
+    const int32_t *lcnt = nullptr;   // with G: row r has lcnt[r] entries (A's light ones) from rowptr[r]
 };
 
 template <typename V, bool NUMERIC, bool TEMP, bool PRES = true>
@@ -1404,7 +1405,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
             if (s_abort) break;
         }
         const int32_t r = rows[ri];
-        const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
+        const int64_t a0 = A.rowptr[r], a1 = ex.lcnt ? a0 + ex.lcnt[r] : A.rowptr[r + 1];
         // A row that cannot overflow needs no checks, and when every input
         // value is >= 1 its counters alone mark presence (no count is 0).
         const bool checked = NUMERIC && (bin_of[r] & kRiskyBit) != 0;
@@ -2499,7 +2500,7 @@ DenseExtra dense_extra(const DenseTemp *t, bool single_pass) {
         e.gstride = t->dpart.limb_stride;
         e.glimbs = t->dpart.limbs;
         e.gbits = t->dpart.bits;
-        e.skip = t->dpart.skip;
+        e.lcnt = t->dpart.lcnt;
     }
     return e;
 }
@@ -2658,9 +2659,15 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                         // kernel takes its front
                         const int32_t *dl = temp->split ? temp->perm : list;
                         const int32_t dn = temp->split ? temp->n_front : n;
+                        // with a tensor-core part, A's light entries only
+                        DevCsr Al = A;
+                        if (temp->dpart.G) {
+                            Al.col = const_cast<int32_t *>(temp->dpart.lcol);
+                            Al.val = const_cast<uint32_t *>(temp->dpart.lval);
+                        }
                         if (dn > 0)
                             kern<<<std::max(1, std::min(grid, dn)), kDenseThreads, sm, s>>>(
-                                A, B, T, dl, dn, cnt, nullptr, 0, (int32_t)W, st, temp->stride, bin_of, positive,
+                                Al, B, T, dl, dn, cnt, nullptr, 0, (int32_t)W, st, temp->stride, bin_of, positive,
                                 b_distinct, h->abort_on_certain_overflow, dense_extra(temp, true));
                         if (temp->split) {
                             RMCM_CUDA(h, cudaEventRecord(h->ev_join, h->aux));
