@@ -452,22 +452,38 @@ __global__ void __launch_bounds__(kPackWarps * 32) k_pack_banked(DevCsr B, int32
 }
 
 // Row ids into per-bin lists laid out back to back (offsets from bin_count).
-__global__ void k_scatter(int64_t m, const uint8_t *bin_of, const int32_t *bin_count, int32_t *bin_cursor,
-                          int32_t *lists, int64_t *cnt) {
-    __shared__ int32_t off[kNumBins];
-    if (threadIdx.x == 0) {
+__global__ void __launch_bounds__(256) k_scatter(int64_t m, const uint8_t *bin_of, const int32_t *bin_count,
+                                                 int32_t *bin_cursor, int32_t *lists, int64_t *cnt) {
+    // slots are handed out per tile of 256 rows: lanes of a warp with the
+    // same bin take consecutive ranks (one shared add per warp and bin), the
+    // tile one global add per bin, so a million rows do not queue on a few
+    // global counters
+    __shared__ int32_t off[kNumBins], s_cnt[kNumBins], s_base[kNumBins];
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (tid == 0) {
         int32_t s = 0;
         for (int b = 0; b < kNumBins; b++) { off[b] = s; s += bin_count[b]; }
     }
-    __syncthreads();
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x) {
-        const int b = bin_of[r] & ~kRiskyBit;
-        if (b == kEmptyBin) {
-            cnt[r] = 0;   // rows without products have no entries
-            continue;
+    for (int64_t r0 = (int64_t)blockIdx.x * 256; r0 < m; r0 += (int64_t)gridDim.x * 256) {
+        if (tid < kNumBins) s_cnt[tid] = 0;
+        __syncthreads();
+        const int64_t r = r0 + tid;
+        int b = kEmptyBin;
+        if (r < m) {
+            b = bin_of[r] & ~kRiskyBit;
+            if (b == kEmptyBin) cnt[r] = 0;   // rows without products have no entries
         }
-        const int32_t pos = atomicAdd(bin_cursor + b, 1);
-        lists[off[b] + pos] = (int32_t)r;
+        const unsigned peers = __match_any_sync(kFull, b);
+        const int leader = __ffs(peers) - 1;
+        int32_t wbase = 0;
+        if (lane == leader && b != kEmptyBin) wbase = atomicAdd(&s_cnt[b], __popc(peers));
+        wbase = __shfl_sync(kFull, wbase, leader);
+        const int32_t rank = wbase + __popc(peers & ((1u << lane) - 1u));
+        __syncthreads();
+        if (tid < kNumBins && s_cnt[tid]) s_base[tid] = atomicAdd(bin_cursor + tid, s_cnt[tid]);
+        __syncthreads();
+        if (b != kEmptyBin) lists[off[b] + s_base[b] + rank] = (int32_t)r;
+        __syncthreads();
     }
 }
 
