@@ -1341,10 +1341,18 @@ RMCM_API int32_t rmcm_mat_download_async(rmcm_handle *h, rmcm_mat *m, int64_t *r
     RMCM_CUDA(h, cudaEventRecord(h->ev_fork, h->stream));
     RMCM_CUDA(h, cudaStreamWaitEvent(h->xfer, h->ev_fork, 0));
     cudaStream_t x = h->xfer;
-    if (rowptr) RMCM_CUDA(h, cudaMemcpyAsync(rowptr, m->d.rowptr, 8 * (m->d.rows + 1), cudaMemcpyDeviceToHost, x));
-    if (col && m->d.nnz) RMCM_CUDA(h, cudaMemcpyAsync(col, m->d.col, 4 * m->d.nnz, cudaMemcpyDeviceToHost, x));
-    if (val && m->d.nnz)
-        RMCM_CUDA(h, cudaMemcpyAsync(val, m->d.val, val_bytes(m->valtype) * m->d.nnz, cudaMemcpyDeviceToHost, x));
+    // pieces of at most 8 MB: the executor's small read-backs on the
+    // handle's stream get the copy engine between them
+    auto copy = [&](void *dst, const void *src, int64_t bytes) -> int32_t {
+        constexpr int64_t kPiece = 8LL << 20;
+        for (int64_t o = 0; o < bytes; o += kPiece)
+            RMCM_CUDA(h, cudaMemcpyAsync((char *)dst + o, (const char *)src + o, std::min(kPiece, bytes - o),
+                                         cudaMemcpyDeviceToHost, x));
+        return RMCM_OK;
+    };
+    if (rowptr) RMCM_TRY(copy(rowptr, m->d.rowptr, 8 * (m->d.rows + 1)));
+    if (col && m->d.nnz) RMCM_TRY(copy(col, m->d.col, 4 * m->d.nnz));
+    if (val && m->d.nnz) RMCM_TRY(copy(val, m->d.val, val_bytes(m->valtype) * m->d.nnz));
     if (!m->xfer_done) RMCM_CUDA(h, cudaEventCreateWithFlags(&m->xfer_done, cudaEventDisableTiming));
     RMCM_CUDA(h, cudaEventRecord(m->xfer_done, x));
     return RMCM_OK;
