@@ -1341,6 +1341,19 @@ RMCM_API int32_t rmcm_mat_download_async(rmcm_handle *h, rmcm_mat *m, int64_t *r
     RMCM_CUDA(h, cudaEventRecord(h->ev_fork, h->stream));
     RMCM_CUDA(h, cudaStreamWaitEvent(h->xfer, h->ev_fork, 0));
     cudaStream_t x = h->xfer;
+    {
+        // pinned destinations: SM stores (k_copy_out), so the copy engines stay
+        // free for the executor's small read-backs on the handle's stream
+        const void *src[3] = {m->d.rowptr, m->d.col, m->d.val};
+        void *dst[3] = {rowptr, m->d.nnz ? col : nullptr, m->d.nnz ? val : nullptr};
+        const int64_t bytes[3] = {8 * (m->d.rows + 1), 4 * m->d.nnz, val_bytes(m->valtype) * m->d.nnz};
+        if (copy_out_launch(src, dst, bytes, x)) {
+            h->launches++;
+            if (!m->xfer_done) RMCM_CUDA(h, cudaEventCreateWithFlags(&m->xfer_done, cudaEventDisableTiming));
+            RMCM_CUDA(h, cudaEventRecord(m->xfer_done, x));
+            return RMCM_OK;
+        }
+    }
     // pieces of at most 8 MB: the executor's small read-backs on the
     // handle's stream get the copy engine between them
     auto copy = [&](void *dst, const void *src, int64_t bytes) -> int32_t {

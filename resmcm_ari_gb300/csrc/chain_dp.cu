@@ -138,6 +138,58 @@ __global__ void __launch_bounds__(256) k_digest(DevCsr C, unsigned long long *ou
 
 }  // namespace
 
+namespace {
+
+// Copy of up to three device ranges into host memory (device addresses of
+// pinned host buffers) by SM stores: the copy engines stay free for the small
+// read-backs of the executor.  Ranges whose source and destination share
+// their 16-byte alignment move in 16-byte words between byte-wise ends.
+struct OutRange {
+    const char *src;
+    char *dst;
+    int64_t bytes;
+};
+
+__global__ void __launch_bounds__(512) k_copy_out(OutRange r0, OutRange r1, OutRange r2) {
+    const OutRange rs[3] = {r0, r1, r2};
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+    for (int i = 0; i < 3; i++) {
+        const OutRange r = rs[i];
+        if (r.bytes <= 0) continue;
+        const int64_t head = ((16 - ((uintptr_t)r.src & 15)) & 15) < r.bytes ? ((16 - ((uintptr_t)r.src & 15)) & 15)
+                                                                             : r.bytes;
+        const bool same = (((uintptr_t)r.src ^ (uintptr_t)r.dst) & 15) == 0;
+        const int64_t body = same ? (r.bytes - head) / 16 : 0;
+        const int64_t tail0 = same ? head + body * 16 : 0;
+        if (same) {
+            for (int64_t b = tid; b < head; b += nt) r.dst[b] = r.src[b];
+            const uint4 *s4 = (const uint4 *)(r.src + head);
+            uint4 *d4 = (uint4 *)(r.dst + head);
+            for (int64_t w = tid; w < body; w += nt) d4[w] = s4[w];
+        }
+        for (int64_t b = tail0 + tid; b < r.bytes; b += nt) r.dst[b] = r.src[b];
+    }
+}
+
+}  // namespace
+
+// Download of a result's arrays by k_copy_out on stream s; false when some
+// destination has no device address (pageable memory): the caller copies.
+bool copy_out_launch(const void *const *src, void *const *dst_host, const int64_t *bytes, cudaStream_t s) {
+    OutRange r[3] = {};
+    for (int i = 0; i < 3; i++) {
+        if (!dst_host[i] || bytes[i] <= 0) continue;
+        void *alias = nullptr;
+        if (cudaHostGetDevicePointer(&alias, dst_host[i], 0) != cudaSuccess || !alias) {
+            cudaGetLastError();
+            return false;
+        }
+        r[i] = OutRange{(const char *)src[i], (char *)alias, bytes[i]};
+    }
+    k_copy_out<<<16, 512, 0, s>>>(r[0], r[1], r[2]);
+    return cudaGetLastError() == cudaSuccess;
+}
+
 int32_t mat_digest_launch(rmcm_handle *h, const rmcm_mat *m, uint64_t *out_dev) {
     cudaStream_t s = h->stream;
     RMCM_CUDA(h, cudaMemsetAsync(out_dev, 0, 2 * sizeof(uint64_t), s));

@@ -194,6 +194,9 @@ void dev_free(rmcm_handle *h, void *p, int64_t bytes);
 int32_t scratch_reserve(rmcm_handle *h, int64_t bytes);
 int32_t mat_alloc(rmcm_handle *h, int64_t rows, int64_t cols, int64_t nnz, int32_t valtype, rmcm_mat **out);
 void mat_release(rmcm_handle *h, rmcm_mat *m);
+// Copies up to three device ranges into pinned host buffers with a small
+// kernel on stream s (chain_dp.cu); false if a buffer is not device-mapped.
+bool copy_out_launch(const void *const *src, void *const *dst_host, const int64_t *bytes, cudaStream_t s);
 // Read and clear the device status words; maps them to a status code.
 int32_t check_status(rmcm_handle *h);
 
