@@ -173,12 +173,28 @@ __global__ void __launch_bounds__(512) k_copy_out(OutRange r0, OutRange r1, OutR
 
 }  // namespace
 
+// Page-locked host memory (allocated or registered with CUDA).  Only such
+// buffers go through the copy kernels: a pageable buffer may be device-
+// addressable too (the GPU reaches all host memory here), but its owner may
+// free it as soon as the call returns, before an asynchronous kernel has read
+// it -- pageable copies stay on the copy engine, which stages them before
+// returning.
+static bool pinned_host(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
 // Download of a result's arrays by k_copy_out on stream s; false when some
-// destination has no device address (pageable memory): the caller copies.
+// destination is not page-locked: the caller copies.
 bool copy_out_launch(const void *const *src, void *const *dst_host, const int64_t *bytes, cudaStream_t s) {
     OutRange r[3] = {};
     for (int i = 0; i < 3; i++) {
         if (!dst_host[i] || bytes[i] <= 0) continue;
+        if (!pinned_host(dst_host[i])) return false;
         void *alias = nullptr;
         if (cudaHostGetDevicePointer(&alias, dst_host[i], 0) != cudaSuccess || !alias) {
             cudaGetLastError();
