@@ -101,7 +101,7 @@ class ProductStats(C.Structure):
                 ("bytes_a", C.c_int64), ("bytes_b_touched", C.c_int64), ("bytes_c", C.c_int64),
                 ("analyze_ms", C.c_double), ("symbolic_ms", C.c_double), ("numeric_ms", C.c_double),
                 ("valtype", C.c_int32), ("bin_rows", C.c_int32 * 8),
-                ("gemm_limbs", C.c_int32), ("gemm_inner", C.c_int64)]
+                ("gemm_limbs", C.c_int32), ("gemm_inner", C.c_int64), ("gemm_ms", C.c_double)]
 
     def as_dict(self) -> dict:
         d = {f: getattr(self, f) for f, _ in self._fields_ if f != "bin_rows"}

@@ -1104,7 +1104,10 @@ RMCM_API int32_t rmcm_get_product_stats(rmcm_handle *h, rmcm_product_stats *out,
         if (cudaEventElapsedTime(&a, r.ev[0], r.ev[1]) != cudaSuccess) a = 0;
         if (cudaEventElapsedTime(&b, r.ev[2], r.ev[3]) != cudaSuccess) b = 0;
         if (cudaEventElapsedTime(&c, r.ev[4], r.ev[5]) != cudaSuccess) c = 0;
+        float gm = 0;
+        if (r.st.gemm_limbs > 0 && cudaEventElapsedTime(&gm, r.ev[6], r.ev[7]) != cudaSuccess) gm = 0;
         cudaGetLastError();   // an unrecorded event must not leak into later launch checks
+        r.st.gemm_ms = gm;
         r.st.analyze_ms = a;
         r.st.symbolic_ms = b;
         r.st.numeric_ms = c;

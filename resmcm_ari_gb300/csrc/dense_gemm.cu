@@ -179,7 +179,8 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather_b(DevCsr B, const int
 // on success dp.G holds L limb panels (rows x ld floats each) and dp.skip
 // flags the heavy inner indices; otherwise dp stays empty (and the product
 // runs sparse).  bmax: an upper bound on B's values.
-int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint64_t bmax, DensePart &dp) {
+int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint64_t bmax, DensePart &dp,
+                         cudaEvent_t ev_begin, cudaEvent_t ev_end) {
     dp = DensePart{};
     const int32_t inv_density = h->tune.gemm_inv_density;
     if (inv_density <= 0 || A.rows == 0 || B.cols == 0 || A.cols == 0) return RMCM_OK;
@@ -294,6 +295,7 @@ int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint6
     if (cublasSetStream(cb, s) != CUBLAS_STATUS_SUCCESS) return fail3(set_error(h, RMCM_ECUDA, "cublasSetStream"));
     // row-major G_l (M x N) = Ad (M x ldk) Bd_l (ldk x N): column-major G_l^T = Bd_l^T Ad^T
     const float one = 1.0f, zero = 0.0f;
+    if (ev_begin) cudaEventRecord(ev_begin, s);
     for (int l = 0; l < limbs; l++) {
         const cublasStatus_t st = cublasGemmEx(cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)N, (int)M, (int)ldk, &one,
                                                Bd + l * b_limb, CUDA_R_16F, (int)ldn, Ad, CUDA_R_16F, (int)ldk,
@@ -301,6 +303,7 @@ int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint6
                                                CUBLAS_GEMM_DEFAULT);
         if (st != CUBLAS_STATUS_SUCCESS) return fail3(set_error(h, RMCM_ECUDA, "dense part: cublasGemmEx failed"));
     }
+    if (ev_end) cudaEventRecord(ev_end, s);
     // the B gather saw no value wider than the limbs
     RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned + 8, stats + 2, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
     RMCM_CUDA(h, cudaStreamSynchronize(s));

@@ -71,7 +71,7 @@ struct Tuning {
 // (analyze, symbolic + scan, numeric).
 struct ProdRecord {
     rmcm_product_stats st{};
-    cudaEvent_t ev[6] = {};
+    cudaEvent_t ev[8] = {};   // analysis, symbolic, numeric passes; [6..7] the tensor-core GEMMs
 };
 
 // Sizes one SpGEMM read back from the device, kept so that the same product
@@ -225,7 +225,9 @@ struct DensePart {
     void *mem = nullptr, *sel = nullptr, *amem = nullptr;
     int64_t bytes = 0, sel_bytes = 0, abytes = 0;
 };
-int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint64_t bmax, DensePart &dp);
+// ev_begin / ev_end (may be null) are recorded around the GEMMs.
+int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint64_t bmax, DensePart &dp,
+                         cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr);
 void dense_part_release(rmcm_handle *h, DensePart &dp);
 void cublas_destroy(rmcm_handle *h);
 // estimator.cu: c_dev[len*len] on the device

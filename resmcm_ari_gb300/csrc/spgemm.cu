@@ -2979,7 +2979,8 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         if (want) {
             uint64_t bmax = 1;
             if (!Bm->ones) memcpy(&bmax, (int32_t *)h->h_pinned + 58, sizeof(uint64_t));
-            const int32_t drc = dense_part_build(h, A, B, bmax, dtemp.dpart);
+            const int32_t drc = dense_part_build(h, A, B, bmax, dtemp.dpart, rec ? h->prof[rec_idx].ev[6] : nullptr,
+                                                 rec ? h->prof[rec_idx].ev[7] : nullptr);
             if (drc != RMCM_OK) {
                 dense_part_release(h, dtemp.dpart);
                 if (dtemp.pk_mem) dev_free(h, dtemp.pk_mem, dtemp.pk_bytes);
