@@ -2256,6 +2256,10 @@ __global__ void __launch_bounds__(kRankThreads) k_rank_split_val(DevCsr A, DevCs
     if (__syncthreads_or(ovf) && threadIdx.x == 0) raise_status(st, kOverflow);
 }
 
+__global__ void k_iota(int32_t *v, int32_t n) {
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = i;
+}
+
 // Compacts TEMP-mode slots into C: row rows[ri] has cnt = rowptr[r+1]-rowptr[r]
 // entries at slot ri of the temporary.
 template <typename V>
@@ -2457,7 +2461,7 @@ struct DenseTemp {
     int32_t *col = nullptr;
     void *val = nullptr;
     int64_t stride = 0;
-    int64_t bytes = 0;
+    int64_t bytes = 0, vbytes = 0;   // the two allocations (columns, counts)
     bool no_risky = false;            // no row can overflow: with positive inputs, no presence bytes
     // packed copy of B (k_pack_banked) for the plain path of single-window rows
     const uint32_t *pk = nullptr;
@@ -2909,14 +2913,19 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         const int64_t bytes = (int64_t)counts[kBinDense] * stride * (4 + (int64_t)sizeof(V));
         const int64_t room = h->budget - h->in_use;
         if (replay || (bytes <= h->tune.dense_temp_max_bytes && bytes < room / 2)) {
-            void *p = nullptr;
-            if (dev_alloc(h, &p, bytes) == RMCM_OK) {
+            // columns and counts in two allocations: a product whose rows all
+            // come out full can take them over as its own arrays
+            const int64_t cb = (int64_t)counts[kBinDense] * stride * 4, vb = bytes - cb;
+            void *pc = nullptr, *pv = nullptr;
+            if (dev_alloc(h, &pc, cb) == RMCM_OK && dev_alloc(h, &pv, vb) == RMCM_OK) {
                 dtemp.active = true;
-                dtemp.col = (int32_t *)p;
-                dtemp.val = (char *)p + (int64_t)counts[kBinDense] * stride * 4;
+                dtemp.col = (int32_t *)pc;
+                dtemp.val = pv;
                 dtemp.stride = stride;
-                dtemp.bytes = bytes;
+                dtemp.bytes = cb;
+                dtemp.vbytes = vb;
             } else {
+                if (pc) dev_free(h, pc, cb);
                 h->last_error.clear();
             }
         }
@@ -2984,7 +2993,10 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
             if (drc != RMCM_OK) {
                 dense_part_release(h, dtemp.dpart);
                 if (dtemp.pk_mem) dev_free(h, dtemp.pk_mem, dtemp.pk_bytes);
-                if (dtemp.active) dev_free(h, dtemp.col, dtemp.bytes);
+                if (dtemp.active) {
+                    dev_free(h, dtemp.col, dtemp.bytes);
+                    dev_free(h, dtemp.val, dtemp.vbytes);
+                }
                 return drc;
             }
         }
@@ -3129,7 +3141,10 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         if (dtemp.pk_mem) dev_free(h, dtemp.pk_mem, dtemp.pk_bytes);
         dtemp.pk_mem = nullptr;
         dtemp.pk = nullptr;
-        if (dtemp.active) dev_free(h, dtemp.col, dtemp.bytes);
+        if (dtemp.active) {
+            dev_free(h, dtemp.col, dtemp.bytes);
+            dev_free(h, dtemp.val, dtemp.vbytes);
+        }
         if (dtemp.split) dev_free(h, dtemp.split_mem, dtemp.split_bytes);
         dtemp.active = false;
         dtemp.split = false;
@@ -3145,7 +3160,17 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         return rc;
     }
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[2], s);
-    rc = launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap, &dtemp, bin_of, positive, Bm->distinct, &rsplit);
+    // every row single-pass dense (no split): slot i of the temporary is row i,
+    // so a product whose rows all come out full can keep it as C
+    const bool all_dense = dtemp.active && !dtemp.split && counts[kBinDense] == m;
+    if (all_dense) {
+        k_iota<<<grid_for(h, m, 256, 8), 256, 0, s>>>(lists, (int32_t)m);
+        h->launches++;
+        if (cudaGetLastError() != cudaSuccess) rc = set_error(h, RMCM_ECUDA, "row list launch");
+    }
+    if (rc == RMCM_OK)
+        rc = launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap, &dtemp,
+                                   bin_of, positive, Bm->distinct, &rsplit);
     if (rc == RMCM_OK)
         rc = scan_rowptr(h, cnt, m, C->d.rowptr, tiles, (unsigned long long *)(small + 44), replay ? plan->nnz : -1);
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[3], s);
@@ -3182,9 +3207,21 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
             return set_error(h, RMCM_EOVERFLOW, "path counts exceed the value type");
         }
     }
-    if (rc == RMCM_OK) rc = mat_alloc(h, m, B.cols, nnz, Am->valtype, &C);
+    // every row full: the temporary's layout (row i at i * stride) is C's
+    const bool adopt = rc == RMCM_OK && all_dense && nnz == m * dtemp.stride;
+    if (adopt) {
+        C->d.col = dtemp.col;
+        C->d.val = dtemp.val;
+        C->d.nnz = nnz;
+        C->bytes += (4 + (int64_t)sizeof(V)) * nnz;
+        dtemp.active = false;   // owned by C now
+    } else if (rc == RMCM_OK) {
+        rc = mat_alloc(h, m, B.cols, nnz, Am->valtype, &C);
+    }
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[4], s);
-    if (rc == RMCM_OK) rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap, &dtemp, bin_of, positive, Bm->distinct, &rsplit);
+    if (rc == RMCM_OK && !adopt)
+        rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap, &dtemp,
+                                  bin_of, positive, Bm->distinct, &rsplit);
     const int32_t gemm_limbs = dtemp.dpart.G ? dtemp.dpart.limbs : 0;
     const int64_t gemm_inner = dtemp.dpart.G ? dtemp.dpart.heavy : 0;
     drop_cursors();
