@@ -2941,38 +2941,6 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         dtemp.no_risky = risky_rows == 0;
     }
     {
-        // Pack B when the dense bin reuses its entries many times and every
-        // value fits beside the column bits.
-        int32_t cbits = 0;
-        if (replay) {
-            cbits = plan->pack_cbits;
-        } else if (pack_cand && counts[kBinDense] > 0 && flops_total >= kPackReuse * B.nnz) {
-            uint64_t bmax = 1;
-            if (!Bm->ones) memcpy(&bmax, (int32_t *)h->h_pinned + 58, sizeof(uint64_t));
-            const int32_t cb = 32 - __builtin_clz((uint32_t)(B.cols - 1));
-            if (cb < 32 && bmax < (1ull << (32 - cb))) cbits = cb;
-        }
-        if (cbits > 0) {
-            void *p = nullptr;
-            if (dev_alloc(h, &p, 4 * B.nnz) == RMCM_OK) {
-                dtemp.pk = (const uint32_t *)p;
-                dtemp.cbits = cbits;
-                dtemp.pk_mem = p;
-                dtemp.pk_bytes = 4 * B.nnz;
-                k_pack_banked<<<grid_for(h, B.rows * 32, kPackWarps * 32, 6), kPackWarps * 32, 0, s>>>(
-                    B, cbits, (uint32_t *)p, h->d_status);
-                h->launches++;
-                RMCM_CUDA(h, cudaGetLastError());
-            } else if (replay) {
-                return set_error(h, RMCM_ENOMEM, "replay: packed copy of B could not be allocated");
-            } else {
-                h->last_error.clear();
-                cbits = 0;
-            }
-        }
-        if (record) plan->pack_cbits = cbits;
-    }
-    {
         // Tensor-core part (dense_gemm.cu): every row with products in the
         // single-pass dense bin, uint32, positive, no row able to overflow, a
         // large product whose rows need no split over CTAs (skewed rows keep
@@ -3000,6 +2968,39 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
                 return drc;
             }
         }
+    }
+    {
+        // Pack B when the dense bin reuses its entries many times and every
+        // value fits beside the column bits.
+        int32_t cbits = 0;
+        if (replay) {
+            cbits = plan->pack_cbits;
+        } else if (pack_cand && counts[kBinDense] > 0 && flops_total >= kPackReuse * B.nnz && !dtemp.dpart.G) {
+            // (with a tensor-core part the light rows left are short: no packing)
+            uint64_t bmax = 1;
+            if (!Bm->ones) memcpy(&bmax, (int32_t *)h->h_pinned + 58, sizeof(uint64_t));
+            const int32_t cb = 32 - __builtin_clz((uint32_t)(B.cols - 1));
+            if (cb < 32 && bmax < (1ull << (32 - cb))) cbits = cb;
+        }
+        if (cbits > 0) {
+            void *p = nullptr;
+            if (dev_alloc(h, &p, 4 * B.nnz) == RMCM_OK) {
+                dtemp.pk = (const uint32_t *)p;
+                dtemp.cbits = cbits;
+                dtemp.pk_mem = p;
+                dtemp.pk_bytes = 4 * B.nnz;
+                k_pack_banked<<<grid_for(h, B.rows * 32, kPackWarps * 32, 6), kPackWarps * 32, 0, s>>>(
+                    B, cbits, (uint32_t *)p, h->d_status);
+                h->launches++;
+                RMCM_CUDA(h, cudaGetLastError());
+            } else if (replay) {
+                return set_error(h, RMCM_ENOMEM, "replay: packed copy of B could not be allocated");
+            } else {
+                h->last_error.clear();
+                cbits = 0;
+            }
+        }
+        if (record) plan->pack_cbits = cbits;
     }
     // Dense rows with far more products than a fair share of the device are
     // split over several CTAs (k_dense_split).
