@@ -282,7 +282,7 @@ RMCM_API int32_t rmcm_estimate_metapath(rmcm_handle *h, rmcm_graph *g, const cha
  *                    (exact: see dense_gemm.cu); 0 = never (0 .. 65536)
  *   gemm_min_mflops  products with fewer multiply-adds (millions) never try
  *                    it (>= 0)
- * Defaults: 32, 4096, 16, 2048, 0.5, 512, 512.  A batch keeps the values it
+ * Defaults: 4, 4096, 16, 2048, 0.5, 512, 512.  A batch keeps the values it
  * was created with (its recorded products never use the GEMM). */
 typedef struct rmcm_tuning {
     int32_t threads_per_row;

@@ -118,7 +118,7 @@ int32_t mat_alloc(rmcm_handle *h, int64_t rows, int64_t cols, int64_t nnz, int32
 
 void mat_release(rmcm_handle *h, rmcm_mat *m) {
     if (!m) return;
-    if (m->rowsum) dev_free(h, m->rowsum, 8 * (m->d.rows + 1));
+    if (m->rowsum) dev_free(h, m->rowsum, 8 * (m->d.rows + 1) + 8 * m->d.rows);
     if (m->est_long) dev_free(h, m->est_long, 4 * (int64_t)m->n_est_long);
     if (m->xfer_done) cudaEventDestroy(m->xfer_done);
     dev_free(h, m->d.rowptr, 8 * (m->d.rows + 1));

@@ -30,6 +30,9 @@ struct DevCsr {
     int32_t *col = nullptr;
     void *val = nullptr;
     const uint64_t *rowsum = nullptr;   // per-row sum of values (saturating); null when every value is 1
+    // with rowsum: per row {length, row sum saturated to 0xffffffff}, one
+    // 8-byte gather where the analysis of a uint32 product needs both
+    const uint2 *info = nullptr;
 };
 
 // Device-side status words, one int each (set with atomicOr, never cleared by kernels).
@@ -54,7 +57,7 @@ struct Tuning {
     // 1..16 = that many lanes per row for rows of at most that many products
     // (k_micro), the rest of the short rows a warp each; 128 = no short-row
     // bins, short rows go to the 128-thread CTAs of the 512-slot hash bin
-    int32_t threads_per_row = 32;
+    int32_t threads_per_row = 4;
     int32_t hash_max_flops = 4096;  // rows above go to the dense / rank bins
     int32_t dense_ratio = 16;       // dense when flops * dense_ratio >= cols (and one window covers cols)
     int32_t warp_max_flops = 2048;  // output width <= 2048 and at most this many flops: warp bin (0: none)
@@ -105,6 +108,7 @@ struct rmcm_mat {
     bool positive = false;              // every value is >= 1 (a counter > 0 then marks presence)
     bool distinct = false;              // no column repeats within a row
     uint64_t *rowsum = nullptr;         // lazily computed row sums (device, rows + 1: the largest value last), owned
+                                        // followed by `rows` uint2 {length, sum saturated to 32 bits}
     int64_t max_row = -1;               // longest row (entries); -1 when unknown
     // rows longer than kEstLongRow entries, ascending (device), when known:
     // the estimator gives each a whole CTA

@@ -226,6 +226,39 @@ __device__ __forceinline__ void analyze_entries(const DevCsr &A, const DevCsr &B
                                                 int64_t &f, unsigned long long &srow) {
     const V *Aval = (const V *)A.val;
     int64_t k = k0;
+    if (sizeof(V) == 4 && B.info) {
+        // uint32: one 8-byte gather per entry (length, row sum saturated to
+        // 32 bits, read as 2^32 when saturated: the bound stays an upper
+        // bound and the exact total stays a lower one)
+        auto bsum_of = [](uint32_t s) -> unsigned long long { return s == 0xffffffffu ? (1ull << 32) : s; };
+        for (; k + 3 * (int64_t)step < k1; k += 4 * (int64_t)step) {
+            int32_t a[4];
+            unsigned long long av[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                a[u] = A.col[k + u * step];
+                av[u] = Aval[k + u * step];
+            }
+            uint2 in[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) in[u] = B.info[a[u]];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                f += in[u].x;
+                const unsigned long long bs = bsum_of(in[u].y);
+                const unsigned long long prod = __umul64hi(av[u], bs) ? ~0ull : av[u] * bs;
+                srow = sat_add(srow, prod);
+            }
+        }
+        for (; k < k1; k += step) {
+            const uint2 in = B.info[A.col[k]];
+            f += in.x;
+            const unsigned long long av = Aval[k], bs = bsum_of(in.y);
+            const unsigned long long prod = __umul64hi(av, bs) ? ~0ull : av * bs;
+            srow = sat_add(srow, prod);
+        }
+        return;
+    }
     // four entries per step: their gathers are independent and overlap
     for (; k + 3 * (int64_t)step < k1; k += 4 * (int64_t)step) {
         int32_t a[4];
@@ -344,9 +377,10 @@ __global__ void __launch_bounds__(256) k_analyze_long_finish(DevCsr A, DevCsr B,
 }
 
 // Saturating row sums of a matrix's values (warp per row); out[M.rows]
-// (zeroed by the caller) receives the largest value.
+// (zeroed by the caller) receives the largest value, info[r] the row's
+// {length, sum saturated to 0xffffffff}.
 template <typename V>
-__global__ void k_rowsum(DevCsr M, uint64_t *out) {
+__global__ void k_rowsum(DevCsr M, uint64_t *out, uint2 *info) {
     const int lane = threadIdx.x & 31;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const V *v = (const V *)M.val;
@@ -360,7 +394,11 @@ __global__ void k_rowsum(DevCsr M, uint64_t *out) {
         }
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) sum = sat_add(sum, __shfl_xor_sync(kFull, sum, d));
-        if (lane == 0) out[r] = sum;
+        if (lane == 0) {
+            out[r] = sum;
+            info[r] = make_uint2((uint32_t)min(M.rowptr[r + 1] - M.rowptr[r], (int64_t)0xffffffff),
+                                 sum > 0xffffffffull ? 0xffffffffu : (uint32_t)sum);
+        }
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
@@ -2756,15 +2794,17 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     // row sums of B bound the counts of every output row (computed once per matrix)
     if (!Bm->ones && !Bm->rowsum && Bm->d.rows > 0) {
         rmcm_mat *Bw = const_cast<rmcm_mat *>(Bm);
-        RMCM_TRY(dev_alloc(h, (void **)&Bw->rowsum, 8 * (Bm->d.rows + 1)));
+        RMCM_TRY(dev_alloc(h, (void **)&Bw->rowsum, 8 * (Bm->d.rows + 1) + 8 * Bm->d.rows));
         RMCM_CUDA(h, cudaMemsetAsync(Bw->rowsum + Bm->d.rows, 0, 8, s));
-        k_rowsum<V><<<grid_for(h, Bm->d.rows * 32, 256, 8), 256, 0, s>>>(Bm->d, Bw->rowsum);
+        k_rowsum<V><<<grid_for(h, Bm->d.rows * 32, 256, 8), 256, 0, s>>>(Bm->d, Bw->rowsum,
+                                                                          (uint2 *)(Bw->rowsum + Bm->d.rows + 1));
         h->launches++;
         RMCM_CUDA(h, cudaGetLastError());
     }
     const DevCsr A = Am->d;
     DevCsr B = Bm->d;
     B.rowsum = Bm->ones ? nullptr : Bm->rowsum;
+    B.info = B.rowsum ? (const uint2 *)(Bm->rowsum + Bm->d.rows + 1) : nullptr;
     const bool positive = Am->positive && Bm->positive;
     const int64_t m = A.rows;
     // scratch layout: flops[m] i64 | cnt[m] i64 | tile sums | bin_of[m] u8 | lists[m] i32 | small counters | cursors

@@ -155,6 +155,6 @@ def test_bad_tuning_is_rejected(native, engine):
                {"warp_max_flops": -1}, {"warp_max_flops": 70000}):
         with pytest.raises(native.RmcmError):
             engine.set_tuning(**kw)
-    assert engine.get_tuning() == {"threads_per_row": 32, "hash_max_flops": 4096, "dense_ratio": 16,
+    assert engine.get_tuning() == {"threads_per_row": 4, "hash_max_flops": 4096, "dense_ratio": 16,
                                    "warp_max_flops": 2048, "hash_load": 0.5, "gemm_inv_density": 512,
                                    "gemm_min_mflops": 512}
