@@ -157,6 +157,7 @@ struct AnalyzeOut {
     unsigned long long *dense_max_flops;
     unsigned long long *rank_max_flops;
     int32_t *risky_rows;
+    unsigned long long *max_total;        // largest row total bound S
 };
 
 struct AnalyzeShared {
@@ -167,6 +168,7 @@ struct AnalyzeShared {
     unsigned long long flops;
     unsigned long long max_flops;
     unsigned long long max_rank_flops;
+    unsigned long long max_total;
 };
 
 __device__ __forceinline__ void analyze_shared_init(AnalyzeShared &sh) {
@@ -178,6 +180,7 @@ __device__ __forceinline__ void analyze_shared_init(AnalyzeShared &sh) {
         sh.flops = 0;
         sh.max_flops = 0;
         sh.max_rank_flops = 0;
+        sh.max_total = 0;
     }
 }
 
@@ -190,6 +193,7 @@ __device__ __forceinline__ void analyze_shared_flush(AnalyzeShared &sh, const An
         if (sh.max_rank_flops) atomicMax(o.rank_max_flops, sh.max_rank_flops);
         if (sh.certain) atomicOr(o.certain, 1);
         if (sh.risky) atomicAdd(o.risky_rows, sh.risky);
+        if (sh.max_total) atomicMax(o.max_total, sh.max_total);
     }
 }
 
@@ -206,6 +210,7 @@ __device__ __forceinline__ void analyze_row(int64_t r, int64_t f, unsigned long 
     o.bin_of[r] = (uint8_t)(b | (risky ? kRiskyBit : 0));
     if (f) atomicAdd(&sh.flops, (unsigned long long)f);
     if (risky && b != kEmptyBin) atomicAdd(&sh.risky, 1);
+    if (sizeof(V) == 4 && risky) atomicMax(&sh.max_total, srow);
     if (sizeof(V) == 4 && risky) {
         const unsigned long long distinct = (unsigned long long)min(f, ncols);
         if (srow == ~0ull || srow / vmax > distinct) sh.certain = 1;
@@ -2834,7 +2839,8 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     // [44..45] longest C row (u64), [46] unsplit dense rows, [48..51]
     // profiling sums, [52] rank split slots, [53] unsplit rank rows,
     // [54..55] largest rank-row flops (u64), [56] rows that may overflow,
-    // [58..59] largest value of B (u64, when B may be packed)
+    // [58..59] largest value of B (u64, when B may be packed), [60..61]
+    // largest total bound S of a row that may overflow (uint32)
     int32_t *small = (int32_t *)(sc + o_small);
     RMCM_CUDA(h, cudaMemsetAsync(small, 0, 256, s));
     // B may be packed for the dense bin (uint32, positive, one window)
@@ -2865,8 +2871,16 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         bp.warp_max = h->tune.warp_max_flops;
     }
     if (m > 0) {
-        AnalyzeOut ao{flops, bin_of, small, small + 16, (unsigned long long *)(small + 32), small + 40,
-                      (unsigned long long *)(small + 36), (unsigned long long *)(small + 54), small + 56};
+        AnalyzeOut ao{flops,
+                      bin_of,
+                      small,
+                      small + 16,
+                      (unsigned long long *)(small + 32),
+                      small + 40,
+                      (unsigned long long *)(small + 36),
+                      (unsigned long long *)(small + 54),
+                      small + 56,
+                      (unsigned long long *)(small + 60)};
         // rows longer than kLongAnalyze entries: walked by the whole grid
         const bool long_rows = Am->max_row > kLongAnalyze;
         const int64_t max_long = A.nnz / kLongAnalyze + 1;
@@ -2914,6 +2928,15 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         dense_max_alen = ((int32_t *)h->h_pinned)[16];
         memcpy(&flops_total, (int32_t *)h->h_pinned + 32, sizeof(int64_t));
         certain = ((int32_t *)h->h_pinned)[40] != 0;
+        if (sizeof(V) == 4 && h->abort_on_certain_overflow && !certain) {
+            // a row whose total exceeds 16 x 2^32 averages more than 2^32/128
+            // per column: with skewed counts an entry overflows all but
+            // surely, so widen before computing (a wrong guess only costs
+            // uint64 arithmetic)
+            uint64_t mt = 0;
+            memcpy(&mt, (int32_t *)h->h_pinned + 60, sizeof(uint64_t));
+            if (mt / 16 > 0xffffffffull) certain = true;
+        }
     }
     if (record) {
         memcpy(plan->counts, counts, sizeof(counts));
