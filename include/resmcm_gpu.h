@@ -105,7 +105,7 @@ typedef struct rmcm_product_stats {
     double analyze_ms, symbolic_ms, numeric_ms;  /* CUDA-event times on the handle's stream */
     int32_t valtype;
     int32_t bin_rows[8];                /* rows per bin: tiny, hash512, hash2k, hash8k, dense, rank, micro, warp */
-    int32_t gemm_limbs;                 /* limbs of B in the tensor-core GEMM (0: no GEMM part) */
+    int32_t gemm_limbs;                 /* limb pairs (A x B) of the tensor-core GEMM (0: no GEMM part) */
     int64_t gemm_inner;                 /* inner indices multiplied by that GEMM */
     double gemm_ms;                     /* CUDA-event time of its GEMM calls */
 } rmcm_product_stats;

@@ -148,11 +148,12 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather_a(DevCsr A, const int
 // Limb l of the heavy rows of B: Bd[l][h][c] = (B[list[h]][c] >> (bits l)) &
 // (2^bits - 1) as FP16 (ld columns, zero elsewhere).  stats[2] = largest
 // value seen (checked against the limbs).
+template <typename V>
 __global__ void __launch_bounds__(kGatherThreads) k_gather_b(DevCsr B, const int32_t *list, int32_t nh, int32_t ld,
                                                              int32_t limbs, int32_t bits, __half *Bd,
                                                              int64_t limb_stride, unsigned long long *stats) {
-    const uint32_t *bv = (const uint32_t *)B.val;
-    const uint32_t mask = (1u << bits) - 1u;
+    const V *bv = (const V *)B.val;
+    const V mask = ((V)1 << bits) - (V)1;
     unsigned long long mx = 0;
     for (int64_t h = blockIdx.x; h < nh; h += gridDim.x) {
         const int32_t u = list[h];
@@ -162,15 +163,93 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather_b(DevCsr B, const int
         }
         __syncthreads();
         for (int64_t k = B.rowptr[u] + threadIdx.x; k < B.rowptr[u + 1]; k += kGatherThreads) {
-            const uint32_t v = bv[k];
+            const V v = bv[k];
             const int32_t c = B.col[k];
-            mx = v > mx ? v : mx;
+            mx = (unsigned long long)v > mx ? (unsigned long long)v : mx;
             for (int l = 0; l < limbs; l++)
-                Bd[l * limb_stride + h * (int64_t)ld + c] = __uint2half_rn((v >> (bits * l)) & mask);
+                Bd[l * limb_stride + h * (int64_t)ld + c] = __uint2half_rn((uint32_t)((v >> (bits * l)) & mask));
         }
         __syncthreads();
     }
     if (mx) atomicMax(stats + 2, mx);
+}
+
+// uint64 products: per row of A the number of heavy entries and the largest
+// heavy value (stats[3], stats[4]: maxima over rows).  A warp per row.
+__global__ void k_heavy_stats64(DevCsr A, const int32_t *slot, unsigned long long *stats) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t *av = (const uint64_t *)A.val;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned long long cmax = 0, vmax = 0;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < A.rows; r += nwarps) {
+        unsigned long long c = 0;
+        for (int64_t k = A.rowptr[r] + lane; k < A.rowptr[r + 1]; k += 32) {
+            if (slot[A.col[k]] >= 0) {
+                c++;
+                vmax = av[k] > vmax ? av[k] : vmax;
+            }
+        }
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) c += __shfl_xor_sync(0xffffffffu, c, d);
+        cmax = c > cmax ? c : cmax;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, vmax, d);
+        vmax = o > vmax ? o : vmax;
+    }
+    if (lane == 0) {
+        if (cmax) atomicMax(stats + 3, cmax);
+        if (vmax) atomicMax(stats + 4, vmax);
+    }
+}
+
+// uint64 row panels of A: limb l of each heavy value, (A[r][u] >> (bits l))
+// & (2^bits - 1) as FP16 at Ad[l][r][slot[u]]; the light entries compacted
+// per row as for uint32.
+__global__ void __launch_bounds__(kGatherThreads) k_gather_a64(DevCsr A, const int32_t *slot, int32_t ld,
+                                                               int32_t limbs, int32_t bits, __half *Ad,
+                                                               int64_t limb_stride, int32_t *lcol, uint64_t *lval,
+                                                               int32_t *lcnt) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __half *row = (__half *)smem;
+    __shared__ int32_t s_light;
+    const int lane = threadIdx.x & 31;
+    const uint64_t *av = (const uint64_t *)A.val;
+    const uint64_t mask = (1ull << bits) - 1ull;
+    for (int64_t r = blockIdx.x; r < A.rows; r += gridDim.x) {
+        const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
+        if (threadIdx.x == 0) s_light = 0;
+        __syncthreads();
+        for (int l = 0; l < limbs; l++) {
+            for (int i = threadIdx.x; i < ld / 8; i += kGatherThreads) ((uint4 *)row)[i] = make_uint4(0, 0, 0, 0);
+            __syncthreads();
+            for (int64_t k0 = a0; k0 < a1; k0 += kGatherThreads) {
+                const int64_t k = k0 + threadIdx.x;
+                const int32_t c = k < a1 ? A.col[k] : -1;
+                const int32_t sl = c >= 0 ? slot[c] : -1;
+                const uint64_t v = k < a1 ? av[k] : 0ull;
+                if (sl >= 0) row[sl] = __uint2half_rn((uint32_t)((v >> (bits * l)) & mask));
+                if (l == 0) {
+                    const bool light = c >= 0 && sl < 0;
+                    const unsigned lb = __ballot_sync(0xffffffffu, light);
+                    int base = 0;
+                    if (lane == 0 && lb) base = atomicAdd(&s_light, __popc(lb));
+                    base = __shfl_sync(0xffffffffu, base, 0);
+                    if (light) {
+                        const int64_t o = a0 + base + __popc(lb & ((1u << lane) - 1u));
+                        lcol[o] = c;
+                        lval[o] = v;
+                    }
+                }
+            }
+            __syncthreads();
+            uint4 *dst = (uint4 *)(Ad + l * limb_stride + r * (int64_t)ld);
+            for (int i = threadIdx.x; i < ld / 8; i += kGatherThreads) dst[i] = ((const uint4 *)row)[i];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) lcnt[r] = s_light;
+    }
 }
 
 }  // namespace
@@ -277,7 +356,7 @@ int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint6
         dev_free(h, mem, bd_bytes + g_bytes);
         return fail2(rc);
     };
-    k_gather_b<<<(int)std::min<int64_t>(nh, (int64_t)h->sm_count * 8), kGatherThreads, 0, s>>>(
+    k_gather_b<uint32_t><<<(int)std::min<int64_t>(nh, (int64_t)h->sm_count * 8), kGatherThreads, 0, s>>>(
         B, list, (int32_t)nh, (int32_t)ldn, limbs, bits, Bd, b_limb, stats);
     h->launches++;
     if (ldk > nh) {
@@ -322,6 +401,176 @@ int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint6
     dp.limb_stride = g_limb;
     dp.limbs = limbs;
     dp.bits = bits;
+    dp.heavy = nh;
+    dp.sel = sel;
+    dp.sel_bytes = sel_bytes;
+    dp.skip = flag;
+    return RMCM_OK;
+}
+
+// uint64 form: A's heavy values are split into limbs as well, and the heavy
+// indices into chunks of kc so that every partial sum of a GEMM output,
+// at most min(heavy entries of a row, kc) x (A limb max) x (B limb max),
+// stays <= 2^24.  G holds la x lb x nq panels, ((i lb + j) nq + q) in order;
+// the row's counter takes sum G << (bits (i + j)) modulo 2^64.
+int32_t dense_part_build64(rmcm_handle *h, const DevCsr &A, const DevCsr &B, DensePart &dp, cudaEvent_t ev_begin,
+                           cudaEvent_t ev_end) {
+    dp = DensePart{};
+    const int32_t inv_density = h->tune.gemm_inv_density;
+    if (inv_density <= 0 || A.rows == 0 || B.cols == 0 || A.cols == 0) return RMCM_OK;
+    cudaStream_t s = h->stream;
+    const int64_t M = A.rows, N = B.cols, K = A.cols;
+    const int64_t ldn = (N + 7) / 8 * 8;
+    const double thr = (double)M * (double)N / (double)inv_density;
+    auto al = [](int64_t x) { return (x + 255) & ~255LL; };
+    const int64_t o_cnt = 0, o_flag = o_cnt + al(4 * K), o_slot = o_flag + al(K), o_list = o_slot + al(4 * K);
+    const int64_t o_small = o_list + al(4 * kMaxHeavy), sel_bytes = o_small + 256;
+    char *sel = nullptr;
+    RMCM_TRY(dev_alloc(h, (void **)&sel, sel_bytes));
+    uint32_t *cnt = (uint32_t *)(sel + o_cnt);
+    uint8_t *flag = (uint8_t *)(sel + o_flag);
+    int32_t *slot = (int32_t *)(sel + o_slot), *list = (int32_t *)(sel + o_list);
+    int32_t *nheavy = (int32_t *)(sel + o_small);
+    unsigned long long *stats = (unsigned long long *)(sel + o_small + 64);
+    auto fail = [&](int32_t rc) {
+        dev_free(h, sel, sel_bytes);
+        dp = DensePart{};
+        return rc;
+    };
+    RMCM_CUDA(h, cudaMemsetAsync(cnt, 0, 4 * K, s));
+    RMCM_CUDA(h, cudaMemsetAsync(sel + o_small, 0, 256, s));
+    k_col_sample<<<h->sm_count * 8, 256, 0, s>>>(A, cnt);
+    k_heavy_select<<<h->sm_count * 8, 256, 0, s>>>(K, cnt, B.rowptr, thr, flag, slot, list, nheavy,
+                                                  (int32_t)kMaxHeavy);
+    k_heavy_stats64<<<h->sm_count * 8, 256, 0, s>>>(A, slot, stats);
+    h->launches += 3;
+    RMCM_CUDA(h, cudaGetLastError());
+    // heavy count; heavy entries per row and largest heavy value of A; B's largest value
+    RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned + 8, sel + o_small, 64 + 40, cudaMemcpyDeviceToHost, s));
+    uint64_t bmax = 1;
+    if (B.rowsum) RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned + 24, B.rowsum + B.rows, 8, cudaMemcpyDeviceToHost, s));
+    RMCM_CUDA(h, cudaStreamSynchronize(s));
+    const int64_t nh = std::min<int64_t>(((int32_t *)(h->h_pinned + 8))[0], kMaxHeavy);
+    const uint64_t hrow = (uint64_t)h->h_pinned[8 + 8 + 3], amax = (uint64_t)h->h_pinned[8 + 8 + 4];
+    if (B.rowsum) bmax = (uint64_t)h->h_pinned[24];
+    if (nh < 64 || amax == 0 || bmax == 0) return fail(RMCM_OK);
+    auto bitlen = [](uint64_t v) {
+        int b = 0;
+        while (b < 64 && (v >> b) != 0) b++;
+        return b;
+    };
+    // limb width: the fewest dense multiply-adds (limb pairs) with at most
+    // 16 chunks of at least 64 indices each
+    int32_t best_bits = 0, best_la = 0, best_lb = 0;
+    int64_t best_kc = 0, best_nq = 0;
+    for (int32_t bits = 11; bits >= 1; bits--) {
+        const int32_t la = (bitlen(amax) + bits - 1) / bits, lb = (bitlen(bmax) + bits - 1) / bits;
+        if (la > 4 || lb > 4 || bits * (la - 1 + lb - 1) >= 64) continue;
+        const uint64_t mask = (1ull << bits) - 1;
+        const double prod = (double)std::min(amax, mask) * (double)std::min(bmax, mask);
+        int64_t kc = (int64_t)(16777216.0 / prod) / 64 * 64;
+        int64_t nq = 1;
+        if ((double)hrow * prod <= 16777216.0) {
+            kc = (nh + 63) / 64 * 64;
+        } else {
+            if (kc < 64) continue;
+            nq = (nh + kc - 1) / kc;
+            if (nq > 16) continue;
+        }
+        if (best_bits == 0 || (int64_t)la * lb < (int64_t)best_la * best_lb ||
+            ((int64_t)la * lb == (int64_t)best_la * best_lb && nq < best_nq)) {
+            best_bits = bits;
+            best_la = la;
+            best_lb = lb;
+            best_kc = kc;
+            best_nq = nq;
+        }
+    }
+    if (best_bits == 0) return fail(RMCM_OK);
+    const int32_t bits = best_bits, la = best_la, lb = best_lb;
+    const int64_t kc = best_kc, nq = best_nq, ldk = kc * nq;
+    const int64_t a_limb = M * ldk, b_limb = ldk * ldn, g_panel = M * ldn, npan = (int64_t)la * lb * nq;
+    const int64_t a_bytes = al(2 * la * a_limb), l_bytes = al(12 * A.nnz) + al(4 * M);
+    const int64_t bd_bytes = al(2 * lb * b_limb), g_bytes = al(4 * npan * g_panel);
+    if (a_bytes + l_bytes + bd_bytes + g_bytes > (h->budget - h->in_use) / 3) return fail(RMCM_OK);
+    if (ldk * 2 > 160 * 1024) return fail(RMCM_OK);
+    __half *Ad = nullptr;
+    char *amem = nullptr, *mem = nullptr;
+    if (dev_alloc(h, (void **)&Ad, a_bytes) != RMCM_OK) {
+        h->last_error.clear();
+        return fail(RMCM_OK);
+    }
+    if (dev_alloc(h, (void **)&amem, l_bytes) != RMCM_OK || dev_alloc(h, (void **)&mem, bd_bytes + g_bytes) != RMCM_OK) {
+        if (amem) dev_free(h, amem, l_bytes);
+        dev_free(h, Ad, a_bytes);
+        h->last_error.clear();
+        return fail(RMCM_OK);
+    }
+    auto fail3 = [&](int32_t rc) {
+        dev_free(h, mem, bd_bytes + g_bytes);
+        dev_free(h, amem, l_bytes);
+        dev_free(h, Ad, a_bytes);
+        return fail(rc);
+    };
+    int32_t *lcol = (int32_t *)amem;
+    uint64_t *lval = (uint64_t *)(amem + al(4 * A.nnz));
+    int32_t *lcnt = (int32_t *)(amem + al(12 * A.nnz));
+    __half *Bd = (__half *)mem;
+    float *G = (float *)(mem + bd_bytes);
+    {
+        const int64_t smem = ldk * 2;
+        if (smem > 48 * 1024 &&
+            cudaFuncSetAttribute(k_gather_a64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+            cudaGetLastError();
+            return fail3(RMCM_OK);
+        }
+        const int grid = (int)std::min<int64_t>(M, (int64_t)h->sm_count * 8);
+        k_gather_a64<<<grid, kGatherThreads, smem, s>>>(A, slot, (int32_t)ldk, la, bits, Ad, a_limb, lcol, lval, lcnt);
+        k_gather_b<uint64_t><<<(int)std::min<int64_t>(nh, (int64_t)h->sm_count * 8), kGatherThreads, 0, s>>>(
+            B, list, (int32_t)nh, (int32_t)ldn, lb, bits, Bd, b_limb, stats);
+        h->launches += 2;
+        if (ldk > nh)
+            for (int l = 0; l < lb; l++)
+                RMCM_CUDA(h, cudaMemsetAsync(Bd + l * b_limb + nh * ldn, 0, 2 * (ldk - nh) * ldn, s));
+        RMCM_CUDA(h, cudaGetLastError());
+    }
+    if (!h->cublas) {
+        cublasHandle_t cb = nullptr;
+        if (cublasCreate(&cb) != CUBLAS_STATUS_SUCCESS) return fail3(RMCM_OK);
+        h->cublas = cb;
+    }
+    cublasHandle_t cb = (cublasHandle_t)h->cublas;
+    if (cublasSetStream(cb, s) != CUBLAS_STATUS_SUCCESS) return fail3(set_error(h, RMCM_ECUDA, "cublasSetStream"));
+    // per limb pair: G_(i,j,q) = Ad_i[:, chunk q] Bd_j[chunk q, :], the chunks as one strided batch
+    const float one = 1.0f, zero = 0.0f;
+    if (ev_begin) cudaEventRecord(ev_begin, s);
+    for (int i = 0; i < la; i++)
+        for (int j = 0; j < lb; j++) {
+            const cublasStatus_t st = cublasGemmStridedBatchedEx(
+                cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)N, (int)M, (int)kc, &one, Bd + j * b_limb, CUDA_R_16F, (int)ldn,
+                (long long)kc * ldn, Ad + i * a_limb, CUDA_R_16F, (int)ldk, (long long)kc, &zero,
+                G + ((int64_t)i * lb + j) * nq * g_panel, CUDA_R_32F, (int)ldn, (long long)g_panel, (int)nq,
+                CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
+            if (st != CUBLAS_STATUS_SUCCESS)
+                return fail3(set_error(h, RMCM_ECUDA, "dense part: cublasGemmStridedBatchedEx failed"));
+        }
+    if (ev_end) cudaEventRecord(ev_end, s);
+    dev_free(h, Ad, a_bytes);
+    dp.amem = amem;
+    dp.abytes = l_bytes;
+    dp.lcol = lcol;
+    dp.lval = (const uint32_t *)lval;
+    dp.lcnt = lcnt;
+    dp.mem = mem;
+    dp.bytes = bd_bytes + g_bytes;
+    dp.G = G;
+    dp.ld = ldn;
+    dp.limb_stride = g_panel;
+    dp.limbs = lb;
+    dp.bits = bits;
+    dp.alimbs = la;
+    dp.abits = bits;
+    dp.chunks = (int32_t)nq;
     dp.heavy = nh;
     dp.sel = sel;
     dp.sel_bytes = sel_bytes;

@@ -219,7 +219,9 @@ int32_t convert_values(rmcm_handle *h, const rmcm_mat *src, int32_t valtype, rmc
 struct DensePart {
     const float *G = nullptr;
     int64_t ld = 0, limb_stride = 0;
-    int32_t limbs = 0, bits = 0;
+    int32_t limbs = 0, bits = 0;      // B's limbs
+    int32_t alimbs = 1, abits = 0;    // A's limbs (uint64 products; 1 and 0 for uint32)
+    int32_t chunks = 1;               // chunks of the heavy indices (uint64 products)
     int64_t heavy = 0;
     const uint8_t *skip = nullptr;
     // A's light entries: row r's are lcol/lval[rowptr[r] .. + lcnt[r])
@@ -232,6 +234,10 @@ struct DensePart {
 // ev_begin / ev_end (may be null) are recorded around the GEMMs.
 int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint64_t bmax, DensePart &dp,
                          cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr);
+// uint64 products: A split into limbs too and the heavy indices into chunks;
+// G panel ((i * limbs + j) * chunks + q) adds G << (bits * (i + j)).
+int32_t dense_part_build64(rmcm_handle *h, const DevCsr &A, const DevCsr &B, DensePart &dp,
+                           cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr);
 void dense_part_release(rmcm_handle *h, DensePart &dp);
 void cublas_destroy(rmcm_handle *h);
 // estimator.cu: c_dev[len*len] on the device

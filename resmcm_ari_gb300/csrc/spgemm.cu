@@ -1416,7 +1416,8 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
 struct DenseExtra {
     const uint32_t *pk = nullptr;
     int32_t cbits = 0;
-    int32_t glimbs = 0, gbits = 0;
+    int32_t glimbs = 0, gbits = 0;     // limbs of B
+    int32_t galimbs = 1, gchunks = 1;  // limbs of A, chunks of the heavy indices (same limb width)
     const float *G = nullptr;
     int64_t gld = 0, gstride = 0;
     const uint8_t *skip = nullptr;
@@ -1483,14 +1484,21 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                 else atomicAdd((AtomV *)(acc + lc), (AtomV)p);
             }
         };
-        if constexpr (NUMERIC && sizeof(V) == 4) {
+        if constexpr (NUMERIC) {
             if (ex.G) {
-                // the row's tensor-core part seeds the counters (one window)
+                // the row's tensor-core part seeds the counters (one window):
+                // panel (i, j, q) adds G << (gbits (i + j)), modulo 2^bits(V)
                 const float *g = ex.G + (int64_t)r * ex.gld;
                 for (int c = tid; c < (int)B.cols; c += NT) {
-                    uint32_t v = 0;
-                    for (int l = 0; l < ex.glimbs; l++)
-                        v += __float2uint_rn(g[l * ex.gstride + c]) << (ex.gbits * l);
+                    V v = 0;
+                    int p = 0;
+                    for (int i = 0; i < ex.galimbs; i++)
+                        for (int j = 0; j < ex.glimbs; j++) {
+                            const int sh = ex.gbits * (i + j);
+                            for (int q = 0; q < ex.gchunks; q++, p++)
+                                if (sh < 8 * (int)sizeof(V))
+                                    v += (V)__float2ull_rn(g[(int64_t)p * ex.gstride + c]) << sh;
+                        }
                     acc[c] = v;
                 }
                 __syncthreads();
@@ -2563,6 +2571,8 @@ DenseExtra dense_extra(const DenseTemp *t, bool single_pass) {
         e.gstride = t->dpart.limb_stride;
         e.glimbs = t->dpart.limbs;
         e.gbits = t->dpart.bits;
+        e.galimbs = t->dpart.alimbs;
+        e.gchunks = t->dpart.chunks;
         e.lcnt = t->dpart.lcnt;
     }
     return e;
@@ -3011,16 +3021,25 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         int64_t mdf = 0;
         if (!replay) memcpy(&mdf, (int32_t *)h->h_pinned + 36, sizeof(int64_t));
         const int64_t fpart0 = std::max<int64_t>(kSplitMinFlops, flops_total / ((int64_t)h->sm_count * 4));
-        bool want = sizeof(V) == 4 && !plan && dtemp.active && positive && dtemp.no_risky &&
+        // (uint64 products, whose dense parts are whole-row GEMMs in the
+        // retail and stress chains, take it even with skewed rows)
+        // (the panel gathers store one value per (row, index): no repeated
+        // column within a row of A or B)
+        bool want = !plan && dtemp.active && positive && dtemp.no_risky && Am->distinct && Bm->distinct &&
                     flops_total >= (int64_t)h->tune.gemm_min_mflops * 1000000 && h->tune.gemm_inv_density > 0 &&
-                    mdf <= fpart0;
+                    (sizeof(V) == 8 || mdf <= fpart0);
         for (int b = 0; b < kNumBins && want; b++)
             if (b != kBinDense && counts[b] > 0) want = false;
         if (want) {
-            uint64_t bmax = 1;
-            if (!Bm->ones) memcpy(&bmax, (int32_t *)h->h_pinned + 58, sizeof(uint64_t));
-            const int32_t drc = dense_part_build(h, A, B, bmax, dtemp.dpart, rec ? h->prof[rec_idx].ev[6] : nullptr,
-                                                 rec ? h->prof[rec_idx].ev[7] : nullptr);
+            cudaEvent_t e0 = rec ? h->prof[rec_idx].ev[6] : nullptr, e1 = rec ? h->prof[rec_idx].ev[7] : nullptr;
+            int32_t drc = RMCM_OK;
+            if (sizeof(V) == 4) {
+                uint64_t bmax = 1;
+                if (!Bm->ones) memcpy(&bmax, (int32_t *)h->h_pinned + 58, sizeof(uint64_t));
+                drc = dense_part_build(h, A, B, bmax, dtemp.dpart, e0, e1);
+            } else {
+                drc = dense_part_build64(h, A, B, dtemp.dpart, e0, e1);
+            }
             if (drc != RMCM_OK) {
                 dense_part_release(h, dtemp.dpart);
                 if (dtemp.pk_mem) dev_free(h, dtemp.pk_mem, dtemp.pk_bytes);
@@ -3286,7 +3305,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     if (rc == RMCM_OK && !adopt)
         rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap, &dtemp,
                                   bin_of, positive, Bm->distinct, &rsplit);
-    const int32_t gemm_limbs = dtemp.dpart.G ? dtemp.dpart.limbs : 0;
+    const int32_t gemm_limbs = dtemp.dpart.G ? dtemp.dpart.limbs * dtemp.dpart.alimbs : 0;
     const int64_t gemm_inner = dtemp.dpart.G ? dtemp.dpart.heavy : 0;
     drop_cursors();
     drop_temp();

@@ -754,3 +754,23 @@ def test_tensor_core_part_in_a_chain_and_batch(native):
     b.free()
     hg.close()
     eng.close()
+
+
+def test_tensor_core_part_uint64(native):
+    """uint64 products: A and B both split into FP16 limbs and the heavy
+    indices into chunks (every partial sum <= 2^24); equal to scipy's int64
+    product and to the same product with the GEMM turned off."""
+    rng = np.random.default_rng(72)
+    A, B = _heavy_inner(rng, 1200, 2500, 1500, 300, bbig=200000)
+    A = A.tocsr()
+    A.data = A.data * 1000
+    eng = native.Engine(device=0)
+    eng.set_tuning(gemm_min_mflops=0)
+    eng.set_profiling(1)
+    _check_product(native, eng, A, B, native.VAL_U64)
+    st = eng.product_stats()[-1]
+    assert st["gemm_inner"] >= 250 and st["gemm_limbs"] >= 4
+    eng.set_tuning(gemm_inv_density=0)
+    _check_product(native, eng, A, B, native.VAL_U64)
+    assert eng.product_stats()[-1]["gemm_inner"] == 0
+    eng.close()
