@@ -102,7 +102,9 @@ typedef struct rmcm_product_stats {
     int64_t touched_rows;               /* distinct columns of A (B rows read); level 2 only */
     int64_t touched_nnz;                /* entries of those B rows; level 2 only */
     int64_t bytes_a, bytes_b_touched, bytes_c;   /* level 2 only */
-    double analyze_ms, symbolic_ms, numeric_ms;  /* CUDA-event times on the handle's stream */
+    double analyze_ms, symbolic_ms, numeric_ms;  /* CUDA-event times on the handle's stream; symbolic_ms
+                                                    includes the setup after the analysis (temporaries,
+                                                    packing, the tensor-core part, split preparation) */
     int32_t valtype;
     int32_t bin_rows[8];                /* rows per bin: tiny, hash512, hash2k, hash8k, dense, rank, micro, warp */
     int32_t gemm_limbs;                 /* limb pairs (A x B) of the tensor-core GEMM (0: no GEMM part) */

@@ -2920,7 +2920,12 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         }
         RMCM_CUDA(h, cudaGetLastError());
     }
-    if (rec) RMCM_CUDA(h, cudaEventRecord(h->prof[rec_idx].ev[1], s));
+    if (rec) {
+        // the symbolic time starts here: it includes the product's setup
+        // (temporaries, packing, the tensor-core part, split preparation)
+        RMCM_CUDA(h, cudaEventRecord(h->prof[rec_idx].ev[1], s));
+        RMCM_CUDA(h, cudaEventRecord(h->prof[rec_idx].ev[2], s));
+    }
     // bin counts, the longest dense A row and the flops to the host (a replay
     // takes them from the recorded plan)
     int32_t counts[kNumBins];
@@ -3242,7 +3247,6 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         drop_rank();
         return rc;
     }
-    if (rec) cudaEventRecord(h->prof[rec_idx].ev[2], s);
     // every row single-pass dense (no split): slot i of the temporary is row i,
     // so a product whose rows all come out full can keep it as C
     const bool all_dense = dtemp.active && !dtemp.split && counts[kBinDense] == m;
