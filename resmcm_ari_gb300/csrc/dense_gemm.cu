@@ -254,6 +254,57 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather_a64(DevCsr A, const i
 
 }  // namespace
 
+// Heavy inner indices of C = A B: sampled column counts of A and the density
+// rule give each heavy index a slot (k_heavy_select).  With stats64 also the
+// largest number of heavy entries in a row of A and the largest heavy value
+// (k_heavy_stats64).  On success hs.sel holds the buffers (the caller frees
+// it); nh < 64 means the caller gives up.
+struct HeavySet {
+    char *sel = nullptr;
+    int64_t sel_bytes = 0;
+    uint8_t *flag = nullptr;
+    int32_t *slot = nullptr, *list = nullptr;
+    unsigned long long *stats = nullptr;   // device: [2] largest B value seen, [3..4] as above
+    int64_t nh = 0;
+    uint64_t hrow = 0, amax = 0;
+};
+
+int32_t select_heavy(rmcm_handle *h, const DevCsr &A, const DevCsr &B, bool stats64, HeavySet &hs) {
+    hs = HeavySet{};
+    cudaStream_t s = h->stream;
+    const int64_t M = A.rows, N = B.cols, K = A.cols;
+    const double thr = (double)M * (double)N / (double)h->tune.gemm_inv_density;
+    auto al = [](int64_t x) { return (x + 255) & ~255LL; };
+    const int64_t o_cnt = 0, o_flag = o_cnt + al(4 * K), o_slot = o_flag + al(K), o_list = o_slot + al(4 * K);
+    const int64_t o_small = o_list + al(4 * kMaxHeavy);
+    hs.sel_bytes = o_small + 256;
+    RMCM_TRY(dev_alloc(h, (void **)&hs.sel, hs.sel_bytes));
+    uint32_t *cnt = (uint32_t *)(hs.sel + o_cnt);
+    hs.flag = (uint8_t *)(hs.sel + o_flag);
+    hs.slot = (int32_t *)(hs.sel + o_slot);
+    hs.list = (int32_t *)(hs.sel + o_list);
+    int32_t *nheavy = (int32_t *)(hs.sel + o_small);
+    hs.stats = (unsigned long long *)(hs.sel + o_small + 64);
+    RMCM_CUDA(h, cudaMemsetAsync(cnt, 0, 4 * K, s));
+    RMCM_CUDA(h, cudaMemsetAsync(hs.sel + o_small, 0, 256, s));
+    k_col_sample<<<h->sm_count * 8, 256, 0, s>>>(A, cnt);
+    k_heavy_select<<<h->sm_count * 8, 256, 0, s>>>(K, cnt, B.rowptr, thr, hs.flag, hs.slot, hs.list, nheavy,
+                                                  (int32_t)kMaxHeavy);
+    h->launches += 2;
+    if (stats64) {
+        k_heavy_stats64<<<h->sm_count * 8, 256, 0, s>>>(A, hs.slot, hs.stats);
+        h->launches++;
+    }
+    RMCM_CUDA(h, cudaGetLastError());
+    // the count (and the stats) in one read-back: h_pinned[8..] = small area
+    RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned + 8, hs.sel + o_small, 64 + 40, cudaMemcpyDeviceToHost, s));
+    RMCM_CUDA(h, cudaStreamSynchronize(s));
+    hs.nh = std::min<int64_t>(((int32_t *)(h->h_pinned + 8))[0], kMaxHeavy);
+    hs.hrow = (uint64_t)h->h_pinned[8 + 8 + 3];
+    hs.amax = (uint64_t)h->h_pinned[8 + 8 + 4];
+    return RMCM_OK;
+}
+
 // Builds the tensor-core part of C = A B (uint32, single-window dense rows):
 // on success dp.G holds L limb panels (rows x ld floats each) and dp.skip
 // flags the heavy inner indices; otherwise dp stays empty (and the product
@@ -264,35 +315,22 @@ int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint6
     const int32_t inv_density = h->tune.gemm_inv_density;
     if (inv_density <= 0 || A.rows == 0 || B.cols == 0 || A.cols == 0) return RMCM_OK;
     cudaStream_t s = h->stream;
-    const int64_t M = A.rows, N = B.cols, K = A.cols;
+    const int64_t M = A.rows, N = B.cols;
     const int64_t ldn = (N + 7) / 8 * 8;
-    const double thr = (double)M * (double)N / (double)inv_density;
-    // heavy-set scratch: counts, flags, slots, list, counters/stats
     auto al = [](int64_t x) { return (x + 255) & ~255LL; };
-    const int64_t o_cnt = 0, o_flag = o_cnt + al(4 * K), o_slot = o_flag + al(K), o_list = o_slot + al(4 * K);
-    const int64_t o_small = o_list + al(4 * kMaxHeavy), sel_bytes = o_small + 256;
-    char *sel = nullptr;
-    RMCM_TRY(dev_alloc(h, (void **)&sel, sel_bytes));
-    uint32_t *cnt = (uint32_t *)(sel + o_cnt);
-    uint8_t *flag = (uint8_t *)(sel + o_flag);
-    int32_t *slot = (int32_t *)(sel + o_slot), *list = (int32_t *)(sel + o_list);
-    int32_t *nheavy = (int32_t *)(sel + o_small);
-    unsigned long long *stats = (unsigned long long *)(sel + o_small + 64);
+    HeavySet hs;
+    RMCM_TRY(select_heavy(h, A, B, false, hs));
+    char *sel = hs.sel;
+    const int64_t sel_bytes = hs.sel_bytes;
+    uint8_t *flag = hs.flag;
+    int32_t *slot = hs.slot, *list = hs.list;
+    unsigned long long *stats = hs.stats;
     auto fail = [&](int32_t rc) {
         dev_free(h, sel, sel_bytes);
         dp = DensePart{};
         return rc;
     };
-    RMCM_CUDA(h, cudaMemsetAsync(cnt, 0, 4 * K, s));
-    RMCM_CUDA(h, cudaMemsetAsync(sel + o_small, 0, 256, s));
-    k_col_sample<<<h->sm_count * 8, 256, 0, s>>>(A, cnt);
-    k_heavy_select<<<h->sm_count * 8, 256, 0, s>>>(K, cnt, B.rowptr, thr, flag, slot, list, nheavy,
-                                                  (int32_t)kMaxHeavy);
-    h->launches += 2;
-    RMCM_CUDA(h, cudaGetLastError());
-    RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned + 8, nheavy, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-    RMCM_CUDA(h, cudaStreamSynchronize(s));
-    const int64_t nh = std::min<int64_t>(((int32_t *)(h->h_pinned + 8))[0], kMaxHeavy);
+    const int64_t nh = hs.nh;
     // worth a GEMM only when the heavy part is a real share of the work
     if (nh < 64) return fail(RMCM_OK);
     const int64_t ldk = (nh + 63) / 64 * 64;
@@ -419,40 +457,30 @@ int32_t dense_part_build64(rmcm_handle *h, const DevCsr &A, const DevCsr &B, Den
     const int32_t inv_density = h->tune.gemm_inv_density;
     if (inv_density <= 0 || A.rows == 0 || B.cols == 0 || A.cols == 0) return RMCM_OK;
     cudaStream_t s = h->stream;
-    const int64_t M = A.rows, N = B.cols, K = A.cols;
+    const int64_t M = A.rows, N = B.cols;
     const int64_t ldn = (N + 7) / 8 * 8;
-    const double thr = (double)M * (double)N / (double)inv_density;
     auto al = [](int64_t x) { return (x + 255) & ~255LL; };
-    const int64_t o_cnt = 0, o_flag = o_cnt + al(4 * K), o_slot = o_flag + al(K), o_list = o_slot + al(4 * K);
-    const int64_t o_small = o_list + al(4 * kMaxHeavy), sel_bytes = o_small + 256;
-    char *sel = nullptr;
-    RMCM_TRY(dev_alloc(h, (void **)&sel, sel_bytes));
-    uint32_t *cnt = (uint32_t *)(sel + o_cnt);
-    uint8_t *flag = (uint8_t *)(sel + o_flag);
-    int32_t *slot = (int32_t *)(sel + o_slot), *list = (int32_t *)(sel + o_list);
-    int32_t *nheavy = (int32_t *)(sel + o_small);
-    unsigned long long *stats = (unsigned long long *)(sel + o_small + 64);
+    HeavySet hs;
+    RMCM_TRY(select_heavy(h, A, B, true, hs));
+    char *sel = hs.sel;
+    const int64_t sel_bytes = hs.sel_bytes;
+    uint8_t *flag = hs.flag;
+    int32_t *slot = hs.slot, *list = hs.list;
+    unsigned long long *stats = hs.stats;
     auto fail = [&](int32_t rc) {
         dev_free(h, sel, sel_bytes);
         dp = DensePart{};
         return rc;
     };
-    RMCM_CUDA(h, cudaMemsetAsync(cnt, 0, 4 * K, s));
-    RMCM_CUDA(h, cudaMemsetAsync(sel + o_small, 0, 256, s));
-    k_col_sample<<<h->sm_count * 8, 256, 0, s>>>(A, cnt);
-    k_heavy_select<<<h->sm_count * 8, 256, 0, s>>>(K, cnt, B.rowptr, thr, flag, slot, list, nheavy,
-                                                  (int32_t)kMaxHeavy);
-    k_heavy_stats64<<<h->sm_count * 8, 256, 0, s>>>(A, slot, stats);
-    h->launches += 3;
-    RMCM_CUDA(h, cudaGetLastError());
-    // heavy count; heavy entries per row and largest heavy value of A; B's largest value
-    RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned + 8, sel + o_small, 64 + 40, cudaMemcpyDeviceToHost, s));
+    // B's largest value (row sums' last slot; 1 for a matrix of ones)
     uint64_t bmax = 1;
-    if (B.rowsum) RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned + 24, B.rowsum + B.rows, 8, cudaMemcpyDeviceToHost, s));
-    RMCM_CUDA(h, cudaStreamSynchronize(s));
-    const int64_t nh = std::min<int64_t>(((int32_t *)(h->h_pinned + 8))[0], kMaxHeavy);
-    const uint64_t hrow = (uint64_t)h->h_pinned[8 + 8 + 3], amax = (uint64_t)h->h_pinned[8 + 8 + 4];
-    if (B.rowsum) bmax = (uint64_t)h->h_pinned[24];
+    if (B.rowsum) {
+        RMCM_CUDA(h, cudaMemcpyAsync(h->h_pinned + 24, B.rowsum + B.rows, 8, cudaMemcpyDeviceToHost, s));
+        RMCM_CUDA(h, cudaStreamSynchronize(s));
+        bmax = (uint64_t)h->h_pinned[24];
+    }
+    const int64_t nh = hs.nh;
+    const uint64_t hrow = hs.hrow, amax = hs.amax;
     if (nh < 64 || amax == 0 || bmax == 0) return fail(RMCM_OK);
     auto bitlen = [](uint64_t v) {
         int b = 0;
