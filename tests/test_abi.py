@@ -58,3 +58,39 @@ def test_create_without_gpu_reports_cuda_error(native):
     rc = native.lib().rmcm_create(C.byref(h), None)
     assert rc == native.ECUDA
     assert native.lib().rmcm_status_string(rc) == b"CUDA error"
+
+
+STRUCTS = [("Opts", "rmcm_opts"), ("Timings", "rmcm_timings"), ("ProductStats", "rmcm_product_stats"),
+           ("Tuning", "rmcm_tuning"), ("ServerOpts", "rmcm_server_opts"), ("QueryResult", "rmcm_query_result"),
+           ("ServerCounters", "rmcm_server_counters")]
+
+
+def test_ctypes_mirrors_match_the_header(native, tmp_path):
+    """Every ctypes structure of the binding has the size and field offsets
+    the C compiler gives the header's struct (compiled here with gcc)."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "resmcm_gpu.h"', "int main(void) {"]
+    for py, c in STRUCTS:
+        lines.append(f'  printf("{py} sizeof %zu\\n", sizeof({c}));')
+        for f, _ in getattr(native, py)._fields_:
+            lines.append(f'  printf("{py} {f} %zu\\n", offsetof({c}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "abi.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "abi"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run(["gcc", "-std=c11", "-I" + inc, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    want = {}
+    for ln in out:
+        if ln:
+            py, f, v = ln.split()
+            want[(py, f)] = int(v)
+    for py, _ in STRUCTS:
+        cls = getattr(native, py)
+        assert C.sizeof(cls) == want[(py, "sizeof")], py
+        for f, _ in cls._fields_:
+            assert getattr(cls, f).offset == want[(py, f)], (py, f)
