@@ -277,11 +277,13 @@ RMCM_API int32_t rmcm_estimate_metapath(rmcm_handle *h, rmcm_graph *g, const cha
  *                    (0 .. 65536; 0 = none)
  *   hash_load        hash tables get at least min(products, width) / load
  *                    slots (0.1 .. 0.75)
- *   gemm_inv_density uint32 products whose rows all take the single-pass dense
- *                    path: inner indices with (A column count / rows) x
+ *   gemm_inv_density products whose rows all take the single-pass dense path
+ *                    (uint32 or uint64, positive, no row able to overflow):
+ *                    inner indices with (A column count / rows) x
  *                    (B row length / cols) >= 1 / gemm_inv_density are
- *                    multiplied as a dense FP16 GEMM on the tensor cores
- *                    (exact: see dense_gemm.cu); 0 = never (0 .. 65536)
+ *                    multiplied as dense FP16 GEMMs on the tensor cores
+ *                    (exact: values in limbs, partial sums below 2^24, see
+ *                    dense_gemm.cu); 0 = never (0 .. 65536)
  *   gemm_min_mflops  products with fewer multiply-adds (millions) never try
  *                    it (>= 0)
  * Defaults: 4, 4096, 16, 2048, 0.5, 512, 512.  A batch keeps the values it
