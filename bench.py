@@ -45,7 +45,6 @@ import os
 import statistics
 import subprocess
 import sys
-import tempfile
 import threading
 import time
 
@@ -76,27 +75,15 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched (CUDA graph) section")
     ap.add_argument("--no-served", action="store_true", help="skip the served (query server) section")
     ap.add_argument("--no-stress", action="store_true", help="skip the stress (12-matrix uint64 chain) section")
+    ap.add_argument("--no-parity", action="store_true", help="skip the parity check against the oracle")
     return ap.parse_args()
 
 
 def make_graph(scale: float, seed: int):
-    """Seeded graph, cached on local disk per (scale, seed)."""
-    key = f"retail_s{seed}_x{scale:g}"
-    path = os.path.join(tempfile.gettempdir(), f"resmcm_bench_{key}.npz")
-    if os.path.exists(path):
-        z = np.load(path)
-        g = synth.SyntheticHIN(key, z["type_sizes"].tolist())
-        g._adj = (z["ptr"], z["nbr"], z["et"])
-        g.metapaths = synth.retail_like(n_u=10, n_i=10, n_c=2, n_t=2, ui_edges=10).metapaths
-        return g
-    sc = lambda x: max(2, int(round(x * scale)))  # noqa: E731
-    g = synth.retail_like(n_u=sc(1_000_000), n_i=sc(300_000), n_c=sc(2_000), n_t=sc(20_000),
-                          ui_edges=sc(20_000_000), seed=seed)
-    ptr, nbr, et = g.adjacency()
-    tmp = path + f".{os.getpid()}.tmp.npz"
-    np.savez(tmp, type_sizes=np.array(g.type_sizes), ptr=ptr, nbr=nbr, et=et)
-    os.replace(tmp, path)
-    return g
+    """The seeded retail graph (regenerated on every run: about 20 s, and
+    nothing stale can be measured)."""
+    from resmcm_ari_gb300 import workloads
+    return workloads.retail_four_chains(scale=scale, seed=seed)
 
 
 class ClockSampler:
@@ -238,7 +225,7 @@ def run_reference(args):
         return
     g = make_graph(args.scale, args.seed)
     mps = select(g.metapaths, args.chains)
-    steps, warmup = max(1, args.steps), max(0, min(args.warmup, 1))
+    steps, warmup = max(1, args.steps), max(0, args.warmup)
     cb = cpu_reference(g, mps, steps, warmup, f"{len(mps)} full chains per step ({WORKLOAD})")
     line = {"impl": "reference", "metric": "chains/s", "value": cb["value"], "unit": "chains/s", "n_gpus": 0,
             "steps": steps, "warmup": warmup, "ms_per_step": cb["s_per_pass"] * 1e3, "higher_is_better": True,
@@ -247,7 +234,8 @@ def run_reference(args):
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": cb["value"], "unit": "chains/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "oracle port of efficient/resmcm.cpp (Boolean bitmap Gustavson, OpenMP dynamic schedule); "
-                    "the reference source itself is not present on this host"}
+                    "the reference's own binary cannot run here (its source is not on this host and compiled "
+                    "x86 objects do not travel to it)"}
     print(json.dumps(line), flush=True)
 
 
@@ -365,6 +353,66 @@ def stress_section(rg, device, scale=0.1):
     hg.close()
     eng.close()
     return out
+
+
+def parity_section(eng, hg, g, mps, rg, threads=None):
+    """Results of the timed workload against the CPU oracle, after the timed
+    region: per chain the GPU result's nnz and order-free digest (structure
+    and exact path counts, rmcm_mat_digest) against the counting oracle's,
+    the estimates within 1e-9 relative of the oracle's one-thread sums, and
+    the multiplication order against the oracle's.  Where the reference's own
+    result sizes for this graph are on disk (the fixture made by the
+    reference), the nnz is checked against them too."""
+    import oracle
+    oracle.build()
+    t0 = time.perf_counter()
+    og = oracle.OracleGraph.from_synthetic(g)
+    threads = threads or os.cpu_count() or 1
+    ref_nnz = {}
+    fx = os.path.join(ROOT, "tests", "golden", "retail_full.json")
+    if os.path.exists(fx) and g.name == "retail_like_u1000000_i300000_c2000_t20000_s1":
+        with open(fx) as f:
+            ref_nnz = {r["metapath"]: int(r["nnz"]) for r in json.load(f)["paths"]}
+    chains, ok = [], True
+    for mp in mps:
+        C, _, rc = eng.run_metapath(hg, mp, keep=True)
+        n_gpu, d_gpu = eng.digest(C)
+        C.free()
+        r = og.chain(mp, oracle.MODE_COUNT, threads=threads, export=False, digest=True)
+        leaves = hg.leaves(mp, rg.VAL_U32)
+        c_gpu = eng.estimate(leaves)
+        c_orc = og.estimate(mp, threads=1)
+        nz = c_orc != 0
+        rel = float((np.abs(c_gpu[nz] - c_orc[nz]) / np.abs(c_orc[nz])).max(initial=0.0))
+        est_ok = bool(np.array_equal(c_gpu[~nz], c_orc[~nz]) and rel <= 1e-9)
+        _, _, pairs_gpu = eng.order(c_gpu)
+        _, _, pairs_orc = oracle.dp(c_orc)
+        rec = {"metapath": mp, "nnz": int(n_gpu), "nnz_equal": int(n_gpu) == int(r.nnz),
+               "digest_equal": int(d_gpu) == int(r.digest) and r.status == oracle.ORC_OK,
+               "estimates_max_rel_err": rel, "estimates_ok": est_ok,
+               "order_equal": bool(np.array_equal(np.asarray(pairs_gpu).reshape(-1),
+                                                  np.asarray(pairs_orc).reshape(-1)))}
+        if mp in ref_nnz:
+            rec["reference_nnz_equal"] = int(n_gpu) == ref_nnz[mp]
+        ok = ok and rec["nnz_equal"] and rec["digest_equal"] and est_ok and rec["order_equal"] and \
+            rec.get("reference_nnz_equal", True)
+        chains.append(rec)
+    og.close()
+    return {"ok": bool(ok), "against": "counting oracle (exact uint64 path counts, oracle/oracle.c) on the "
+                                      "same graph; nnz also against the reference's own results where its "
+                                      "fixture covers the graph",
+            "oracle_threads": threads, "seconds": time.perf_counter() - t0, "chains": chains}
+
+
+def guarded(name, fn, *a, **kw):
+    """Run an optional section; a failure becomes an error field in the line
+    instead of ending the benchmark."""
+    try:
+        return fn(*a, **kw)
+    except Exception as e:  # noqa: BLE001 -- reported, not swallowed
+        import traceback
+        traceback.print_exc(file=sys.stderr)
+        return {"error": f"{name}: {type(e).__name__}: {e}"}
 
 
 def select(mps, spec):
@@ -578,18 +626,20 @@ def main():
         e2e = {"value": replica_value(len(mps), ws, e2e_s), "unit": "chains/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3}
 
-    batched = served = None
+    parity = batched = served = stress = None
+    if rank == 0 and not args.no_parity:
+        parity = guarded("parity", parity_section, eng, hg, g, mps, rg)
     if rank == 0 and not args.no_batched:
-        batched = batched_section(rg, local)
+        batched = guarded("batched", batched_section, rg, local)
     if rank == 0 and not args.no_served:
-        served = served_section(rg, eng, hg, g)
-    stress = None
+        served = guarded("served", served_section, rg, eng, hg, g)
     if rank == 0 and not args.no_stress:
-        stress = stress_section(rg, local)
+        stress = guarded("stress", stress_section, rg, local)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        cpu = cpu_reference(g, mps, 1, 0, f"one full pass over the {len(mps)} chains ({WORKLOAD})")
+        cpu = guarded("cpu_baseline", cpu_reference, g, mps, 2, 1,
+                      f"two full passes over the {len(mps)} chains after one warm-up pass ({WORKLOAD})")
         cpu.pop("s_per_pass", None)
 
     if rank == 0:
@@ -607,7 +657,7 @@ def main():
             "nnz_per_s": step_nnz * ws / (ms_per_step / 1e3),
             "result_nnz_per_step": step_nnz,
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
-            "batched": batched, "served": served, "stress": stress,
+            "parity": parity, "batched": batched, "served": served, "stress": stress,
         }
         print(json.dumps(line), flush=True)
     hg.close()

@@ -389,17 +389,19 @@ RMCM_API int32_t rmcm_server_destroy(rmcm_server *s);
  * No counterpart in the reference.  For callers that may not allocate device
  * memory when they need an estimate (a host framework that owns all device
  * memory through its own pool, a serving loop that forbids allocation after
- * start-up, code recording a stream into a graph): same estimates as
+ * start-up): same estimates as
  * rmcm_estimate, computed from caller-owned device CSR arrays of the chain
  * (rows[i] x cols[i], rowptr[i] with rows[i]+1 int64 entries, col[i] int32
  * column indices; cols[i] == rows[i+1]) into the host array c_out[len*len].
  * It calls no allocating routine: its temporaries live in a fixed 32 MiB
  * device array that every GPU which loads this library holds until the
  * process exits, so a chain fits when 2*8*len*max(rows) bytes plus about
- * 0.2 MiB stay within 32 MiB (len <= 16); larger chains return RMCM_EINVAL.
- * The first call on a device looks the array up (make it before any stream
- * capture).  All calls share the array: calls that overlap on the GPU race,
- * so issue them one after another.  Synchronises `stream` (NULL = default). */
+ * 0.2 MiB stay within 32 MiB (len <= 16); larger chains return RMCM_EINVAL
+ * before anything is launched.  The first call on a device looks the array
+ * up (make that first call before any stream capture).  All calls share the
+ * array: calls that overlap on the GPU race, so issue them one after
+ * another.  Copies the estimates to c_out and synchronises `stream` (NULL =
+ * the default stream) before it returns. */
 RMCM_API int32_t rmcm_estimate_noalloc(int32_t len, const int64_t *rows, const int64_t *cols,
                                        const int64_t *const *rowptr, const int32_t *const *col, double *c_out,
                                        void *stream);

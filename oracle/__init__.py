@@ -24,7 +24,9 @@ LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libref_resmcm.so")
 REF_CLI_PATH = os.path.join(HERE, "_ref", "resmcm")
 REF_NAIVE_LIB_PATH = os.path.join(HERE, "_ref", "libref_naive.so")
-DEFAULT_REF = "/root/reference"
+# checkout of swordzlim/RESMCM_ARI used to build the reference harness; unset
+# means the location oracle/Makefile names
+DEFAULT_REF = os.environ.get("RESMCM_REF_DIR") or None
 
 MODE_BOOL, MODE_COUNT = 0, 1
 ORC_OK, ORC_EOVERFLOW = 0, 3
@@ -44,8 +46,8 @@ def build(ref_dir: str | None = None, quiet: bool = True) -> None:
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True, stdout=out)
     ref = ref_dir or DEFAULT_REF
-    if os.path.isfile(os.path.join(ref, "efficient", "resmcm.cpp")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref}"], check=True, stdout=out)
+    cmd = ["make", "-s", "-C", HERE, "ref-if-present"] + ([f"REF={ref}"] if ref else [])
+    subprocess.run(cmd, check=True, stdout=out)
 
 
 _lib = None
@@ -82,6 +84,7 @@ def lib():
         L.orc_result_nnz.argtypes = [C.c_void_p]
         L.orc_result_nnz.restype = C.c_int64
         L.orc_result_export.argtypes = [C.c_void_p, _i64p, C.c_void_p, C.c_void_p]
+        L.orc_result_digest.argtypes = [C.c_void_p, C.POINTER(C.c_uint64)]
         L.orc_result_free.argtypes = [C.c_void_p]
         _lib = L
     return _lib
@@ -112,9 +115,10 @@ def dp(c: np.ndarray):
 
 
 class OracleResult:
-    def __init__(self, rowptr, col, val, nnz, times, status):
+    def __init__(self, rowptr, col, val, nnz, times, status, digest=None):
         self.rowptr, self.col, self.val = rowptr, col, val
         self.nnz, self.times, self.status = nnz, times, status
+        self.digest = digest
 
 
 class OracleGraph:
@@ -198,7 +202,10 @@ class OracleGraph:
         return c.reshape(L, L)
 
     def chain(self, metapath: str, mode: int = MODE_COUNT, threads: int = 1, pairs=None,
-              export: bool = True) -> OracleResult:
+              export: bool = True, digest: bool = False) -> OracleResult:
+        """One chain through the oracle's executor.  ``export`` copies the
+        result out (local ids, rows sorted); ``digest`` computes its
+        order-free digest instead (the library's rmcm_mat_digest function)."""
         h = C.c_void_p()
         t = OrcTimes()
         if pairs is None:
@@ -209,9 +216,14 @@ class OracleGraph:
                                             C.byref(t))
         if rc not in (ORC_OK, ORC_EOVERFLOW):
             raise ValueError(f"oracle chain failed with status {rc}")
+        dg = None
         try:
             nnz = lib().orc_result_nnz(h)
             rowptr = col = val = None
+            if digest:
+                d = C.c_uint64(0)
+                lib().orc_result_digest(h, C.byref(d))
+                dg = int(d.value)
             if export:
                 rows = lib().orc_result_rows(h)
                 rowptr = np.zeros(rows + 1, np.int64)
@@ -223,7 +235,7 @@ class OracleGraph:
         finally:
             lib().orc_result_free(h)
         times = {"es": t.es, "dp": t.dp, "spgemm": t.spgemm, "total": t.total}
-        return OracleResult(rowptr, col, val, nnz, times, rc)
+        return OracleResult(rowptr, col, val, nnz, times, rc, dg)
 
 
 # --------------------------------------------------------------------------

@@ -876,6 +876,39 @@ int orc_result_export(const orc_result *r, int64_t *rowptr, int32_t *col, uint64
     return fail ? ORC_ENOMEM : ORC_OK;
 }
 
+/* splitmix64 output function (Steele, Lea and Flood, OOPSLA 2014). */
+static uint64_t mix64(uint64_t x) {
+    x ^= x >> 30;
+    x *= 0xBF58476D1CE4E5B9ULL;
+    x ^= x >> 27;
+    x *= 0x94D049BB133111EBULL;
+    return x ^ (x >> 31);
+}
+
+/* Order-free digest of the result in local ids: the sum mod 2^64 over its
+ * entries (r, c, v) of mix64(mix64(r * 2^32 + c) + v), v = 1 in Boolean
+ * mode.  Not in the reference; it lets a test compare a result of billions
+ * of entries with another implementation's without exporting it. */
+int orc_result_digest(const orc_result *r, uint64_t *digest) {
+    const orc_graph *g = r->g;
+    int32_t rt = r->mat->row_vt;
+    int64_t b0 = g->bin_ptr[rt], b1 = g->bin_ptr[rt + 1];
+    uint64_t acc = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : acc)
+    for (int64_t k = b0; k < b1; k++) {
+        int32_t u = g->bin_ids[k];
+        uint64_t row = (uint64_t)(k - b0) << 32;
+        int64_t L = r->mat->len[u];
+        for (int64_t q = 0; q < L; q++) {
+            uint64_t key = row | (uint64_t)(uint32_t)g->local[r->mat->cols[u][q]];
+            uint64_t v = r->mode == ORC_MODE_COUNT ? r->mat->vals[u][q] : 1;
+            acc += mix64(mix64(key) + v);
+        }
+    }
+    *digest = acc;
+    return ORC_OK;
+}
+
 void orc_result_free(orc_result *r) {
     if (!r) return;
     rowmat_free(r->mat);

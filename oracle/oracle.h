@@ -89,6 +89,9 @@ int64_t orc_result_rows(const orc_result *r);
 int64_t orc_result_nnz(const orc_result *r);
 /* Export in local ids with each row sorted ascending; val may be NULL. */
 int orc_result_export(const orc_result *r, int64_t *rowptr, int32_t *col, uint64_t *val);
+/* Order-free digest of the result (local ids): sum mod 2^64 of
+ * mix64(mix64(row * 2^32 + col) + value), value 1 in Boolean mode. */
+int orc_result_digest(const orc_result *r, uint64_t *digest);
 void orc_result_free(orc_result *r);
 
 #ifdef __cplusplus

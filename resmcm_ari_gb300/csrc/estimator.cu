@@ -288,9 +288,10 @@ int32_t estimate(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, double *c_
 // Some callers of this library may not call cudaMalloc (or any allocating
 // routine) at the point where they need an estimate: a host framework that
 // owns every byte of device memory through its own pool and forbids plugins
-// from allocating behind its back, a latency-critical serving loop that
-// allows no allocation after start-up, or code that is recording a CUDA
-// stream into a graph.  rmcm_estimate_noalloc serves them.  The caller passes
+// from allocating behind its back, or a latency-critical serving loop that
+// allows no allocation after start-up (an allocation can synchronise the
+// device or fail under memory pressure at the worst moment).
+// rmcm_estimate_noalloc serves them.  The caller passes
 // its chain as plain device CSR arrays it already owns and a host array for
 // the estimates; every temporary the estimator needs (two levels of row
 // sparsities, per-block partial sums and the estimate matrix) lives in the
@@ -322,6 +323,9 @@ extern "C" RMCM_API int32_t rmcm_estimate_noalloc(int32_t len, const int64_t *ro
     int64_t max_rows = 1;
     for (int i = 0; i < len; i++) {
         if (rows[i] < 0 || cols[i] < 0 || cols[i] > INT32_MAX || (rows[i] > 0 && !rowptr[i])) return RMCM_EINVAL;
+        // two FP64 levels of len values per row must fit the array: refuse
+        // before any size product can wrap around
+        if (rows[i] > kNoAllocScratchBytes / (16 * (int64_t)len)) return RMCM_EINVAL;
         if (i + 1 < len && cols[i] != rows[i + 1]) return RMCM_EINVAL;
         max_rows = std::max(max_rows, rows[i]);
     }

@@ -48,6 +48,9 @@ CASES = [
       "relations": [[0, 1], [1, 2], [2, 3], [0, 2], [1, 3]], "mean_deg": [2, 5]},
      ("random", 17, 14, (2, 9)), False),
     ("config0_full", "dblp_like", {}, ["1-3-0-1-2-4-0-0-1"], False),
+    # the plain-at-scale workload the benchmark times: U=1M, I=300k, C=2k,
+    # T=20k, its four chains
+    ("retail_full", "retail_like", {"seed": 1}, None, False),
 ]
 
 

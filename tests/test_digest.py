@@ -47,3 +47,15 @@ def test_digest_ignores_entry_order_but_not_values():
     val2[0] += 1
     assert csr_digest(rowptr, col, val) != csr_digest(rowptr, col, val2)
     assert csr_digest(np.array([0], np.int64), np.zeros(0, np.int32)) == (0, 0)
+
+
+def test_oracle_digest_equals_the_host_digest_of_its_export(oracle_mod):
+    """The oracle's C digest (used at full workload sizes, where exporting
+    the result is too large) is the same function as csr_digest."""
+    from resmcm_ari_gb300 import synth
+    g = synth.dblp_like(n_a=800, n_p=1600, n_v=10, seed=3)
+    og = oracle_mod.OracleGraph.from_synthetic(g)
+    for mp, mode in (("1-3-0-1-2-4-0-0-1", oracle_mod.MODE_COUNT), ("0-0-1-3-0", oracle_mod.MODE_BOOL)):
+        r = og.chain(mp, mode, threads=2, digest=True)
+        assert r.digest == csr_digest(r.rowptr, r.col, r.val)[1]
+        assert r.nnz == int(r.rowptr[-1])
