@@ -512,20 +512,27 @@ def main():
                                               "gemm_inner", "gemm_limbs")},
                 "algorithmic_bytes": alg, "launch_ms": avg_ms[dom],
                 "multiply_adds_per_s": b["flops"] / (avg_ms[dom] / 1e3)}
-        # the tensor-core part (exact FP16 GEMM of the heavy inner indices) of
-        # the product that spends the most time in it
+        # the tensor-core part (exact FP16 GEMM of the heavy inner indices):
+        # the product with the most dense multiply-adds, and every GEMM
         gemm_ms = [0.0] * nprod
         for i, st in enumerate(timed_stats):
             gemm_ms[i % nprod] += st["gemm_ms"] / max(1, len(per_prod_ms[i % nprod]))
-        gi = int(np.argmax(gemm_ms))
-        if gemm_ms[gi] > 0:
+        macs_of = [b_["rows"] * b_["gemm_inner"] * b_["cols"] * b_["gemm_limbs"] for b_ in timed_stats[:nprod]]
+        gi = int(np.argmax(macs_of)) if nprod else 0
+        if nprod and gemm_ms[gi] > 0:
             gb = timed_stats[gi]
-            macs = gb["rows"] * gb["gemm_inner"] * gb["cols"] * gb["gemm_limbs"]
+            macs = macs_of[gi]
             tf = 2.0 * macs / (gemm_ms[gi] / 1e3) / 1e12
             tpeak, tkind = peak_tensor()
             roof["tensor_part"] = {"bound": "tensor", "achieved": tf, "peak": tpeak, "unit": "TFLOP/s",
                                    "frac": tf / tpeak, "peak_kind": f"of {tkind} bf16 burst",
-                                   "kernel": "cuBLAS FP16 GEMM (FP32 accumulation) of the heavy inner indices",
+                                   "all_gemms": [{"rows": timed_stats[i]["rows"], "cols": timed_stats[i]["cols"],
+                                                  "gemm_inner": timed_stats[i]["gemm_inner"],
+                                                  "gemm_limbs": timed_stats[i]["gemm_limbs"], "ms": gemm_ms[i],
+                                                  "tflops": 2.0 * macs_of[i] / (gemm_ms[i] / 1e3) / 1e12}
+                                                 for i in range(nprod) if gemm_ms[i] > 0],
+                                   "kernel": "k_tc_seed: tcgen05 FP16 GEMM (FP32 accumulation in TMEM, TMA-fed, "
+                                             "limbs combined into integer seeds) of the heavy inner indices",
                                    "product": {k: gb[k] for k in ("rows", "inner", "cols", "gemm_inner",
                                                                    "gemm_limbs")},
                                    "dense_multiply_adds": macs, "gemm_ms": gemm_ms[gi]}

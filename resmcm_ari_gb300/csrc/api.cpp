@@ -1048,7 +1048,6 @@ RMCM_API int32_t rmcm_destroy(rmcm_handle *h) {
         for (auto &e : r.ev)
             if (e) cudaEventDestroy(e);
     if (h->stream) cudaStreamSynchronize(h->stream);
-    cublas_destroy(h);
     if (h->scratch) dev_free(h, h->scratch, h->scratch_bytes);
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->d_status) cudaFree(h->d_status);

@@ -1,13 +1,13 @@
-// Tensor-core part of dense-bin products (sm_103a; cuBLAS FP16 GEMM, FP32
-// accumulation, exact integer results).
+// Tensor-core part of dense-bin products (sm_103a; FP16 limb GEMMs on
+// tcgen05 with FP32 accumulation in TMEM, exact integer results).
 //
 // A product C = A B whose output rows all sit in the dense bin often has a
 // few inner indices u (columns of A, rows of B) that carry most of its
 // multiply-adds: A's column u is nearly full and so is B's row u (in the
 // retail workload, the heaviest users of T x U . U x C).  For those, the
 // sub-product A[:, H] B[H, :] is dense work: it runs as a GEMM on the tensor
-// cores, and the dense-bin kernel streams only the remaining entries of A
-// into counters seeded with the GEMM's rows.
+// cores (k_tc_seed, tc_gemm.cu), and the dense-bin kernel streams only the
+// remaining entries of A into counters seeded with the GEMM's rows.
 //
 // Exactness.  A's heavy values (<= 2048) and B's heavy values split into L
 // limbs of `bits` bits (each <= 2047) are integers that FP16 holds exactly;
@@ -16,14 +16,14 @@
 // sum of a row's heavy A values, so FP32 holds each of them exactly in any
 // summation order.  The row's counter then takes sum_l G_l << (bits * l)
 // modulo 2^32, the uint32 value of the exact product (rows that could
-// overflow uint32 never come here).
+// overflow uint32 never come here); the GEMM's epilogue forms that sum and
+// writes one uint32 seed per output.
 //
 // The heavy set: an inner index is heavy when (A column count / rows) x
 // (B row length / cols) reaches 1 / inv_density, the point where a dense
 // multiply-add on the tensor cores costs less than the sparse ones it
 // replaces; column counts are sampled (every 8th entry of A).  Which indices
 // are heavy only moves work between the two parts, never changes a result.
-#include <cublas_v2.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -145,33 +145,79 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather_a(DevCsr A, const int
     }
 }
 
-// Limb l of the heavy rows of B: Bd[l][h][c] = (B[list[h]][c] >> (bits l)) &
-// (2^bits - 1) as FP16 (ld columns, zero elsewhere).  stats[2] = largest
-// value seen (checked against the limbs).
+// Limb l of B's heavy rows, transposed for the tensor cores (K contiguous):
+// BdT[l][c][h] = (B[list[h]][c] >> (bits l)) & (2^bits - 1) as FP16, for
+// c < ldn and h < ldk (zero where B has no entry, for h >= nh and c >= cols).
+// A CTA stages the 64 heavy rows h0.. over kBtCols columns in shared memory
+// (33-word pitch: the scatter of a warp's columns hits distinct banks) and
+// writes each output row's 128 bytes coalesced.  stats[2] = largest value.
+constexpr int kBtCols = 256;
+constexpr int kBtPitch = 66;   // halves per staged row: 64 heavy rows + 2
+
 template <typename V>
-__global__ void __launch_bounds__(kGatherThreads) k_gather_b(DevCsr B, const int32_t *list, int32_t nh, int32_t ld,
-                                                             int32_t limbs, int32_t bits, __half *Bd,
-                                                             int64_t limb_stride, unsigned long long *stats) {
+__global__ void __launch_bounds__(kGatherThreads) k_gather_bt(DevCsr B, const int32_t *list, int32_t nh, int32_t ldk,
+                                                              int32_t ldn, int32_t limbs, int32_t bits, __half *BdT,
+                                                              int64_t limb_stride, unsigned long long *stats) {
+    __shared__ __align__(16) __half tile[kBtCols * kBtPitch];
+    __shared__ int64_t s_beg[64], s_end[64];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int32_t h0 = (int32_t)blockIdx.x * 64;
+    const int32_t c0 = (int32_t)blockIdx.y * kBtCols;
+    const int32_t nc = min(kBtCols, ldn - c0);
+    if (threadIdx.x < 64) {
+        // the row's entries with columns in [c0, c0 + kBtCols): two lower bounds
+        const int32_t hr = h0 + (int32_t)threadIdx.x;
+        int64_t b = 0, e = 0;
+        if (hr < nh) {
+            const int32_t u = list[hr];
+            const int64_t end = B.rowptr[u + 1];
+            int64_t lo = B.rowptr[u], hi = end;
+            while (lo < hi) {
+                const int64_t mid = (lo + hi) >> 1;
+                if (B.col[mid] < c0) lo = mid + 1;
+                else hi = mid;
+            }
+            b = lo;
+            hi = end;
+            while (lo < hi) {
+                const int64_t mid = (lo + hi) >> 1;
+                if (B.col[mid] < c0 + kBtCols) lo = mid + 1;
+                else hi = mid;
+            }
+            e = lo;
+        }
+        s_beg[threadIdx.x] = b;
+        s_end[threadIdx.x] = e;
+    }
     const V *bv = (const V *)B.val;
     const V mask = ((V)1 << bits) - (V)1;
     unsigned long long mx = 0;
-    for (int64_t h = blockIdx.x; h < nh; h += gridDim.x) {
-        const int32_t u = list[h];
-        for (int l = 0; l < limbs; l++) {
-            uint4 *dst = (uint4 *)(Bd + l * limb_stride + h * (int64_t)ld);
-            for (int i = threadIdx.x; i < ld / 8; i += kGatherThreads) dst[i] = make_uint4(0, 0, 0, 0);
+    uint32_t *tw = (uint32_t *)tile;
+    for (int l = 0; l < limbs; l++) {
+        for (int i = threadIdx.x; i < kBtCols * kBtPitch / 2; i += kGatherThreads) tw[i] = 0u;
+        __syncthreads();
+        for (int hr = warp; hr < 64; hr += kGatherThreads / 32) {
+            const int64_t e = s_end[hr];
+            for (int64_t k = s_beg[hr] + lane; k < e; k += 32) {
+                const int32_t c = B.col[k];
+                const V v = bv[k];
+                if (l == 0) mx = (unsigned long long)v > mx ? (unsigned long long)v : mx;
+                tile[(c - c0) * kBtPitch + hr] = __uint2half_rn((uint32_t)((v >> (bits * l)) & mask));
+            }
         }
         __syncthreads();
-        for (int64_t k = B.rowptr[u] + threadIdx.x; k < B.rowptr[u + 1]; k += kGatherThreads) {
-            const V v = bv[k];
-            const int32_t c = B.col[k];
-            mx = (unsigned long long)v > mx ? (unsigned long long)v : mx;
-            for (int l = 0; l < limbs; l++)
-                Bd[l * limb_stride + h * (int64_t)ld + c] = __uint2half_rn((uint32_t)((v >> (bits * l)) & mask));
+        for (int cr = warp; cr < nc; cr += kGatherThreads / 32) {
+            uint32_t *dst = (uint32_t *)(BdT + l * limb_stride + (int64_t)(c0 + cr) * ldk + h0);
+            dst[lane] = tw[cr * (kBtPitch / 2) + lane];
         }
         __syncthreads();
     }
-    if (mx) atomicMax(stats + 2, mx);
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, mx, d);
+        mx = o > mx ? o : mx;
+    }
+    if (lane == 0 && mx) atomicMax(stats + 2, mx);
 }
 
 // uint64 products: per row of A the number of heavy entries and the largest
@@ -306,7 +352,7 @@ int32_t select_heavy(rmcm_handle *h, const DevCsr &A, const DevCsr &B, bool stat
 }
 
 // Builds the tensor-core part of C = A B (uint32, single-window dense rows):
-// on success dp.G holds L limb panels (rows x ld floats each) and dp.skip
+// on success dp.S holds the uint32 seeds (rows x ld) and dp.skip
 // flags the heavy inner indices; otherwise dp stays empty (and the product
 // runs sparse).  bmax: an upper bound on B's values.
 int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint64_t bmax, DensePart &dp,
@@ -334,11 +380,12 @@ int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint6
     // worth a GEMM only when the heavy part is a real share of the work
     if (nh < 64) return fail(RMCM_OK);
     const int64_t ldk = (nh + 63) / 64 * 64;
-    // dense panels: A (M x ldk) and up to 3 limbs of B (ldk x ldn), FP16; G (L x M x ldn), FP32
+    // dense panels: A (M x ldk) and up to 3 limbs of B held transposed
+    // (ldn x ldk), FP16; the seeds S (M x ldn), uint32
     const int64_t a_bytes = al(2 * M * ldk), b_limb = ldk * ldn, g_limb = M * ldn;
     const int64_t max_bytes = (h->budget - h->in_use) / 3;
     const int64_t l_bytes = al(8 * A.nnz) + al(4 * M);
-    if (a_bytes + l_bytes + al(2 * 3 * b_limb) + al(4 * 3 * g_limb) > max_bytes) return fail(RMCM_OK);
+    if (a_bytes + l_bytes + al(2 * 3 * b_limb) + al(4 * g_limb) > max_bytes) return fail(RMCM_OK);
     if (ldk * 2 > 160 * 1024) return fail(RMCM_OK);
     // A panel (freed once the GEMMs are queued); A's light entries
     // (compacted per row) and their counts (kept for the dense kernel)
@@ -382,43 +429,30 @@ int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint6
     while (bbits < 64 && (bmax >> bbits) != 0) bbits++;
     const int32_t limbs = std::max(1, (bbits + bits - 1) / bits);
     if (limbs > 3 || bits * (limbs - 1) >= 32) return fail2(RMCM_OK);
-    const int64_t bd_bytes = al(2 * limbs * b_limb), g_bytes = al(4 * limbs * g_limb);
+    const int64_t bd_bytes = al(2 * limbs * b_limb), g_bytes = al(4 * g_limb);
     char *mem = nullptr;
     if (dev_alloc(h, (void **)&mem, bd_bytes + g_bytes) != RMCM_OK) {
         h->last_error.clear();
         return fail2(RMCM_OK);
     }
-    __half *Bd = (__half *)mem;
-    float *G = (float *)(mem + bd_bytes);
+    __half *BdT = (__half *)mem;
+    uint32_t *S = (uint32_t *)(mem + bd_bytes);
     auto fail3 = [&](int32_t rc) {
         dev_free(h, mem, bd_bytes + g_bytes);
         return fail2(rc);
     };
-    k_gather_b<uint32_t><<<(int)std::min<int64_t>(nh, (int64_t)h->sm_count * 8), kGatherThreads, 0, s>>>(
-        B, list, (int32_t)nh, (int32_t)ldn, limbs, bits, Bd, b_limb, stats);
-    h->launches++;
-    if (ldk > nh) {
-        // padding rows of B's panels (heavy slots past nh) are zero
-        for (int l = 0; l < limbs; l++)
-            RMCM_CUDA(h, cudaMemsetAsync(Bd + l * b_limb + nh * ldn, 0, 2 * (ldk - nh) * ldn, s));
+    {
+        dim3 grid((unsigned)(ldk / 64), (unsigned)((ldn + kBtCols - 1) / kBtCols));
+        k_gather_bt<uint32_t><<<grid, kGatherThreads, 0, s>>>(B, list, (int32_t)nh, (int32_t)ldk, (int32_t)ldn,
+                                                             limbs, bits, BdT, b_limb, stats);
+        h->launches++;
+        RMCM_CUDA(h, cudaGetLastError());
     }
-    RMCM_CUDA(h, cudaGetLastError());
-    if (!h->cublas) {
-        cublasHandle_t cb = nullptr;
-        if (cublasCreate(&cb) != CUBLAS_STATUS_SUCCESS) return fail3(RMCM_OK);
-        h->cublas = cb;
-    }
-    cublasHandle_t cb = (cublasHandle_t)h->cublas;
-    if (cublasSetStream(cb, s) != CUBLAS_STATUS_SUCCESS) return fail3(set_error(h, RMCM_ECUDA, "cublasSetStream"));
-    // row-major G_l (M x N) = Ad (M x ldk) Bd_l (ldk x N): column-major G_l^T = Bd_l^T Ad^T
-    const float one = 1.0f, zero = 0.0f;
     if (ev_begin) cudaEventRecord(ev_begin, s);
-    for (int l = 0; l < limbs; l++) {
-        const cublasStatus_t st = cublasGemmEx(cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)N, (int)M, (int)ldk, &one,
-                                               Bd + l * b_limb, CUDA_R_16F, (int)ldn, Ad, CUDA_R_16F, (int)ldk,
-                                               &zero, G + l * g_limb, CUDA_R_32F, (int)ldn, CUBLAS_COMPUTE_32F,
-                                               CUBLAS_GEMM_DEFAULT);
-        if (st != CUBLAS_STATUS_SUCCESS) return fail3(set_error(h, RMCM_ECUDA, "dense part: cublasGemmEx failed"));
+    {
+        const int32_t rc = tc_seed_gemm(h, Ad, BdT, M, N, ldn, 1, limbs, ldk, 1, bits, 4, S, h->d_status + kTimeout);
+        if (rc == RMCM_EINVAL) return fail3(RMCM_OK);   // a shape the kernel does not take: stay sparse
+        if (rc != RMCM_OK) return fail3(rc);
     }
     if (ev_end) cudaEventRecord(ev_end, s);
     // the B gather saw no value wider than the limbs
@@ -434,9 +468,8 @@ int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint6
     dp.lcnt = lcnt;
     dp.mem = mem;
     dp.bytes = bd_bytes + g_bytes;
-    dp.G = G;
+    dp.S = S;
     dp.ld = ldn;
-    dp.limb_stride = g_limb;
     dp.limbs = limbs;
     dp.bits = bits;
     dp.heavy = nh;
@@ -517,9 +550,9 @@ int32_t dense_part_build64(rmcm_handle *h, const DevCsr &A, const DevCsr &B, Den
     if (best_bits == 0) return fail(RMCM_OK);
     const int32_t bits = best_bits, la = best_la, lb = best_lb;
     const int64_t kc = best_kc, nq = best_nq, ldk = kc * nq;
-    const int64_t a_limb = M * ldk, b_limb = ldk * ldn, g_panel = M * ldn, npan = (int64_t)la * lb * nq;
+    const int64_t a_limb = M * ldk, b_limb = ldk * ldn, g_panel = M * ldn;
     const int64_t a_bytes = al(2 * la * a_limb), l_bytes = al(12 * A.nnz) + al(4 * M);
-    const int64_t bd_bytes = al(2 * lb * b_limb), g_bytes = al(4 * npan * g_panel);
+    const int64_t bd_bytes = al(2 * lb * b_limb), g_bytes = al(8 * g_panel);
     if (a_bytes + l_bytes + bd_bytes + g_bytes > (h->budget - h->in_use) / 3) return fail(RMCM_OK);
     if (ldk * 2 > 160 * 1024) return fail(RMCM_OK);
     __half *Ad = nullptr;
@@ -543,8 +576,8 @@ int32_t dense_part_build64(rmcm_handle *h, const DevCsr &A, const DevCsr &B, Den
     int32_t *lcol = (int32_t *)amem;
     uint64_t *lval = (uint64_t *)(amem + al(4 * A.nnz));
     int32_t *lcnt = (int32_t *)(amem + al(12 * A.nnz));
-    __half *Bd = (__half *)mem;
-    float *G = (float *)(mem + bd_bytes);
+    __half *BdT = (__half *)mem;
+    uint64_t *S = (uint64_t *)(mem + bd_bytes);
     {
         const int64_t smem = ldk * 2;
         if (smem > 48 * 1024 &&
@@ -554,34 +587,20 @@ int32_t dense_part_build64(rmcm_handle *h, const DevCsr &A, const DevCsr &B, Den
         }
         const int grid = (int)std::min<int64_t>(M, (int64_t)h->sm_count * 8);
         k_gather_a64<<<grid, kGatherThreads, smem, s>>>(A, slot, (int32_t)ldk, la, bits, Ad, a_limb, lcol, lval, lcnt);
-        k_gather_b<uint64_t><<<(int)std::min<int64_t>(nh, (int64_t)h->sm_count * 8), kGatherThreads, 0, s>>>(
-            B, list, (int32_t)nh, (int32_t)ldn, lb, bits, Bd, b_limb, stats);
+        dim3 bgrid((unsigned)(ldk / 64), (unsigned)((ldn + kBtCols - 1) / kBtCols));
+        k_gather_bt<uint64_t><<<bgrid, kGatherThreads, 0, s>>>(B, list, (int32_t)nh, (int32_t)ldk, (int32_t)ldn, lb,
+                                                              bits, BdT, b_limb, stats);
         h->launches += 2;
-        if (ldk > nh)
-            for (int l = 0; l < lb; l++)
-                RMCM_CUDA(h, cudaMemsetAsync(Bd + l * b_limb + nh * ldn, 0, 2 * (ldk - nh) * ldn, s));
         RMCM_CUDA(h, cudaGetLastError());
     }
-    if (!h->cublas) {
-        cublasHandle_t cb = nullptr;
-        if (cublasCreate(&cb) != CUBLAS_STATUS_SUCCESS) return fail3(RMCM_OK);
-        h->cublas = cb;
-    }
-    cublasHandle_t cb = (cublasHandle_t)h->cublas;
-    if (cublasSetStream(cb, s) != CUBLAS_STATUS_SUCCESS) return fail3(set_error(h, RMCM_ECUDA, "cublasSetStream"));
-    // per limb pair: G_(i,j,q) = Ad_i[:, chunk q] Bd_j[chunk q, :], the chunks as one strided batch
-    const float one = 1.0f, zero = 0.0f;
+    // every limb pair and chunk of the heavy indices in one kernel, summed
+    // with its shift into one uint64 seed per output
     if (ev_begin) cudaEventRecord(ev_begin, s);
-    for (int i = 0; i < la; i++)
-        for (int j = 0; j < lb; j++) {
-            const cublasStatus_t st = cublasGemmStridedBatchedEx(
-                cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)N, (int)M, (int)kc, &one, Bd + j * b_limb, CUDA_R_16F, (int)ldn,
-                (long long)kc * ldn, Ad + i * a_limb, CUDA_R_16F, (int)ldk, (long long)kc, &zero,
-                G + ((int64_t)i * lb + j) * nq * g_panel, CUDA_R_32F, (int)ldn, (long long)g_panel, (int)nq,
-                CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
-            if (st != CUBLAS_STATUS_SUCCESS)
-                return fail3(set_error(h, RMCM_ECUDA, "dense part: cublasGemmStridedBatchedEx failed"));
-        }
+    {
+        const int32_t rc = tc_seed_gemm(h, Ad, BdT, M, N, ldn, la, lb, kc, nq, bits, 8, S, h->d_status + kTimeout);
+        if (rc == RMCM_EINVAL) return fail3(RMCM_OK);
+        if (rc != RMCM_OK) return fail3(rc);
+    }
     if (ev_end) cudaEventRecord(ev_end, s);
     dev_free(h, Ad, a_bytes);
     dp.amem = amem;
@@ -591,9 +610,8 @@ int32_t dense_part_build64(rmcm_handle *h, const DevCsr &A, const DevCsr &B, Den
     dp.lcnt = lcnt;
     dp.mem = mem;
     dp.bytes = bd_bytes + g_bytes;
-    dp.G = G;
+    dp.S = S;
     dp.ld = ldn;
-    dp.limb_stride = g_panel;
     dp.limbs = lb;
     dp.bits = bits;
     dp.alimbs = la;
@@ -611,11 +629,6 @@ void dense_part_release(rmcm_handle *h, DensePart &dp) {
     if (dp.mem) dev_free(h, dp.mem, dp.bytes);
     if (dp.sel) dev_free(h, dp.sel, dp.sel_bytes);
     dp = DensePart{};
-}
-
-void cublas_destroy(rmcm_handle *h) {
-    if (h->cublas) cublasDestroy((cublasHandle_t)h->cublas);
-    h->cublas = nullptr;
 }
 
 }  // namespace rmcm

@@ -151,7 +151,6 @@ struct rmcm_handle {
     std::set<rmcm_batch *> batches;  // batches recorded on this handle
     bool abort_on_certain_overflow = false;   // spgemm returns EOVERFLOW before computing when sure
     int32_t order_mode = RMCM_ORDER_RES;
-    void *cublas = nullptr;          // cuBLAS handle of the dense-bin GEMMs (created on first use)
 };
 
 struct rmcm_graph {
@@ -212,13 +211,14 @@ int32_t spgemm(rmcm_handle *h, const rmcm_mat *A, const rmcm_mat *B, rmcm_mat **
                ProductPlan *plan = nullptr);
 int32_t fill_ones(rmcm_handle *h, void *val, int64_t nnz, int32_t valtype);
 int32_t convert_values(rmcm_handle *h, const rmcm_mat *src, int32_t valtype, rmcm_mat **out);
-// dense_gemm.cu: tensor-core part of a uint32 dense-bin product.  G holds
-// `limbs` FP32 panels (A.rows x ld, limb_stride apart); row r's uint32 part is
-// sum_l G_l[r][c] << (bits * l).  skip[u] flags the inner indices it covers;
-// the entries of A on the others are listed per row (lcol, lval, lcnt).
+// dense_gemm.cu: tensor-core part of a dense-bin product.  S holds the
+// dense part's exact counts in the product's value type (A.rows x ld): the
+// sum over the limb GEMMs of G << (bits (i + j)), formed by the GEMM's
+// epilogue (tc_gemm.cu).  skip[u] flags the inner indices it covers; the
+// entries of A on the others are listed per row (lcol, lval, lcnt).
 struct DensePart {
-    const float *G = nullptr;
-    int64_t ld = 0, limb_stride = 0;
+    const void *S = nullptr;
+    int64_t ld = 0;
     int32_t limbs = 0, bits = 0;      // B's limbs
     int32_t alimbs = 1, abits = 0;    // A's limbs (uint64 products; 1 and 0 for uint32)
     int32_t chunks = 1;               // chunks of the heavy indices (uint64 products)
@@ -234,12 +234,16 @@ struct DensePart {
 // ev_begin / ev_end (may be null) are recorded around the GEMMs.
 int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint64_t bmax, DensePart &dp,
                          cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr);
-// uint64 products: A split into limbs too and the heavy indices into chunks;
-// G panel ((i * limbs + j) * chunks + q) adds G << (bits * (i + j)).
+// uint64 products: A split into limbs too and the heavy indices into chunks.
 int32_t dense_part_build64(rmcm_handle *h, const DevCsr &A, const DevCsr &B, DensePart &dp,
                            cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr);
 void dense_part_release(rmcm_handle *h, DensePart &dp);
-void cublas_destroy(rmcm_handle *h);
+// tc_gemm.cu: S (M x ldn of uint32 or uint64, vbytes) = sum over limbs and
+// chunks of Ad_i[:, chunk q] BdT_j[:, chunk q]^T << (bits (i + j)), on
+// tcgen05; RMCM_EINVAL for shapes it does not take.
+int32_t tc_seed_gemm(rmcm_handle *h, const void *Ad, const void *BdT, int64_t M, int64_t N, int64_t ldn,
+                     int32_t la, int32_t lb, int64_t kc, int64_t nq, int32_t bits, int32_t vbytes, void *S,
+                     int *err_dev);
 // estimator.cu: c_dev[len*len] on the device
 int32_t estimate(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, double *c_dev);
 // chain_dp.cu: split/cost/pairs on the device

@@ -1410,18 +1410,17 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
 // stride `tstride` entries) and its length goes to cnt[r]; the symbolic pass
 // is skipped for these rows and k_copy_rows compacts the slots into C.
 // Per-product extras of the dense bin (single-window rows only): the packed
-// copy of B (k_pack_banked) and the tensor-core part of the product (G panels
-// of uint32 limbs; skip[u] flags the inner indices it covers, whose A entries
-// the kernel leaves out).
+// copy of B (k_pack_banked) and the tensor-core part of the product (S: the
+// dense part's counts in the product's value type, one row of gld per row of
+// A; skip[u] flags the inner indices it covers, whose A entries the kernel
+// leaves out).
 struct DenseExtra {
     const uint32_t *pk = nullptr;
     int32_t cbits = 0;
-    int32_t glimbs = 0, gbits = 0;     // limbs of B
-    int32_t galimbs = 1, gchunks = 1;  // limbs of A, chunks of the heavy indices (same limb width)
-    const float *G = nullptr;
-    int64_t gld = 0, gstride = 0;
+    const void *S = nullptr;
+    int64_t gld = 0;
     const uint8_t *skip = nullptr;
-    const int32_t *lcnt = nullptr;   // with G: row r has lcnt[r] entries (A's light ones) from rowptr[r]
+    const int32_t *lcnt = nullptr;   // with S: row r has lcnt[r] entries (A's light ones) from rowptr[r]
 };
 
 template <typename V, bool NUMERIC, bool TEMP, bool PRES = true>
@@ -1485,22 +1484,10 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
             }
         };
         if constexpr (NUMERIC) {
-            if (ex.G) {
-                // the row's tensor-core part seeds the counters (one window):
-                // panel (i, j, q) adds G << (gbits (i + j)), modulo 2^bits(V)
-                const float *g = ex.G + (int64_t)r * ex.gld;
-                for (int c = tid; c < (int)B.cols; c += NT) {
-                    V v = 0;
-                    int p = 0;
-                    for (int i = 0; i < ex.galimbs; i++)
-                        for (int j = 0; j < ex.glimbs; j++) {
-                            const int sh = ex.gbits * (i + j);
-                            for (int q = 0; q < ex.gchunks; q++, p++)
-                                if (sh < 8 * (int)sizeof(V))
-                                    v += (V)__float2ull_rn(g[(int64_t)p * ex.gstride + c]) << sh;
-                        }
-                    acc[c] = v;
-                }
+            if (ex.S) {
+                // the row's tensor-core part seeds the counters (one window)
+                const V *g = (const V *)ex.S + (int64_t)r * ex.gld;
+                for (int c = tid; c < (int)B.cols; c += NT) acc[c] = g[c];
                 __syncthreads();
             }
         }
@@ -2565,14 +2552,9 @@ DenseExtra dense_extra(const DenseTemp *t, bool single_pass) {
     if (!t) return e;
     e.pk = t->pk;
     e.cbits = t->cbits;
-    if (single_pass && t->dpart.G) {
-        e.G = t->dpart.G;
+    if (single_pass && t->dpart.S) {
+        e.S = t->dpart.S;
         e.gld = t->dpart.ld;
-        e.gstride = t->dpart.limb_stride;
-        e.glimbs = t->dpart.limbs;
-        e.gbits = t->dpart.bits;
-        e.galimbs = t->dpart.alimbs;
-        e.gchunks = t->dpart.chunks;
         e.lcnt = t->dpart.lcnt;
     }
     return e;
@@ -2734,7 +2716,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                         const int32_t dn = temp->split ? temp->n_front : n;
                         // with a tensor-core part, A's light entries only
                         DevCsr Al = A;
-                        if (temp->dpart.G) {
+                        if (temp->dpart.S) {
                             Al.col = const_cast<int32_t *>(temp->dpart.lcol);
                             Al.val = const_cast<uint32_t *>(temp->dpart.lval);
                         }
@@ -3062,7 +3044,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         int32_t cbits = 0;
         if (replay) {
             cbits = plan->pack_cbits;
-        } else if (pack_cand && counts[kBinDense] > 0 && flops_total >= kPackReuse * B.nnz && !dtemp.dpart.G) {
+        } else if (pack_cand && counts[kBinDense] > 0 && flops_total >= kPackReuse * B.nnz && !dtemp.dpart.S) {
             // (with a tensor-core part the light rows left are short: no packing)
             uint64_t bmax = 1;
             if (!Bm->ones) memcpy(&bmax, (int32_t *)h->h_pinned + 58, sizeof(uint64_t));
@@ -3095,7 +3077,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     if (replay) max_dense_f = plan->max_dense_flops;
     else memcpy(&max_dense_f, (int32_t *)h->h_pinned + 36, sizeof(int64_t));
     if (record) plan->max_dense_flops = max_dense_f;
-    if (dtemp.active && !dtemp.dpart.G) {
+    if (dtemp.active && !dtemp.dpart.S) {
         // (with a tensor-core part the heaviest work is in the GEMM: no split)
         const int64_t fpart = std::max<int64_t>(kSplitMinFlops, flops_total / ((int64_t)h->sm_count * 4));
         if (max_dense_f > fpart) {
@@ -3309,8 +3291,8 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     if (rc == RMCM_OK && !adopt)
         rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap, &dtemp,
                                   bin_of, positive, Bm->distinct, &rsplit);
-    const int32_t gemm_limbs = dtemp.dpart.G ? dtemp.dpart.limbs * dtemp.dpart.alimbs : 0;
-    const int64_t gemm_inner = dtemp.dpart.G ? dtemp.dpart.heavy : 0;
+    const int32_t gemm_limbs = dtemp.dpart.S ? dtemp.dpart.limbs * dtemp.dpart.alimbs : 0;
+    const int64_t gemm_inner = dtemp.dpart.S ? dtemp.dpart.heavy : 0;
     drop_cursors();
     drop_temp();
     drop_rank();

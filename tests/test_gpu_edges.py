@@ -693,10 +693,11 @@ def _heavy_inner(rng, m, k, n, nheavy, bbig=None):
     return A, B
 
 
-@pytest.mark.parametrize("bbig", [None, 5000, 200000])
-def test_tensor_core_part_of_dense_rows(native, bbig):
-    """Heavy inner indices multiplied as an FP16 GEMM with FP32 accumulation
-    (B split into limbs when its values are wide): the product equals scipy's
+@pytest.mark.parametrize("bbig,limbs", [(None, 1), (5000, 2), (200000, 2), (5000000, 3)])
+def test_tensor_core_part_of_dense_rows(native, bbig, limbs):
+    """Heavy inner indices multiplied as FP16 GEMMs on the tensor cores with
+    FP32 accumulation (B split into one to three limbs when its values are
+    wide, the limbs summed by the GEMM's epilogue): the product equals scipy's
     and the same product with the GEMM turned off, bit for bit."""
     rng = np.random.default_rng(70 if bbig is None else bbig)
     A, B = _heavy_inner(rng, 1200, 2500, 1500, 300, bbig)
@@ -705,7 +706,7 @@ def test_tensor_core_part_of_dense_rows(native, bbig):
     eng.set_profiling(1)
     _check_product(native, eng, A, B, native.VAL_U32)
     st = eng.product_stats()[-1]
-    assert st["gemm_inner"] >= 250 and st["gemm_limbs"] == (1 if bbig is None else 2)
+    assert st["gemm_inner"] >= 250 and st["gemm_limbs"] == limbs
     eng.set_tuning(gemm_inv_density=0)
     _check_product(native, eng, A, B, native.VAL_U32)
     assert eng.product_stats()[-1]["gemm_inner"] == 0
@@ -772,5 +773,51 @@ def test_tensor_core_part_uint64(native):
     assert st["gemm_inner"] >= 250 and st["gemm_limbs"] >= 4
     eng.set_tuning(gemm_inv_density=0)
     _check_product(native, eng, A, B, native.VAL_U64)
+    assert eng.product_stats()[-1]["gemm_inner"] == 0
+    eng.close()
+
+
+@pytest.mark.parametrize("m,n,heavy", [(256, 90, 300), (129, 1030, 200), (640, 384, 513), (131, 2100, 64)])
+def test_tensor_core_part_tile_edges(native, m, n, heavy):
+    """The tensor-core GEMM's 128 x 128 output tiles and 64-wide K blocks at
+    their edges: rows and columns that fill a tile exactly, fall one short or
+    one over, fewer columns than a tile and than a multiple of 8, and heavy
+    index counts just past a K block.  Equal to scipy and to the GEMM off."""
+    rng = np.random.default_rng(m * 7919 + n)
+    A, B = _heavy_inner(rng, m, heavy + 900, n, heavy)
+    eng = native.Engine(device=0)
+    eng.set_tuning(gemm_min_mflops=0)
+    eng.set_profiling(1)
+    _check_product(native, eng, A, B, native.VAL_U32)
+    assert eng.product_stats()[-1]["gemm_inner"] >= heavy // 2
+    _check_product(native, eng, A, B, native.VAL_U64)
+    assert eng.product_stats()[-1]["gemm_inner"] >= heavy // 2
+    eng.set_tuning(gemm_inv_density=0)
+    _check_product(native, eng, A, B, native.VAL_U32)
+    assert eng.product_stats()[-1]["gemm_inner"] == 0
+    eng.close()
+
+
+@pytest.mark.parametrize("vt,m,n,heavy,scale_a,bbig", [
+    ("u32", 300, 500, 1100, 1, None),        # 4 tiles of 256 x 256, 18 K blocks: every tile in two units
+    ("u64", 1200, 1500, 600, 1000, 200000),  # two A and two B limbs, 10 chunks: units span several groups
+])
+def test_tensor_core_part_split_units(native, vt, m, n, heavy, scale_a, bbig):
+    """Fewer output tiles than SMs: the tensor-core GEMM splits each tile's
+    K blocks over several CTAs that add their parts into the seeds with
+    atomics.  Equal to scipy and to the GEMM off, bit for bit."""
+    rng = np.random.default_rng(m + n + heavy)
+    A, B = _heavy_inner(rng, m, heavy + 1500, n, heavy, bbig)
+    A = A.tocsr()
+    A.data = A.data * scale_a
+    val = native.VAL_U32 if vt == "u32" else native.VAL_U64
+    eng = native.Engine(device=0)
+    eng.set_tuning(gemm_min_mflops=0)
+    eng.set_profiling(1)
+    for _ in range(2):
+        _check_product(native, eng, A, B, val)
+        assert eng.product_stats()[-1]["gemm_inner"] >= heavy // 2
+    eng.set_tuning(gemm_inv_density=0)
+    _check_product(native, eng, A, B, val)
     assert eng.product_stats()[-1]["gemm_inner"] == 0
     eng.close()
