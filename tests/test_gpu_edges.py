@@ -295,6 +295,22 @@ def test_rank_bin_for_wide_rows(native, engine, n):
         _check_product(native, engine, A, B, vt)
 
 
+def test_rank_bin_short_and_long_wide_rows(native, engine):
+    """2^20-column rows in one rank launch: most with ~10K entries, two with
+    more than 30K; uint32 and uint64 match scipy."""
+    rng = np.random.default_rng(37)
+    m, k, n = 30, 3000, 1 << 20
+    a_nnz = rng.integers(150, 250, m)
+    a_nnz[5] = 700
+    a_nnz[17] = 900
+    A = _random_csr(rng, m, k, a_nnz, vmax=3)
+    B = _random_csr(rng, k, n, rng.integers(40, 80, k), vmax=3)
+    ref = (A @ B).tocsr()
+    assert np.diff(ref.indptr).max() > 30_000 and np.median(np.diff(ref.indptr)) < 15_000
+    for vt in (native.VAL_U32, native.VAL_U64):
+        _check_product(native, engine, A, B, vt)
+
+
 def test_rank_bin_detects_overflow(native, engine):
     import ctypes
     rng = np.random.default_rng(32)
