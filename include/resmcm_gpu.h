@@ -227,6 +227,23 @@ RMCM_API int32_t rmcm_chain(rmcm_handle *h, rmcm_mat *const *chain, int32_t len,
 RMCM_API int32_t rmcm_run_metapath(rmcm_handle *h, rmcm_graph *g, const char *metapath, rmcm_mat **C,
                                    rmcm_timings *t);
 
+/* ---- whole meta-path, result delivered in blocks of rows ------------------
+ * The executor of SSP_dynamic (efficient/resmcm.cpp:702-760) and the nnz
+ * count of main (:859-868), for results too large to hold on the device: the
+ * chain runs as rmcm_run_metapath, except that its final product is computed
+ * a block of rows at a time (rows of its left operand) and each block is
+ * handed to fn as a device matrix (rows block_rows x the result's columns,
+ * row pointers from 0, valid only during the call; row0 = the block's first
+ * row in the result), then freed.  rows_per_block 0 lets the library choose:
+ * a block's RES-estimated entries take at most a quarter of the device
+ * memory left under the handle's budget.  A non-OK return from fn stops the
+ * chain with that status.  t->nnz is the sum over the blocks.  In AUTO mode
+ * blocks that fit uint32 are delivered as uint32 and, after the first block
+ * that overflows, the rest as uint64 (each block's values are exact). */
+typedef int32_t (*rmcm_block_fn)(void *user, int64_t row0, const rmcm_mat *block);
+RMCM_API int32_t rmcm_run_metapath_blocks(rmcm_handle *h, rmcm_graph *g, const char *metapath,
+                                          int64_t rows_per_block, rmcm_block_fn fn, void *user, rmcm_timings *t);
+
 /* Order used by rmcm_run_metapath / rmcm_chain when no pair list is given.
  * The ablation orders of the reference's l2r and naive programs skip the
  * estimator (es time 0), exactly as those programs do. */
@@ -329,6 +346,11 @@ RMCM_API int32_t rmcm_batch_free(rmcm_handle *h, rmcm_batch *b);
  * over entries (r, c, v) of f(f(r * 2^32 + c) + v), f the splitmix64 output
  * function.  Equal matrices give equal digests.  Synchronises the stream. */
 RMCM_API int32_t rmcm_mat_digest(rmcm_handle *h, const rmcm_mat *m, uint64_t *nnz, uint64_t *digest);
+/* rmcm_mat_digest of m taken as rows row0.. of a larger matrix: the digests of
+ * a result's blocks (rmcm_run_metapath_blocks) add up, mod 2^64, to the
+ * digest of the whole result.  No counterpart in the reference. */
+RMCM_API int32_t rmcm_mat_digest_rows(rmcm_handle *h, const rmcm_mat *m, int64_t row0, uint64_t *nnz,
+                                      uint64_t *digest);
 
 /* ---- query server ------------------------------------------------------------
  * A request loop over resident graphs: the reference's per-meta-path steps

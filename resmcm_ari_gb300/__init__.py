@@ -172,6 +172,8 @@ def lib():
         "rmcm_batch_info": ([vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)], i32),
         "rmcm_batch_free": ([vp, vp], i32),
         "rmcm_mat_digest": ([vp, vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], i32),
+        "rmcm_mat_digest_rows": ([vp, vp, i64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], i32),
+        "rmcm_run_metapath_blocks": ([vp, vp, C.c_char_p, i64, BLOCK_FN, vp, C.POINTER(Timings)], i32),
         "rmcm_set_tuning": ([vp, C.POINTER(Tuning)], i32),
         "rmcm_get_tuning": ([vp, C.POINTER(Tuning)], i32),
         "rmcm_server_create": ([vp, C.POINTER(ServerOpts), pp], i32),
@@ -189,6 +191,10 @@ def lib():
         fn.restype = res
     _lib = L
     return L
+
+
+# rmcm_block_fn: (user, row0, block) -> status
+BLOCK_FN = C.CFUNCTYPE(C.c_int32, C.c_void_p, C.c_int64, C.c_void_p)
 
 
 def order_l2r(length: int) -> np.ndarray:
@@ -622,6 +628,35 @@ class Engine:
                                                  C.byref(h) if keep else None, C.byref(t)),
                          allow=(OK, EOVERFLOW))
         return (Matrix(self, h.value) if keep else None), t.as_dict(), rc
+
+    def run_metapath_blocks(self, graph: HeteroGraph, metapath: str, on_block, rows_per_block: int = 0):
+        """rmcm_run_metapath_blocks: the result arrives in blocks of rows;
+        on_block(row0, Matrix) is called for each (the matrix is valid only
+        during the call).  Returns (timings, status)."""
+        err = []
+
+        def cb(_user, row0, blk):
+            try:
+                on_block(int(row0), Matrix(self, blk, owned=False))
+                return OK
+            except Exception as e:  # noqa: BLE001 -- re-raised after the call
+                err.append(e)
+                return EINVAL
+
+        fn = BLOCK_FN(cb)
+        t = Timings()
+        rc = lib().rmcm_run_metapath_blocks(self._h, graph._h, metapath.encode(), int(rows_per_block), fn, None,
+                                           C.byref(t))
+        if err:
+            raise err[0]
+        self._check(rc, allow=(OK, EOVERFLOW))
+        return t.as_dict(), rc
+
+    def digest_rows(self, m: Matrix, row0: int) -> tuple:
+        """(nnz, digest) of a block taken as rows row0.. of a larger matrix."""
+        n, d = C.c_uint64(), C.c_uint64()
+        self._check(lib().rmcm_mat_digest_rows(self._h, m._h, int(row0), C.byref(n), C.byref(d)))
+        return n.value, d.value
 
     def get_tuning(self) -> dict:
         t = Tuning()

@@ -531,9 +531,17 @@ void dense_order(const int64_t *d, int32_t len, std::vector<int32_t> &split, std
 // counts having fit), and the rest of the chain continues in uint64.  Leaves
 // in uint64 come from `leaf64` when given (the graph's cache), else are
 // widened here.
+//
+// With `sink` set, the final product is computed in blocks of rows of its
+// left operand (a row range of a CSR is its row pointers from the range's
+// first row on) and every block goes to the sink, then is freed: a result
+// larger than the free device memory never exists whole on the device.  The
+// block height is the sink's, or chosen so that a block's estimated entries
+// (RES estimate of the whole chain, spread evenly over the rows) take at most
+// a quarter of the memory left under the budget.  *Cout stays null.
 int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int32_t *fixed_pairs, rmcm_mat **Cout,
                    rmcm_timings *t, bool widen, const std::function<int32_t(int, rmcm_mat **)> &leaf64,
-                   ChainLog *log = nullptr, bool order_given = false) {
+                   ChainLog *log = nullptr, bool order_given = false, const BlockSink *sink = nullptr) {
     rmcm_timings tm{};
     *Cout = nullptr;
     // slot bookkeeping of the optional log
@@ -593,6 +601,11 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
     int32_t pairs[32];
     int32_t rc = RMCM_OK;
     double host_dp_s = -1;
+    double est_result = -1;        // RES estimate of the result's nnz (blocked final product)
+    int64_t block_next = 0;        // blocked final product: first row not yet delivered
+    int64_t block_nnz = 0;
+    bool delivered = false;
+    int32_t block_rc = RMCM_OK;    // EOVERFLOW kept from a delivered block (fixed value type)
     if (!fixed_pairs && h->order_mode != RMCM_ORDER_RES) {
         // ablation orders: no estimator, order computed on the host
         cudaEventRecord(ev[1], s);
@@ -660,6 +673,13 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
             else memcpy(pairs, h->h_pinned, sizeof(int32_t) * 2 * (len - 1));
         }
     }
+    if (rc == RMCM_OK && sink) {
+        // the whole chain's estimated nnz sizes the result's blocks
+        cudaError_t e = cudaMemcpyAsync(h->h_pinned, c_dev + (len - 1), sizeof(double), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = cuda_error(h, e, "estimate download");
+        else memcpy(&est_result, h->h_pinned, sizeof(double));
+    }
     dev_free(h, ord, ord_bytes);
     dev_free(h, c_dev, 8 * 256);
     if (rc != RMCM_OK) return rc;
@@ -725,6 +745,97 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
             else B = stack[sz - 1];
         }
         if (rc != RMCM_OK) break;
+        if (sink && p == len - 2) {
+            // the final product, a block of rows of A at a time
+            const int64_t rows = A->d.rows;
+            int64_t rb = sink->rows_per_block;
+            if (rb <= 0) {
+                const double row_bytes = est_result > 0 && rows > 0
+                                             ? (est_result / (double)rows) * (4.0 + (double)val_bytes(cur)) + 48.0
+                                             : 0.0;
+                const double room = (double)std::max<int64_t>(h->budget - h->in_use, 0) / 4.0;
+                rb = row_bytes > 0 ? (int64_t)std::max(1.0, room / row_bytes) : rows;
+            }
+            rb = std::max<int64_t>(1, std::min<int64_t>(rb, std::max<int64_t>(rows, 1)));
+            bool need_widen = false;
+            while (block_next < rows && rc == RMCM_OK) {
+                const int64_t r0 = block_next, r1 = std::min(rows, r0 + rb);
+                // row view of A: its row pointers from r0 on (entries keep
+                // their positions, so nnz stays A's)
+                rmcm_mat *view = new rmcm_mat(*A);
+                view->d.rowptr = A->d.rowptr + r0;
+                view->d.rows = r1 - r0;
+                view->d.rowsum = nullptr;
+                view->d.info = nullptr;
+                view->rowsum = nullptr;
+                view->est_long = nullptr;
+                view->n_est_long = -1;
+                view->xfer_done = nullptr;
+                view->graph_owned = true;
+                view->bytes = 0;
+                cudaEventRecord(ev[3], s);
+                rmcm_mat *Cb = nullptr;
+                int64_t fl = 0;
+                h->abort_on_certain_overflow = widen && cur == RMCM_VAL_U32;
+                rc = spgemm(h, view, B, &Cb, &fl, nullptr);
+                h->abort_on_certain_overflow = false;
+                cudaEventRecord(ev[4], s);
+                if (view->rowsum) dev_free(h, view->rowsum, 8 * (view->d.rows + 1) + 8 * view->d.rows);
+                delete view;
+                if (rc == RMCM_EOVERFLOW && widen && cur == RMCM_VAL_U32 && !Cb) {
+                    rc = RMCM_OK;
+                    need_widen = true;
+                    break;
+                }
+                if (rc != RMCM_OK) break;
+                cudaEventSynchronize(ev[4]);
+                spgemm_s += elapsed_s(ev[3], ev[4]);
+                const int32_t st = check_status(h);
+                if (st == RMCM_EOVERFLOW && widen && cur == RMCM_VAL_U32) {
+                    mat_release(h, Cb);
+                    need_widen = true;
+                    break;
+                }
+                if (st == RMCM_EOVERFLOW) {
+                    Cb->positive = false;
+                    block_rc = RMCM_EOVERFLOW;
+                } else if (st != RMCM_OK) {
+                    mat_release(h, Cb);
+                    rc = st;
+                    break;
+                }
+                tm.flops += fl;
+                block_nnz += Cb->d.nnz;
+                const int32_t urc = sink->fn(sink->user, r0, Cb);
+                mat_release(h, Cb);
+                if (urc != RMCM_OK) {
+                    rc = set_error(h, urc, "the block sink stopped the chain");
+                    break;
+                }
+                block_next = r1;
+            }
+            if (rc != RMCM_OK) break;
+            if (need_widen) {
+                // blocks delivered so far fitted uint32 and are exact; the
+                // rest of the final product runs in uint64
+                cur = RMCM_VAL_U64;
+                for (auto &m : stack) {
+                    rmcm_mat *w = nullptr;
+                    rc = convert_values(h, m, RMCM_VAL_U64, &w);
+                    if (rc != RMCM_OK) break;
+                    mat_release(h, m);
+                    m = w;
+                }
+                if (rc != RMCM_OK) break;
+                p--;
+                continue;
+            }
+            tm.n_products++;
+            for (auto *m : stack) mat_release(h, m);
+            stack.clear();
+            delivered = true;
+            break;
+        }
         cudaEventRecord(ev[3], s);
         rmcm_mat *C = nullptr;
         int64_t fl = 0;
@@ -824,6 +935,11 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
     tm.spgemm_s = spgemm_s;
     tm.total_s = elapsed_s(ev[0], ev[5]);
     tm.valtype = cur;
+    if (delivered) {
+        tm.nnz = block_nnz;
+        if (t) *t = tm;
+        return block_rc;
+    }
     *Cout = stack[0];
     tm.nnz = stack[0]->d.nnz;
     if (log) {
@@ -1477,6 +1593,56 @@ RMCM_API int32_t rmcm_run_metapath(rmcm_handle *h, rmcm_graph *g, const char *me
         mat_release(h, res);
     }
     return rc;
+}
+
+RMCM_API int32_t rmcm_run_metapath_blocks(rmcm_handle *h, rmcm_graph *g, const char *metapath,
+                                          int64_t rows_per_block, rmcm_block_fn fn, void *user, rmcm_timings *t) {
+    if (!h || !g || !metapath || !fn) return RMCM_EINVAL;
+    std::vector<int32_t> vts, ets;
+    if (parse_path(metapath, vts, ets) != RMCM_OK)
+        return set_error(h, RMCM_EINVAL, std::string("the meta-path is incorrect: ") + metapath);
+    const int len = (int)ets.size();
+    if (len < 1 || len > 16) return set_error(h, RMCM_EINVAL, "meta-path must have 1..16 edge types");
+    const int32_t vt = h->valtype == RMCM_VAL_U64 ? RMCM_VAL_U64 : RMCM_VAL_U32;
+    const bool widen = h->valtype == RMCM_VAL_AUTO;
+    std::vector<rmcm_mat *> mats(len);
+    for (int i = 0; i < len; i++) RMCM_TRY(get_leaf(h, g, vts[i], vts[i + 1], ets[i], vt, &mats[i]));
+    auto leaf64 = [&](int i, rmcm_mat **out) { return get_leaf(h, g, vts[i], vts[i + 1], ets[i], RMCM_VAL_U64, out); };
+    if (len == 1) {
+        // the leaf is the result: one block
+        rmcm_timings tm{};
+        tm.nnz = mats[0]->d.nnz;
+        tm.valtype = vt;
+        const int32_t urc = fn(user, 0, mats[0]);
+        if (t) *t = tm;
+        return urc == RMCM_OK ? RMCM_OK : set_error(h, urc, "the block sink stopped the chain");
+    }
+    BlockSink sink;
+    sink.rows_per_block = rows_per_block;
+    sink.fn = fn;
+    sink.user = user;
+    rmcm_mat *res = nullptr;
+    int32_t rc = chain_exec(h, mats.data(), len, nullptr, &res, t, widen, leaf64, nullptr, false, &sink);
+    if (res) mat_release(h, res);
+    return rc;
+}
+
+RMCM_API int32_t rmcm_mat_digest_rows(rmcm_handle *h, const rmcm_mat *m, int64_t row0, uint64_t *nnz,
+                                      uint64_t *digest) {
+    if (!h || !m || row0 < 0) return RMCM_EINVAL;
+    uint64_t *d = nullptr;
+    RMCM_TRY(dev_alloc(h, (void **)&d, 16));
+    int32_t rc = mat_digest_launch(h, m, d, row0);
+    if (rc == RMCM_OK) {
+        cudaError_t e = cudaMemcpyAsync(h->h_pinned, d, 16, cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) rc = cuda_error(h, e, "digest download");
+    }
+    dev_free(h, d, 16);
+    if (rc != RMCM_OK) return rc;
+    if (nnz) *nnz = (uint64_t)h->h_pinned[0];
+    if (digest) *digest = (uint64_t)h->h_pinned[1];
+    return RMCM_OK;
 }
 
 RMCM_API int32_t rmcm_set_order_mode(rmcm_handle *h, int32_t mode) {

@@ -115,10 +115,12 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
 }
 
 // out[0] = nnz (rowptr[rows]); out[1] += sum over entries (r, c, v) of
-// mix64(mix64(r * 2^32 + c) + v), mod 2^64.  The sum does not depend on the
-// entry order, so equal matrices give equal digests whatever the launch shape.
+// mix64(mix64(r * 2^32 + c) + v), mod 2^64, with r counted from row0 (a block
+// of rows of a larger matrix adds its share of that matrix's digest).  The sum
+// does not depend on the entry order, so equal matrices give equal digests
+// whatever the launch shape.
 template <typename V>
-__global__ void __launch_bounds__(256) k_digest(DevCsr C, unsigned long long *out) {
+__global__ void __launch_bounds__(256) k_digest(DevCsr C, unsigned long long *out, int64_t row0) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     uint64_t acc = 0;
@@ -126,7 +128,7 @@ __global__ void __launch_bounds__(256) k_digest(DevCsr C, unsigned long long *ou
     for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < C.rows; r += warps) {
         const int64_t e1 = C.rowptr[r + 1];
         for (int64_t e = C.rowptr[r] + lane; e < e1; e += 32) {
-            const uint64_t key = ((uint64_t)r << 32) | (uint32_t)C.col[e];
+            const uint64_t key = ((uint64_t)(r + row0) << 32) | (uint32_t)C.col[e];
             const uint64_t v = val ? (uint64_t)val[e] : 1ULL;
             acc += mix64(mix64(key) + v);
         }
@@ -206,15 +208,15 @@ bool copy_out_launch(const void *const *src, void *const *dst_host, const int64_
     return cudaGetLastError() == cudaSuccess;
 }
 
-int32_t mat_digest_launch(rmcm_handle *h, const rmcm_mat *m, uint64_t *out_dev) {
+int32_t mat_digest_launch(rmcm_handle *h, const rmcm_mat *m, uint64_t *out_dev, int64_t row0) {
     cudaStream_t s = h->stream;
     RMCM_CUDA(h, cudaMemsetAsync(out_dev, 0, 2 * sizeof(uint64_t), s));
     const int64_t want = (m->d.rows * 32 + 255) / 256;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)h->sm_count * 8));
     if (m->valtype == RMCM_VAL_U64)
-        k_digest<uint64_t><<<grid, 256, 0, s>>>(m->d, (unsigned long long *)out_dev);
+        k_digest<uint64_t><<<grid, 256, 0, s>>>(m->d, (unsigned long long *)out_dev, row0);
     else
-        k_digest<uint32_t><<<grid, 256, 0, s>>>(m->d, (unsigned long long *)out_dev);
+        k_digest<uint32_t><<<grid, 256, 0, s>>>(m->d, (unsigned long long *)out_dev, row0);
     h->launches++;
     RMCM_CUDA(h, cudaGetLastError());
     return RMCM_OK;

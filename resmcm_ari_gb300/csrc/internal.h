@@ -268,7 +268,13 @@ int32_t chain_plan(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, double *c
 
 // Launches a digest of m into out_dev[0..1] (nnz, order-free entry hash);
 // capture-safe.
-int32_t mat_digest_launch(rmcm_handle *h, const rmcm_mat *m, uint64_t *out_dev);
+int32_t mat_digest_launch(rmcm_handle *h, const rmcm_mat *m, uint64_t *out_dev, int64_t row0 = 0);
+// api.cpp: where the blocked final product of a chain delivers its blocks
+struct BlockSink {
+    int64_t rows_per_block = 0;     // 0: from the estimate and the free budget
+    rmcm_block_fn fn = nullptr;
+    void *user = nullptr;
+};
 int32_t chain_order_launch(rmcm_handle *h, const double *c_dev, int32_t len, double *c16, int32_t *split16,
                            double *cost16, int32_t *pairs32);
 
