@@ -284,29 +284,39 @@ def batched_section(rg, device, seed=2, scale=1 / 200, count=512, lanes=8, reps=
     return out
 
 
-def served_section(rg, eng, hg_retail, g_retail, rates=(100.0, 2000.0), queries=300, lanes=8):
-    """Poisson streams of meta-path queries (2-8 matrices) over two resident
-    graphs, the A/P/V graph and the retail graph, 50/50: plain one query at a
-    time versus the query server (admission against 64 GB)."""
+def served_section(rg, eng, hg_retail, g_retail, rates=(10.0, 100.0, 500.0, 2000.0), queries=60, lanes=8,
+                   span_s=6.0):
+    """Poisson streams of meta-path queries (2-8 matrices, seeded random
+    walks, no size filter) over two resident graphs, the A/P/V graph and the
+    retail graph, 50/50: plain one query at a time versus the query server
+    (admission of RES-predicted bytes against 64 GB; the plain path applies
+    the same rule).  At the low rates the stream is cut to ``span_s`` seconds
+    of arrivals."""
     from resmcm_ari_gb300 import serve, synth
+    budget = 64 << 30
     g0 = synth.dblp_like()
     hg0 = rg.HeteroGraph.from_synthetic(eng, g0)
-    cats = [serve.catalog(eng, hg0, g0, 24, seed=1, max_bytes=4e9),
-            serve.catalog(eng, hg_retail, g_retail, 24, seed=2, max_bytes=4e9)]
-    srv = rg.Server(eng, lanes=lanes, mem_budget_bytes=64 << 30)
+    cats = [serve.catalog(eng, hg0, g0, 24, seed=1), serve.catalog(eng, hg_retail, g_retail, 24, seed=2)]
+    graphs = [hg0, hg_retail]
+    admitted = [[serve.admits(eng, graphs[gi], mp, budget) for mp in cat] for gi, cat in enumerate(cats)]
+    srv = rg.Server(eng, lanes=lanes, mem_budget_bytes=budget)
     srv.add_graph(hg0)
     srv.add_graph(hg_retail)
-    out = {"workload": "Poisson arrivals, 2-8-matrix random-walk meta-paths (24 per graph, RES-predicted "
-                       "bytes <= 4 GB) over the A/P/V graph and the retail graph, 50/50",
-           "budget_bytes": 64 << 30, "lanes": lanes, "rates": []}
+    out = {"workload": "Poisson arrivals, 2-8-matrix seeded random-walk meta-paths (24 per graph, no size "
+                       "filter) over the A/P/V graph and the retail graph, 50/50; queries whose RES-predicted "
+                       "bytes exceed the 64 GB budget are rejected by both paths",
+           "budget_bytes": budget, "lanes": lanes,
+           "catalog_admitted": [int(sum(a)) for a in admitted], "catalog_size": [len(c) for c in cats],
+           "rates": []}
     for rate in rates:
-        stream = serve.poisson_stream(7, rate, queries, cats)
-        p = serve.run_plain(eng, [hg0, hg_retail], stream)
+        n = int(min(queries, max(20, rate * span_s)))
+        stream = serve.poisson_stream(7, rate, n, cats)
+        p = serve.run_plain(eng, graphs, stream, budget=budget)
         s_ = serve.run_served(srv, stream)
         same = all(s_["results"][i] == p["results"][i] for i in range(len(stream)))
-        out["rates"].append({"offered_qps": rate, "queries": queries,
-                             "plain": {k: p[k] for k in ("qps", "p50_ms", "p99_ms")},
-                             "served": {k: s_[k] for k in ("qps", "p50_ms", "p99_ms")},
+        out["rates"].append({"offered_qps": rate, "queries": n,
+                             "plain": {k: p[k] for k in ("qps", "p50_ms", "p99_ms", "rejected")},
+                             "served": {k: s_[k] for k in ("qps", "p50_ms", "p99_ms", "rejected")},
                              "qps_ratio": s_["qps"] / p["qps"], "identical_results": same})
     st = srv.stats()
     out["peak_reserved_bytes"] = st["peak_reserved"]
@@ -316,15 +326,62 @@ def served_section(rg, eng, hg_retail, g_retail, rates=(100.0, 2000.0), queries=
     return out
 
 
+def stress_plan(rg, device, g, mp, capacity):
+    """RES estimates, DP order and the memory plan of the stress chain on
+    graph g, from leaves built straight from the relations (no run)."""
+    from resmcm_ari_gb300 import workloads
+    eng = rg.Engine(device=device, valtype=rg.VAL_U64)
+    cache, leaves = {}, []
+    for rel, fw in workloads.STRESS_LEAVES:
+        if (rel, fw) not in cache:
+            rp, col = workloads.relation_csr(g, rel, fw)
+            r = g.relations[rel]
+            cols = g.type_sizes[r.dst_type if fw else r.src_type]
+            cache[(rel, fw)] = eng.upload(rp, col, cols=cols, valtype=rg.VAL_U64)
+        leaves.append(cache[(rel, fw)])
+    c = eng.estimate(leaves)
+    split, _, pairs = eng.order(c)
+    dims = [m.shape[0] for m in leaves] + [leaves[-1].shape[1]]
+    leaf_bytes = [m.nnz * 12 + (m.shape[0] + 1) * 8 for m in cache.values()]
+    plan = workloads.chain_plan(c, split, dims, leaf_bytes)
+    l2r = [float(c[0, j]) for j in range(1, c.shape[0])]
+    for m in cache.values():
+        m.free()
+    eng.close()
+    # the final product can run in blocks of rows (rmcm_run_metapath_blocks):
+    # then its output need not be whole, but its operands must be
+    fin = plan["products"][-1]
+    live_wo_final = max([n["live_bytes"] for n in plan["products"][:-1]] + [fin["live_bytes"] - fin["bytes"]])
+    return {"order_pairs": pairs.tolist(),
+            "products": [{k: (round(v) if isinstance(v, float) else v) for k, v in n.items()}
+                         for n in plan["products"]],
+            "largest_intermediate_est_nnz": plan["largest_intermediate_nnz"], "result_est_nnz": plan["result_nnz"],
+            "peak_live_bytes": plan["peak_live_bytes"], "peak_at_product": plan["peak_at"],
+            "peak_live_bytes_final_in_blocks": live_wo_final, "device_bytes": capacity,
+            "fits_whole": plan["peak_live_bytes"] <= capacity, "fits_final_in_blocks": live_wo_final <= capacity,
+            "left_to_right_largest_est_nnz": max(l2r)}
+
+
 def stress_section(rg, device, scale=0.1):
     """The twelve-matrix uint64 chain Z-Y-X-Y-X-Y-Z-Y-X-Y-X-Y-Z over the X/Y/Z
-    graph (both-side Zipf(1.6) X-Y degrees), vertex and edge counts x``scale``:
-    one timed run after the leaves are built."""
+    graph (both-side Zipf(1.6) X-Y degrees): at the configured size (X = Y =
+    5M, Z = 100k, 60M X-Y edges) its RES estimates and memory plan decide
+    whether it can run on this GPU at all; the chain is run, timed, at vertex
+    and edge counts x``scale``."""
+    import torch
     from resmcm_ari_gb300 import workloads
+    capacity = torch.cuda.mem_get_info(device)[1]
+    mp = workloads.STRESS_CHAIN
+    t0 = time.perf_counter()
+    full = workloads.stress_graph()
+    full_plan = stress_plan(rg, device, full, mp, capacity)
+    full_plan["seconds"] = time.perf_counter() - t0
+    full_plan["workload"] = (f"X=Y={full.type_sizes[0]}, Z={full.type_sizes[2]}, X-Y {full.relations[0].src.size} "
+                             f"edges, Y-Z {full.relations[1].src.size} edges")
+    del full
     g = workloads.stress_scaled(scale)
     eng = rg.Engine(device=device, valtype=rg.VAL_U64)
     hg = rg.HeteroGraph.from_synthetic(eng, g)
-    mp = workloads.STRESS_CHAIN
     leaves = hg.leaves(mp, rg.VAL_U64)
     c = eng.estimate(leaves)
     split, _, _ = eng.order(c)
@@ -348,7 +405,8 @@ def stress_section(rg, device, scale=0.1):
            "spgemm_s": t["spgemm_s"], "multiply_adds": int(t["flops"]),
            "multiply_adds_per_s": t["flops"] / t["total_s"] if t["total_s"] else None,
            "peak_device_bytes": int(peak),
-           "est_largest_intermediate_nnz": {"res_order": max(inter), "left_to_right": max(c[0, j] for j in range(1, L))}}
+           "est_largest_intermediate_nnz": {"res_order": max(inter), "left_to_right": max(c[0, j] for j in range(1, L))},
+           "configured_size_plan": full_plan}
     C.free()
     hg.close()
     eng.close()

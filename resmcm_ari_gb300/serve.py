@@ -35,9 +35,10 @@ def predicted_bytes(c: np.ndarray, split: np.ndarray, dims: list) -> float:
 
 
 def catalog(engine, hg, g: synth.SyntheticHIN, count: int, seed: int, lengths=(2, 8),
-            max_bytes: float = 2e9, max_tries: int = 20000) -> list:
+            max_bytes: float = float("inf"), max_tries: int = 20000) -> list:
     """``count`` distinct seeded random-walk meta-paths of ``g`` whose
-    predicted bytes stay within ``max_bytes`` (the estimator's own signal)."""
+    predicted bytes stay within ``max_bytes`` (the estimator's own signal;
+    no limit by default)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     out, seen, tries = [], set(), 0
     while len(out) < count and tries < max_tries:
@@ -92,18 +93,34 @@ def run_served(server, stream: list, lead_s: float = 0.05) -> dict:
     server.drain()
     for r in server.poll():
         results[r["tag"]] = r
+    from . import ENOMEM
     ok = [r for r in results.values() if r["status"] == OK]
     lat = [r["t_done"] - r["t_submit"] for r in ok]
     first = base + stream[0][0]
     last = max(r["t_done"] for r in results.values())
     out = _summary(lat, first, last, len(ok), len(stream))
+    out["rejected"] = sum(1 for r in results.values() if r["status"] == ENOMEM)
     out["results"] = {k: (r["status"], r["nnz"], r["digest"]) for k, r in results.items()}
     out["admission_wait_ms_p99"] = float(np.percentile([r["t_admit"] - r["t_submit"] for r in ok], 99) * 1e3) if ok else None
     return out
 
 
-def run_plain(engine, graphs: list, stream: list, lead_s: float = 0.05) -> dict:
-    """The same arrivals through rmcm_run_metapath, one query at a time."""
+def admits(engine, hg, mp: str, budget: float) -> bool:
+    """The server's admission rule for one query: its predicted bytes (RES
+    estimates of its DP order) fit the whole budget."""
+    leaves = hg.leaves(mp)
+    c = engine.estimate(leaves)
+    split, _, _ = engine.order(c)
+    dims = [m.shape[0] for m in leaves] + [leaves[-1].shape[1]]
+    return predicted_bytes(c, split, dims) <= budget
+
+
+def run_plain(engine, graphs: list, stream: list, lead_s: float = 0.05, budget: float = float("inf")) -> dict:
+    """The same arrivals through rmcm_run_metapath, one query at a time.  A
+    query the server's admission rule rejects against ``budget`` is rejected
+    here too (estimate and order only, like the server), so both paths run
+    the same work and give the same results."""
+    from . import ENOMEM
     results, lat = {}, []
     base = time.perf_counter() + lead_s
     last = base
@@ -113,10 +130,13 @@ def run_plain(engine, graphs: list, stream: list, lead_s: float = 0.05) -> dict:
         if now < arrival:
             time.sleep(arrival - now)
         try:
-            C, _, rc = engine.run_metapath(graphs[gi], mp, keep=True)
-            nnz, dig = engine.digest(C)
-            C.free()
-            results[i] = (rc, nnz, dig)
+            if not admits(engine, graphs[gi], mp, budget):
+                results[i] = (ENOMEM, 0, 0)
+            else:
+                C, _, rc = engine.run_metapath(graphs[gi], mp, keep=True)
+                nnz, dig = engine.digest(C)
+                C.free()
+                results[i] = (rc, nnz, dig)
         except Exception as e:  # an error is that query's result
             results[i] = (getattr(e, "status", -1), 0, 0)
         last = time.perf_counter()
@@ -125,4 +145,5 @@ def run_plain(engine, graphs: list, stream: list, lead_s: float = 0.05) -> dict:
     n_ok = sum(1 for r in results.values() if r[0] == OK)
     out = _summary(lat, base + stream[0][0], last, n_ok, len(stream))
     out["results"] = results
+    out["rejected"] = sum(1 for r in results.values() if r[0] == ENOMEM)
     return out

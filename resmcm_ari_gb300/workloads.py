@@ -124,3 +124,63 @@ def stress_scaled(scale: float, seed: int = 4) -> synth.SyntheticHIN:
     """The stress graph with every vertex and edge count multiplied by ``scale``."""
     return stress_graph(seed=seed, n_x=max(2, int(5_000_000 * scale)), n_y=max(2, int(5_000_000 * scale)),
                         n_z=max(2, int(100_000 * scale)), xy_edges=max(1, int(60_000_000 * scale)))
+
+
+def relation_csr(g: synth.SyntheticHIN, rel: int, forward: bool = True):
+    """CSR (rowptr int64, col int32) of one direction of a relation in local
+    ids, rows sorted by column: the leaf matrix of that edge type, built
+    without the graph's text-order adjacency (fast at tens of millions of
+    edges)."""
+    r = g.relations[rel]
+    src, dst = (r.src, r.dst) if forward else (r.dst, r.src)
+    nrows = g.type_sizes[r.src_type if forward else r.dst_type]
+    key = src.astype(np.int64) * np.int64(1 << 32) + dst.astype(np.int64)
+    key = np.sort(key)
+    rows = (key >> 32).astype(np.int64)
+    col = (key & 0xFFFFFFFF).astype(np.int32)
+    rowptr = np.zeros(nrows + 1, np.int64)
+    np.cumsum(np.bincount(rows, minlength=nrows), out=rowptr[1:])
+    return rowptr, col
+
+
+# leaves of the stress chain Z-Y-X-Y-X-Y-Z-Y-X-Y-X-Y-Z: (relation, forward)
+# per position; relation 0 is X-Y, 1 is Y-Z
+STRESS_LEAVES = [(1, False), (0, False), (0, True), (0, False), (0, True), (1, True),
+                 (1, False), (0, False), (0, True), (0, False), (0, True), (1, True)]
+
+
+def chain_plan(c: np.ndarray, split: np.ndarray, dims: list, leaf_bytes: list, val_bytes: int = 8) -> dict:
+    """Device bytes of a chain's products in a given order, from the RES
+    estimates: every product (i, j) of the split tree at (4 + val_bytes)
+    bytes per estimated entry plus 8 per row pointer, and the live set of the
+    executor's stack machine (free after use, as efficient/resmcm.cpp:702-760)
+    while each product runs: resident leaves, the intermediates on the stack
+    and the product's output."""
+    L = c.shape[0]
+    per = 4 + val_bytes
+
+    def nbytes(i, j):
+        return per * float(c[i, j]) + 8.0 * (dims[i] + 1)
+
+    nodes, peak = [], [0.0, None]
+    resident = float(sum(leaf_bytes))
+
+    def run(i, j, held):
+        # returns the bytes of (i, j)'s result; `held` = bytes live outside it
+        if i == j:
+            return 0.0
+        k = int(split[i, j])
+        left = run(i, k, held)
+        right = run(k + 1, j, held + left)
+        out = nbytes(i, j)
+        live = resident + held + left + right + out
+        nodes.append({"i": i, "j": j, "est_nnz": float(c[i, j]), "bytes": out, "live_bytes": live})
+        if live > peak[0]:
+            peak[0], peak[1] = live, (i, j)
+        return out
+
+    run(0, L - 1, 0.0)
+    return {"products": nodes, "peak_live_bytes": peak[0], "peak_at": peak[1],
+            "largest_intermediate_nnz": max((n["est_nnz"] for n in nodes if (n["i"], n["j"]) != (0, L - 1)),
+                                            default=0.0),
+            "result_nnz": float(c[0, L - 1])}
