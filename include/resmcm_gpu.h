@@ -337,6 +337,16 @@ RMCM_API int32_t rmcm_batch_create(rmcm_handle *h, rmcm_graph *g, const char *co
                                    int32_t count, int32_t lanes, rmcm_batch **out);
 /* nnz_out[count], digest_out[count] may be NULL; seconds = device time of
  * the graph launch (CUDA events on the handle's stream). */
+/* The same batch in fused launches: the estimator levels of every chain
+ * (one launch per level step over all chains), the DP of every chain (one
+ * launch), then "waves": wave w multiplies the w-th product of every chain
+ * that has one as ONE SpGEMM of block-diagonal operands (the chains' left
+ * operands stacked, their columns shifted onto their chains' stacked right
+ * operands).  Recorded once, captured as one CUDA graph; rmcm_batch_run,
+ * _info (lanes = 1) and _free apply.  Replaces the per-path loop of main
+ * (efficient/resmcm.cpp:834-889); results equal rmcm_run_metapath's. */
+RMCM_API int32_t rmcm_batch_create_fused(rmcm_handle *h, rmcm_graph *g, const char *const *metapaths,
+                                         int32_t count, rmcm_batch **out);
 RMCM_API int32_t rmcm_batch_run(rmcm_handle *h, rmcm_batch *b, int64_t *nnz_out, uint64_t *digest_out,
                                 double *seconds);
 RMCM_API int32_t rmcm_batch_info(const rmcm_batch *b, int32_t *count, int32_t *lanes,

@@ -168,6 +168,7 @@ def lib():
         "rmcm_graph_global_ids": ([vp, i32, vp], i32),
         "rmcm_mat_save": ([vp, vp, C.c_char_p], i32),
         "rmcm_batch_create": ([vp, vp, vp, i32, i32, pp], i32),
+        "rmcm_batch_create_fused": ([vp, vp, vp, i32, pp], i32),
         "rmcm_batch_run": ([vp, vp, vp, vp, f64p], i32),
         "rmcm_batch_info": ([vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)], i32),
         "rmcm_batch_free": ([vp, vp], i32),
@@ -425,11 +426,17 @@ def csr_digest(rowptr, col, val=None) -> tuple:
 class Batch:
     """Meta-paths recorded once and replayed as one CUDA graph (rmcm_batch_*)."""
 
-    def __init__(self, engine: "Engine", graph: "HeteroGraph", paths: list, lanes: int = 8):
+    def __init__(self, engine: "Engine", graph: "HeteroGraph", paths: list, lanes: int = 8, fused: bool = False):
+        """fused: rmcm_batch_create_fused (estimator levels, DP and one
+        block-diagonal SpGEMM per wave shared by every chain); else
+        rmcm_batch_create (every chain's own launches over ``lanes`` streams)."""
         self.engine, self.graph, self.paths = engine, graph, list(paths)
         arr = (C.c_char_p * len(self.paths))(*[p.encode() for p in self.paths])
         h = C.c_void_p()
-        engine._check(lib().rmcm_batch_create(engine._h, graph._h, arr, len(self.paths), lanes, C.byref(h)))
+        if fused:
+            engine._check(lib().rmcm_batch_create_fused(engine._h, graph._h, arr, len(self.paths), C.byref(h)))
+        else:
+            engine._check(lib().rmcm_batch_create(engine._h, graph._h, arr, len(self.paths), lanes, C.byref(h)))
         self._h = h
 
     def run(self):
@@ -676,8 +683,8 @@ class Engine:
                    int(cur["gemm_min_mflops"]))
         self._check(lib().rmcm_set_tuning(self._h, C.byref(t)))
 
-    def batch(self, graph: HeteroGraph, paths: list, lanes: int = 8) -> Batch:
-        return Batch(self, graph, paths, lanes)
+    def batch(self, graph: HeteroGraph, paths: list, lanes: int = 8, fused: bool = False) -> Batch:
+        return Batch(self, graph, paths, lanes, fused)
 
     def download_async(self, m: Matrix, rowptr_ptr: int, col_ptr: int, val_ptr: int = 0):
         """rmcm_mat_download_async into caller-owned (pinned) host buffers;

@@ -1779,12 +1779,14 @@ struct rmcm_batch {
     int64_t launches_per_run = 0;
     int64_t nodes = 0;
     int64_t runs = 0;
+    rmcm::FusedBatch *fused = nullptr;      // rmcm_batch_create_fused: everything lives here
 };
 
 namespace {
 
 void batch_release(rmcm_batch *b) {
     rmcm_handle *h = b->h;
+    if (b->fused) fused_free(h, b->fused);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     for (auto e : b->fork_join)
@@ -1901,6 +1903,29 @@ RMCM_API int32_t rmcm_get_tuning(const rmcm_handle *h, rmcm_tuning *t) {
     return RMCM_OK;
 }
 
+RMCM_API int32_t rmcm_batch_create_fused(rmcm_handle *h, rmcm_graph *g, const char *const *metapaths, int32_t count,
+                                         rmcm_batch **out) {
+    if (!h || !g || !metapaths || count < 1 || !out) return RMCM_EINVAL;
+    *out = nullptr;
+    if (g->h != h) return set_error(h, RMCM_EINVAL, "batch: the graph belongs to another handle");
+    if (h->order_mode != RMCM_ORDER_RES) return set_error(h, RMCM_EINVAL, "batch: only the RES order is batched");
+    rmcm_batch *b = new rmcm_batch();
+    b->h = h;
+    b->g = g;
+    g->batches++;
+    h->batches.insert(b);
+    for (int32_t i = 0; i < count; i++) b->paths.emplace_back(metapaths[i] ? metapaths[i] : "");
+    int32_t rc = fused_create(h, g, metapaths, count, &b->fused);
+    if (rc != RMCM_OK) {
+        const std::string why = h->last_error;
+        batch_release(b);
+        h->last_error = why;
+        return rc;
+    }
+    *out = b;
+    return RMCM_OK;
+}
+
 RMCM_API int32_t rmcm_batch_create(rmcm_handle *h, rmcm_graph *g, const char *const *metapaths, int32_t count,
                                    int32_t lanes, rmcm_batch **out) {
     if (!h || !g || !metapaths || count < 1 || !out) return RMCM_EINVAL;
@@ -2008,7 +2033,12 @@ RMCM_API int32_t rmcm_batch_create(rmcm_handle *h, rmcm_graph *g, const char *co
 
 RMCM_API int32_t rmcm_batch_run(rmcm_handle *h, rmcm_batch *b, int64_t *nnz_out, uint64_t *digest_out,
                                 double *seconds) {
-    if (!h || !b || b->h != h || !b->exec) return RMCM_EINVAL;
+    if (!h || !b || b->h != h) return RMCM_EINVAL;
+    if (b->fused) {
+        b->runs++;
+        return fused_run(h, b->fused, nnz_out, digest_out, seconds);
+    }
+    if (!b->exec) return RMCM_EINVAL;
     cudaEvent_t *ev = h->ev;
     RMCM_CUDA(h, cudaEventRecord(ev[6], h->stream));
     RMCM_CUDA(h, cudaGraphLaunch(b->exec, h->stream));
@@ -2036,6 +2066,11 @@ RMCM_API int32_t rmcm_batch_run(rmcm_handle *h, rmcm_batch *b, int64_t *nnz_out,
 RMCM_API int32_t rmcm_batch_info(const rmcm_batch *b, int32_t *count, int32_t *lanes, int64_t *launches_per_run,
                                  int64_t *graph_nodes) {
     if (!b) return RMCM_EINVAL;
+    if (b->fused) {
+        fused_info(b->fused, count, launches_per_run, graph_nodes);
+        if (lanes) *lanes = 1;
+        return RMCM_OK;
+    }
     if (count) *count = (int32_t)b->paths.size();
     if (lanes) *lanes = (int32_t)b->lanes.size();
     if (launches_per_run) *launches_per_run = b->launches_per_run;

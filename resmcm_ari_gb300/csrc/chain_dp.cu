@@ -138,6 +138,28 @@ __global__ void __launch_bounds__(256) k_digest(DevCsr C, unsigned long long *ou
     if (blockIdx.x == 0 && threadIdx.x == 0) out[0] = (unsigned long long)C.rowptr[C.rows];
 }
 
+// Digests of many row views in one launch: blockIdx.y picks the view.
+// out[2 o] = the view's nnz, out[2 o + 1] += its entries' hash sum (rows
+// counted from the view's first row); out must start zeroed.
+__global__ void __launch_bounds__(256) k_digest_multi(const DigestJob *jobs, unsigned long long *out) {
+    const DigestJob jb = jobs[blockIdx.y];
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    uint64_t acc = 0;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < jb.rows; r += warps) {
+        const int64_t e1 = jb.rowptr[r + 1];
+        for (int64_t e = jb.rowptr[r] + lane; e < e1; e += 32) {
+            const uint64_t key = ((uint64_t)r << 32) | (uint32_t)jb.col[e];
+            uint64_t v = 1ULL;
+            if (jb.val) v = jb.vbytes == 8 ? ((const uint64_t *)jb.val)[e] : (uint64_t)((const uint32_t *)jb.val)[e];
+            acc += mix64(mix64(key) + v);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0 && acc) atomicAdd(out + 2 * jb.out + 1, (unsigned long long)acc);
+    if (blockIdx.x == 0 && threadIdx.x == 0) out[2 * jb.out] = (unsigned long long)(jb.rowptr[jb.rows] - jb.rowptr[0]);
+}
+
 }  // namespace
 
 namespace {
@@ -206,6 +228,24 @@ bool copy_out_launch(const void *const *src, void *const *dst_host, const int64_
     }
     k_copy_out<<<16, 512, 0, s>>>(r[0], r[1], r[2]);
     return cudaGetLastError() == cudaSuccess;
+}
+
+int32_t digest_multi_launch(rmcm_handle *h, const DigestJob *jobs_dev, int32_t njobs, uint64_t *out_dev) {
+    if (njobs <= 0) return RMCM_OK;
+    if (njobs > 65535) return set_error(h, RMCM_EINVAL, "digest: too many views");
+    k_digest_multi<<<dim3(16, (unsigned)njobs), 256, 0, h->stream>>>(jobs_dev, (unsigned long long *)out_dev);
+    h->launches++;
+    RMCM_CUDA(h, cudaGetLastError());
+    return RMCM_OK;
+}
+
+int32_t chain_order_multi(rmcm_handle *h, const double *c_all, const int32_t *lens_dev, int32_t n, int32_t *split_all,
+                          double *cost_all, int32_t *pairs_all) {
+    if (n <= 0) return RMCM_OK;
+    k_chain_dp<<<(unsigned)n, 32, 0, h->stream>>>(c_all, lens_dev, n, split_all, cost_all, pairs_all, 0);
+    h->launches++;
+    RMCM_CUDA(h, cudaGetLastError());
+    return RMCM_OK;
 }
 
 int32_t mat_digest_launch(rmcm_handle *h, const rmcm_mat *m, uint64_t *out_dev, int64_t row0) {

@@ -92,8 +92,12 @@ inline int32_t level_tile(int64_t rows, int64_t blocks_cap) {
     return t;
 }
 
-__global__ void __launch_bounds__(kEstThreads) k_res_level(DevCsr M, const double *q_next, double *q_cur,
-                                                           LevelArgs la, double *partial, bool skip_long) {
+// One level of one chain, as CTA `bid` of `nblk` (the same work split and
+// summation order whether the CTA belongs to a one-chain launch or to a
+// launch over many chains).
+__device__ __forceinline__ void res_level_body(const DevCsr &M, const double *q_next, double *q_cur,
+                                               const LevelArgs &la, double *partial, bool skip_long, int64_t bid,
+                                               int64_t nblk) {
     __shared__ double s_tp[kEstThreads / 32][32 * kMaxLen];   // tile products: [t * jp + jo]
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int G = 32 / la.jp;
@@ -105,9 +109,8 @@ __global__ void __launch_bounds__(kEstThreads) k_res_level(DevCsr M, const doubl
     double term_sum = 0.0;                       // this lane's rows of target j
     const int T = la.tile;                       // rows per warp step (1 .. 32)
     double *tp = s_tp[warp];
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t t0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * T; t0 < M.rows;
-         t0 += nwarps * T) {
+    const int64_t nwarps = (nblk * blockDim.x) >> 5;
+    for (int64_t t0 = ((bid * blockDim.x + threadIdx.x) >> 5) * T; t0 < M.rows; t0 += nwarps * T) {
         // r_ii of the tile's rows, a lane each (one division for T rows)
         int64_t my_a0 = 0, my_len = 0;
         if (lane < T && t0 + lane < M.rows) {
@@ -160,8 +163,13 @@ __global__ void __launch_bounds__(kEstThreads) k_res_level(DevCsr M, const doubl
     if (threadIdx.x < la.nj) {
         double acc = 0.0;
         for (int w = 0; w < kEstThreads / 32; w++) acc = __dadd_rn(acc, s_part[w][threadIdx.x]);
-        partial[(int64_t)blockIdx.x * kMaxLen + threadIdx.x] = acc;
+        partial[bid * kMaxLen + threadIdx.x] = acc;
     }
+}
+
+__global__ void __launch_bounds__(kEstThreads) k_res_level(DevCsr M, const double *q_next, double *q_cur,
+                                                           LevelArgs la, double *partial, bool skip_long) {
+    res_level_body(M, q_next, q_cur, la, partial, skip_long, blockIdx.x, gridDim.x);
 }
 
 // A CTA per long row (rows listed ascending): warp w multiplies the factors
@@ -171,9 +179,9 @@ __global__ void __launch_bounds__(kEstThreads) k_res_level(DevCsr M, const doubl
 // reduction still adds them in a fixed order.
 constexpr int kEstLongThreads = 1024;
 
-__global__ void __launch_bounds__(kEstLongThreads) k_res_long(DevCsr M, const double *q_next, double *q_cur,
-                                                              LevelArgs la, const int32_t *long_rows,
-                                                              double *partial) {
+__device__ __forceinline__ void res_long_body(const DevCsr &M, const double *q_next, double *q_cur,
+                                              const LevelArgs &la, const int32_t *long_rows, double *partial,
+                                              int64_t bid) {
     __shared__ double s_prod[kEstLongThreads / 32][kMaxLen];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int G = 32 / la.jp;
@@ -181,7 +189,7 @@ __global__ void __launch_bounds__(kEstLongThreads) k_res_long(DevCsr M, const do
     const int jo = lane % la.jp;
     const bool active_j = jo < la.nj && g < G;
     const int j = la.i + 1 + jo;
-    const int64_t u = long_rows[blockIdx.x];
+    const int64_t u = long_rows[bid];
     const int64_t a0 = M.rowptr[u], len = M.rowptr[u + 1] - a0;
     const int64_t k0 = a0 + len * warp / (kEstLongThreads / 32), k1 = a0 + len * (warp + 1) / (kEstLongThreads / 32);
     double prod = 1.0;
@@ -198,12 +206,18 @@ __global__ void __launch_bounds__(kEstLongThreads) k_res_long(DevCsr M, const do
         const int jj = la.i + 1 + threadIdx.x;
         const double sv = __dsub_rn(1.0, p);
         q_cur[u * la.len + jj] = __dsub_rn(1.0, sv);   // q = 1 - r for the next level
-        partial[(int64_t)blockIdx.x * kMaxLen + threadIdx.x] = __dmul_rn(sv, la.dims[jj]);
+        partial[bid * kMaxLen + threadIdx.x] = __dmul_rn(sv, la.dims[jj]);
     }
 }
 
+__global__ void __launch_bounds__(kEstLongThreads) k_res_long(DevCsr M, const double *q_next, double *q_cur,
+                                                              LevelArgs la, const int32_t *long_rows,
+                                                              double *partial) {
+    res_long_body(M, q_next, q_cur, la, long_rows, partial, blockIdx.x);
+}
+
 // One block: c[i*len + j] = sum over blocks (fixed pairwise order).
-__global__ void __launch_bounds__(256) k_res_reduce(const double *partial, int32_t nblocks, LevelArgs la, double *c) {
+__device__ __forceinline__ void res_reduce_body(const double *partial, int32_t nblocks, const LevelArgs &la, double *c) {
     __shared__ double s[256];
     for (int jo = 0; jo < la.nj; jo++) {
         double acc = 0.0;
@@ -217,6 +231,54 @@ __global__ void __launch_bounds__(256) k_res_reduce(const double *partial, int32
         if (threadIdx.x == 0) c[la.i * la.len + la.i + 1 + jo] = s[0];
         __syncthreads();
     }
+}
+
+__global__ void __launch_bounds__(256) k_res_reduce(const double *partial, int32_t nblocks, LevelArgs la, double *c) {
+    res_reduce_body(partial, nblocks, la, c);
+}
+
+// Many chains at once: job j is one level of one chain, exactly the launch
+// the one-chain estimator makes for it (its CTAs are blocks first .. first +
+// blocks - 1 of this grid), so every chain's estimates are bit-identical to
+// rmcm_estimate's.
+struct LevelJob {
+    DevCsr M;
+    const double *q_next;
+    double *q_cur;
+    double *partial;
+    double *c;                  // the chain's len x len estimates
+    const int32_t *long_rows;   // rows with a CTA of their own (nlong of them)
+    LevelArgs la;
+    int64_t first, blocks;      // CTAs of the level launch
+    int64_t lfirst;             // CTAs of the long-row launch: lfirst .. lfirst + nlong - 1
+    int32_t nlong;
+};
+
+__device__ __forceinline__ int find_job(const LevelJob *jobs, int njobs, int64_t b, bool longs) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((longs ? jobs[mid].lfirst : jobs[mid].first) <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(kEstThreads) k_res_level_multi(const LevelJob *jobs, int32_t njobs) {
+    const LevelJob &jb = jobs[find_job(jobs, njobs, blockIdx.x, false)];
+    res_level_body(jb.M, jb.q_next, jb.q_cur, jb.la, jb.partial, jb.nlong > 0, (int64_t)blockIdx.x - jb.first,
+                   jb.blocks);
+}
+
+__global__ void __launch_bounds__(kEstLongThreads) k_res_long_multi(const LevelJob *jobs, int32_t njobs) {
+    const LevelJob &jb = jobs[find_job(jobs, njobs, blockIdx.x, true)];
+    res_long_body(jb.M, jb.q_next, jb.q_cur, jb.la, jb.long_rows, jb.partial + jb.blocks * kMaxLen,
+                  (int64_t)blockIdx.x - jb.lfirst);
+}
+
+__global__ void __launch_bounds__(256) k_res_reduce_multi(const LevelJob *jobs) {
+    const LevelJob &jb = jobs[blockIdx.x];
+    if (jb.la.nj > 0) res_reduce_body(jb.partial, (int32_t)(jb.blocks + jb.nlong), jb.la, jb.c);
 }
 
 }  // namespace
@@ -280,6 +342,97 @@ int32_t estimate(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, double *c_
     return RMCM_OK;
 }
 
+
+// Estimates of many chains, a launch per level step over all of them: step s
+// runs level len_c - 1 - s of every chain c longer than s.  Job tables go to
+// the device through the arena (persistent pinned host memory and device
+// memory, so that a stream capture records copies that stay valid).
+int32_t estimate_multi(rmcm_handle *h, const EstChain *chains, int32_t n, TableArena &arena) {
+    cudaStream_t s = h->stream;
+    const int64_t blocks_cap = (int64_t)h->sm_count * 8;
+    auto al = [](int64_t x) { return (x + 255) & ~255LL; };
+    int32_t max_len = 0;
+    std::vector<int64_t> off(n + 1, 0);
+    for (int32_t c = 0; c < n; c++) {
+        const int32_t len = chains[c].len;
+        if (len < 1 || len > kMaxLen) return set_error(h, RMCM_EINVAL, "estimate: chain length must be 1..16");
+        max_len = std::max(max_len, len);
+        int64_t max_rows = 1, long_cap = 0;
+        for (int i = 0; i < len; i++) {
+            max_rows = std::max(max_rows, chains[c].mats[i]->d.rows);
+            long_cap = std::max<int64_t>(long_cap, chains[c].mats[i]->n_est_long);
+        }
+        off[c + 1] = off[c] + 2 * al(8 * max_rows * len) + al(8 * (blocks_cap + long_cap) * kMaxLen);
+    }
+    char *buf = nullptr;
+    RMCM_TRY(dev_alloc(h, (void **)&buf, std::max<int64_t>(off[n], 256)));
+    cudaError_t e = cudaSuccess;
+    for (int32_t c = 0; c < n && e == cudaSuccess; c++)
+        e = cudaMemsetAsync(chains[c].c_dev, 0, sizeof(double) * chains[c].len * chains[c].len, s);
+    std::vector<LevelJob> jobs;
+    for (int32_t st = 0; st < max_len && e == cudaSuccess; st++) {
+        jobs.clear();
+        int64_t nb = 0, nl = 0;
+        for (int32_t c = 0; c < n; c++) {
+            const int32_t len = chains[c].len;
+            if (st >= len) continue;
+            const int i = len - 1 - st;
+            int64_t max_rows = 1;
+            for (int q = 0; q < len; q++) max_rows = std::max(max_rows, chains[c].mats[q]->d.rows);
+            const int64_t rbytes = al(8 * max_rows * len);
+            // the one-chain estimator swaps its two level buffers every level
+            double *ra = (double *)(buf + off[c]), *rb = (double *)(buf + off[c] + rbytes);
+            double *r_cur = (st % 2 == 0) ? ra : rb, *r_next = (st % 2 == 0) ? rb : ra;
+            const rmcm_mat *Mi = chains[c].mats[i];
+            LevelJob jb{};
+            jb.M = Mi->d;
+            jb.q_next = r_next;
+            jb.q_cur = r_cur;
+            jb.partial = (double *)(buf + off[c] + 2 * rbytes);
+            jb.c = chains[c].c_dev;
+            jb.la.len = len;
+            jb.la.i = i;
+            jb.la.nj = len - 1 - i;
+            int jp = 1;
+            while (jp < jb.la.nj) jp <<= 1;
+            jb.la.jp = jp;
+            jb.la.dim_leaf = (double)Mi->d.cols;
+            for (int q = 0; q < len; q++) jb.la.dims[q] = (double)chains[c].mats[q]->d.cols;
+            jb.la.tile = level_tile(Mi->d.rows, blocks_cap);
+            int64_t blocks = (Mi->d.rows + (int64_t)jb.la.tile * (kEstThreads / 32) - 1) /
+                             ((int64_t)jb.la.tile * (kEstThreads / 32));
+            jb.blocks = std::max<int64_t>(1, std::min(blocks, blocks_cap));
+            jb.nlong = jb.la.nj > 0 && Mi->n_est_long > 0 ? Mi->n_est_long : 0;
+            jb.long_rows = Mi->est_long;
+            jb.first = nb;
+            jb.lfirst = nl;
+            nb += jb.blocks;
+            nl += jb.nlong;
+            jobs.push_back(jb);
+        }
+        void *hp = nullptr, *dp = nullptr;
+        const int64_t tbytes = (int64_t)sizeof(LevelJob) * (int64_t)jobs.size();
+        if (!arena.push(tbytes, &hp, &dp)) {
+            dev_free(h, buf, std::max<int64_t>(off[n], 256));
+            return set_error(h, RMCM_EINTERNAL, "estimate: job table arena full");
+        }
+        memcpy(hp, jobs.data(), tbytes);
+        e = cudaMemcpyAsync(dp, hp, tbytes, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) break;
+        k_res_level_multi<<<(unsigned)nb, kEstThreads, 0, s>>>((const LevelJob *)dp, (int32_t)jobs.size());
+        h->launches++;
+        if (nl > 0) {
+            k_res_long_multi<<<(unsigned)nl, kEstLongThreads, 0, s>>>((const LevelJob *)dp, (int32_t)jobs.size());
+            h->launches++;
+        }
+        k_res_reduce_multi<<<(unsigned)jobs.size(), 256, 0, s>>>((const LevelJob *)dp);
+        h->launches++;
+        e = cudaGetLastError();
+    }
+    dev_free(h, buf, std::max<int64_t>(off[n], 256));
+    if (e != cudaSuccess) return cuda_error(h, e, "multi-chain estimator launch");
+    return RMCM_OK;
+}
 
 // ---------------------------------------------------------------------------
 // RES estimator for callers that cannot allocate device memory

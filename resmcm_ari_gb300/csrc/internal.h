@@ -246,6 +246,31 @@ int32_t tc_seed_gemm(rmcm_handle *h, const void *Ad, const void *BdT, int64_t M,
                      int *err_dev);
 // estimator.cu: c_dev[len*len] on the device
 int32_t estimate(rmcm_handle *h, rmcm_mat *const *chain, int32_t len, double *c_dev);
+// Persistent pinned host memory mirrored by device memory, for small tables
+// that kernels read: filled on the host, copied with cudaMemcpyAsync (under
+// stream capture the copy node reads the pinned memory at every replay, so
+// the table must stay untouched after it is captured).
+struct TableArena {
+    char *host = nullptr;
+    char *dev = nullptr;
+    int64_t cap = 0, used = 0;
+    bool push(int64_t bytes, void **hp, void **dp) {
+        const int64_t b = (bytes + 255) & ~255LL;
+        if (used + b > cap) return false;
+        *hp = host + used;
+        *dp = dev + used;
+        used += b;
+        return true;
+    }
+};
+// estimator.cu: the estimates of many chains, one launch per level step over
+// all of them, each chain bit-identical to estimate()
+struct EstChain {
+    rmcm_mat *const *mats = nullptr;
+    int32_t len = 0;
+    double *c_dev = nullptr;     // len x len
+};
+int32_t estimate_multi(rmcm_handle *h, const EstChain *chains, int32_t n, TableArena &arena);
 // chain_dp.cu: split/cost/pairs on the device
 int32_t chain_order_dev(rmcm_handle *h, const double *c_dev, int32_t len, int32_t *split_dev, double *cost_dev,
                         int32_t *pairs_dev);
@@ -277,5 +302,26 @@ struct BlockSink {
 };
 int32_t chain_order_launch(rmcm_handle *h, const double *c_dev, int32_t len, double *c16, int32_t *split16,
                            double *cost16, int32_t *pairs32);
+// chain_dp.cu: the DP of n chains in one launch (c_all, split_all, cost_all:
+// 16 x 16 per chain holding its len x len compactly; pairs_all: 32 per chain)
+int32_t chain_order_multi(rmcm_handle *h, const double *c_all, const int32_t *lens_dev, int32_t n, int32_t *split_all,
+                          double *cost_all, int32_t *pairs_all);
+// A row view (rows row pointers from rowptr[0], entries at their positions)
+// whose digest goes to out[2 out .. 2 out + 1].
+struct DigestJob {
+    const int64_t *rowptr = nullptr;
+    const int32_t *col = nullptr;
+    const void *val = nullptr;
+    int64_t rows = 0;
+    int32_t vbytes = 4;
+    int32_t out = 0;
+};
+int32_t digest_multi_launch(rmcm_handle *h, const DigestJob *jobs_dev, int32_t njobs, uint64_t *out_dev);
+// batch_fused.cu: many chains as block-diagonal waves (see that file)
+struct FusedBatch;
+int32_t fused_create(rmcm_handle *h, rmcm_graph *g, const char *const *paths, int32_t count, FusedBatch **out);
+int32_t fused_run(rmcm_handle *h, FusedBatch *b, int64_t *nnz_out, uint64_t *digest_out, double *seconds);
+void fused_info(const FusedBatch *b, int32_t *count, int64_t *launches_per_run, int64_t *nodes);
+void fused_free(rmcm_handle *h, FusedBatch *b);
 
 }  // namespace rmcm

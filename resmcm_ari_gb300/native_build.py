@@ -29,7 +29,7 @@ CLI = os.path.join(BUILD, "resmcm_gpu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUDA_HOME, "bin", "nvcc")) else "nvcc"
-CU_SOURCES = ["spgemm.cu", "estimator.cu", "chain_dp.cu", "dense_gemm.cu", "tc_gemm.cu"]
+CU_SOURCES = ["spgemm.cu", "estimator.cu", "chain_dp.cu", "dense_gemm.cu", "tc_gemm.cu", "batch_fused.cu"]
 CPP_SOURCES = ["api.cpp", "server.cpp"]
 HEADERS = ["internal.h"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",

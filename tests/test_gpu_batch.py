@@ -88,6 +88,70 @@ def test_batch_on_random_walks_of_a_five_type_graph(native):
     eng.close()
 
 
+def _fused_equals_plain(native, eng, hg, paths, reps=3):
+    plain = _plain_digests(native, eng, hg, paths)
+    b = eng.batch(hg, paths, fused=True)
+    info = b.info()
+    assert info["count"] == len(paths) and info["lanes"] == 1 and info["launches_per_run"] > 0
+    for _ in range(reps):                                # the graph replays identically
+        nnz, dig, sec = b.run()
+        assert sec > 0
+        assert [(int(n), int(x)) for n, x in zip(nnz, dig)] == plain
+    b.free()
+    return info
+
+
+def test_fused_batch_equals_plain_and_oracle(native, oracle_mod):
+    """Estimator levels, DP and one block-diagonal SpGEMM per wave shared by
+    every chain: every result equals rmcm_run_metapath's and the counting
+    oracle's, in far fewer launches than one chain at a time."""
+    fx = load_fixture("hin4_small")
+    g = make_graph(fx)
+    paths = [r["metapath"] for r in fx["paths"]]
+    eng = native.Engine(device=0)
+    hg = native.HeteroGraph.from_synthetic(eng, g)
+    og = oracle_mod.OracleGraph.from_synthetic(g)
+    for mp in paths:
+        r = og.chain(mp, mode=oracle_mod.MODE_COUNT, threads=4)
+        C, _, _ = eng.run_metapath(hg, mp)
+        assert csr_digest(r.rowptr, r.col, r.val) == eng.digest(C), mp
+        C.free()
+    og.close()
+    info = _fused_equals_plain(native, eng, hg, paths)
+    per_chain = eng.batch(hg, paths, lanes=1)
+    assert info["launches_per_run"] * 3 < per_chain.info()["launches_per_run"]
+    per_chain.free()
+    hg.close()
+    eng.close()
+
+
+def test_fused_batch_with_uint64_escalation_and_single_matrix_paths(native):
+    """K(64,64): long paths overflow uint32; the wave that overflows widens
+    the whole batch to uint64 in the record, and the replay repeats it."""
+    n = 64
+    src = np.repeat(np.arange(n), n)
+    dst = np.tile(np.arange(n), n)
+    g = synth.SyntheticHIN("k64", [n, n], [synth.Relation(0, 1, 0, 1, src, dst)])
+    paths = ["0-0-1", "0-0-1-1-0", "0-0-1-1-0-0-1-1-0-0-1-1-0-0-1-1-0", "1-1-0-0-1-1-0-0-1-1-0", "1-1-0"]
+    eng = native.Engine(device=0, valtype=native.VAL_AUTO)
+    hg = native.HeteroGraph.from_synthetic(eng, g)
+    _fused_equals_plain(native, eng, hg, paths, reps=2)
+    hg.close()
+    eng.close()
+
+
+@pytest.mark.parametrize("count,lengths", [(48, (2, 6)), (160, (2, 10))])
+def test_fused_batch_on_random_walks_of_a_five_type_graph(native, count, lengths):
+    from resmcm_ari_gb300 import workloads
+    g = workloads.batch_graph(seed=2, scale=1 / 400)
+    paths = workloads.batch_walks(5, g, count, lengths=lengths)
+    eng = native.Engine(device=0)
+    hg = native.HeteroGraph.from_synthetic(eng, g)
+    _fused_equals_plain(native, eng, hg, paths, reps=2)
+    hg.close()
+    eng.close()
+
+
 def test_bad_batch_arguments(native, engine):
     g = synth.tiny_dblp()
     hg = native.HeteroGraph.from_synthetic(engine, g)
