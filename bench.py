@@ -239,46 +239,92 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def batched_section(rg, device, seed=2, scale=1 / 200, count=512, lanes=8, reps=5, tune=True):
-    """512 seeded random-walk meta-paths of 2-10 matrices over the five-type
-    schema graph (vertex counts x``scale``): one chain at a time through
-    rmcm_run_metapath, then as one batch replayed as a CUDA graph."""
-    from resmcm_ari_gb300 import autotune, workloads
-    g = workloads.batch_graph(seed=seed, scale=scale)
-    paths = workloads.batch_walks(3, g, count, lengths=(2, 10))
+def batched_section(rg, device, seed=2, count=512, walk_cap=1e9, group_bytes=48e9, reps=3, tune=True):
+    """Meta-paths of 2-10 matrices drawn by seeded random walks over the
+    five-type schema graph at its configured sizes (types of 10k-500k
+    vertices, 5-40 edges per row): a walk whose RES-predicted bytes exceed
+    ``walk_cap`` is rejected by the estimator (counted) and walks are drawn
+    until ``count`` are admitted.  One chain at a time through
+    rmcm_run_metapath versus fused batches (estimator levels, DP and one
+    block-diagonal SpGEMM per wave for all chains, one CUDA graph each;
+    walks grouped so that a group's predicted bytes stay within
+    ``group_bytes``), after the autotuner's sweep of the configured
+    row-binning tunables on the first group."""
+    from resmcm_ari_gb300 import autotune, serve, synth, workloads
+    g = workloads.batch_graph(seed=seed, scale=1.0)
     eng = rg.Engine(device=device)
     hg = rg.HeteroGraph.from_synthetic(eng, g)
+    paths, preds, drawn, k = [], [], 0, 0
+    while len(paths) < count and drawn < 64 * count:
+        for mp in synth.random_metapaths(3 + k, g, 256, (2, 10)):
+            drawn += 1
+            leaves = hg.leaves(mp)
+            c = eng.estimate(leaves)
+            split, _, _ = eng.order(c)
+            dims = [m.shape[0] for m in leaves] + [leaves[-1].shape[1]]
+            pb = serve.predicted_bytes(c, split, dims)
+            if pb <= walk_cap:
+                paths.append(mp)
+                preds.append(pb)
+                if len(paths) == count:
+                    break
+        k += 1
+    groups, cur, acc = [], [], 0.0
+    for mp, pb in zip(paths, preds):
+        if cur and acc + pb > group_bytes:
+            groups.append(cur)
+            cur, acc = [], 0.0
+        cur.append(mp)
+        acc += pb
+    if cur:
+        groups.append(cur)
     for mp in paths:                                   # leaves built untimed
         eng.run_metapath(hg, mp, keep=False)
     t0 = time.perf_counter()
-    plain_nnz = [eng.run_metapath(hg, mp, keep=False)[1]["nnz"] for mp in paths]
+    plain = []
+    for mp in paths:
+        C, _, _ = eng.run_metapath(hg, mp, keep=True)
+        plain.append(eng.digest(C))
+        C.free()
     plain_s = time.perf_counter() - t0
-    out = {"workload": f"five-type schema graph (vertex counts x{scale:g} of 10k-500k), {count} random-walk "
-                       f"meta-paths of 2-10 matrices, uint32 with uint64 escalation",
-           "type_sizes": g.type_sizes, "chains": count, "lanes": lanes,
-           "plain_chains_per_s": count / plain_s, "result_nnz": int(sum(plain_nnz))}
-    if tune:
+    out = {"workload": f"five-type schema graph at its configured sizes {g.type_sizes} "
+                       f"({sum(r.src.size for r in g.relations)} edges), seeded random-walk meta-paths of 2-10 "
+                       f"matrices, uint32 with uint64 escalation",
+           "type_sizes": g.type_sizes, "chains": len(paths), "walks_drawn": drawn,
+           "rejected_by_estimate": drawn - len(paths), "walk_cap_bytes": walk_cap,
+           "groups": len(groups), "predicted_bytes": float(sum(preds)),
+           "plain_chains_per_s": len(paths) / plain_s, "result_nnz": int(sum(n for n, _ in plain))}
+    if tune and groups:
         t0 = time.perf_counter()
-        res = autotune.tune(eng, hg, paths, lanes=lanes, reps=2, mode="coordinate")
+        space = {k_: v for k_, v in autotune.SPACE.items() if k_ != "warp_max_flops"}
+        res = autotune.tune(eng, hg, groups[0], reps=2, mode="coordinate", space=space, fused=True)
         out["autotune"] = {"best": res["best"], "best_ms": res["best_s"] * 1e3, "default_ms": res["default_s"] * 1e3,
-                           "candidates": len(res["table"]), "seconds": time.perf_counter() - t0}
-    t0 = time.perf_counter()
-    b = eng.batch(hg, paths, lanes=lanes)
-    out["record_s"] = time.perf_counter() - t0
-    info = b.info()
-    walls, devs, same = [], [], True
-    for _ in range(reps):
-        t1 = time.perf_counter()
-        nnz, _, dev = b.run()
-        walls.append(time.perf_counter() - t1)
-        devs.append(dev)
-        same = same and list(map(int, nnz)) == list(map(int, plain_nnz))
-    wall = sorted(walls)[len(walls) // 2]
-    out.update({"batched_chains_per_s": count / wall, "speedup_vs_plain": plain_s / wall,
-                "ms_per_run": wall * 1e3, "device_ms_per_run": sorted(devs)[len(devs) // 2] * 1e3,
-                "graph_nodes": info["graph_nodes"], "gpu_launches_per_run": info["launches_per_run"],
-                "identical_nnz": same, "tuning": eng.get_tuning()})
-    b.free()
+                           "candidates": len(res["table"]), "group_chains": len(groups[0]),
+                           "seconds": time.perf_counter() - t0}
+    dev_s, wall_s, launches, nodes, record_s, same = 0.0, 0.0, 0, 0, 0.0, True
+    i0 = 0
+    for grp in groups:
+        t0 = time.perf_counter()
+        bt = eng.batch(hg, grp, fused=True)
+        record_s += time.perf_counter() - t0
+        info = bt.info()
+        launches += info["launches_per_run"]
+        nodes += info["graph_nodes"]
+        walls, devs = [], []
+        for _ in range(reps):
+            t1 = time.perf_counter()
+            nnz, dig, dev = bt.run()
+            walls.append(time.perf_counter() - t1)
+            devs.append(dev)
+            same = same and [(int(a), int(x)) for a, x in zip(nnz, dig)] == plain[i0:i0 + len(grp)]
+        wall_s += sorted(walls)[len(walls) // 2]
+        dev_s += sorted(devs)[len(devs) // 2]
+        bt.free()
+        i0 += len(grp)
+    out.update({"batched_chains_per_s": len(paths) / wall_s, "speedup_vs_plain": plain_s / wall_s,
+                "ms_per_run": wall_s * 1e3, "device_ms_per_run": dev_s * 1e3, "record_s": record_s,
+                "graph_nodes": nodes, "gpu_launches_per_run": launches, "identical_results": same,
+                "tuning": eng.get_tuning()})
     hg.close()
     eng.close()
     return out

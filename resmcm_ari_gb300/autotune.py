@@ -33,10 +33,10 @@ class TuningMismatch(RuntimeError):
     pass
 
 
-def _measure(engine, graph, paths, cfg, lanes, reps, ref):
+def _measure(engine, graph, paths, cfg, lanes, reps, ref, fused=False):
     engine.set_tuning(**cfg)
     t0 = time.perf_counter()
-    b = engine.batch(graph, paths, lanes=lanes)
+    b = engine.batch(graph, paths, lanes=lanes, fused=fused)
     record_s = time.perf_counter() - t0
     try:
         best = float("inf")
@@ -53,14 +53,15 @@ def _measure(engine, graph, paths, cfg, lanes, reps, ref):
 
 
 def tune(engine, graph, paths: list, lanes: int = 8, reps: int = 3, mode: str = "coordinate",
-         space: dict | None = None, apply: bool = True) -> dict:
+         space: dict | None = None, apply: bool = True, fused: bool = False) -> dict:
     """Returns {"best": cfg, "best_s": seconds, "default_s": seconds,
     "table": [(cfg, seconds, record seconds)]} and, with ``apply``, leaves
-    the best tuning set on the engine."""
+    the best tuning set on the engine.  ``fused``: measure fused batches
+    (rmcm_batch_create_fused) instead of per-chain lanes."""
     space = dict(SPACE if space is None else space)
     default = engine.get_tuning()
     base = {k: default[k] for k in space}
-    t_def, rec_def, ref = _measure(engine, graph, paths, base, lanes, reps, None)
+    t_def, rec_def, ref = _measure(engine, graph, paths, base, lanes, reps, None, fused)
     table = [(dict(base), t_def, rec_def)]
     seen = {tuple(sorted(base.items()))}
     best, best_s = dict(base), t_def
@@ -71,7 +72,7 @@ def tune(engine, graph, paths: list, lanes: int = 8, reps: int = 3, mode: str = 
         if key in seen:
             return
         seen.add(key)
-        s, rec, _ = _measure(engine, graph, paths, cfg, lanes, reps, ref)
+        s, rec, _ = _measure(engine, graph, paths, cfg, lanes, reps, ref, fused)
         table.append((dict(cfg), s, rec))
         if s < best_s:
             best, best_s = dict(cfg), s

@@ -36,7 +36,7 @@ class _FakeEngine:
     def set_tuning(self, **kw):
         self.tuning.update(kw)
 
-    def batch(self, graph, paths, lanes=8):
+    def batch(self, graph, paths, lanes=8, fused=False):
         self.created += 1
         return _FakeBatch(self)
 
