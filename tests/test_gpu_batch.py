@@ -222,3 +222,36 @@ def test_bad_tuning_is_rejected(native, engine):
     assert engine.get_tuning() == {"threads_per_row": 4, "hash_max_flops": 4096, "dense_ratio": 16,
                                    "warp_max_flops": 2048, "hash_load": 0.5, "gemm_inv_density": 512,
                                    "gemm_min_mflops": 512}
+
+
+def test_fused_batch_at_the_configured_sizes_matches_the_oracle(native, oracle_mod):
+    """The batched workload at its configured sizes (five types of 10k-500k
+    vertices, 5-40 edges per row): the first 24 seeded walks whose RES
+    prediction stays within 1 GB, as one fused batch, against the counting
+    oracle's exact path counts on the same graph."""
+    import os
+    from resmcm_ari_gb300 import serve, workloads
+    g = workloads.batch_graph(seed=2, scale=1.0)
+    eng = native.Engine(device=0)
+    hg = native.HeteroGraph.from_synthetic(eng, g)
+    paths = []
+    for mp in synth.random_metapaths(3, g, 256, (2, 10)):
+        leaves = hg.leaves(mp)
+        c = eng.estimate(leaves)
+        split, _, _ = eng.order(c)
+        dims = [m.shape[0] for m in leaves] + [leaves[-1].shape[1]]
+        if serve.predicted_bytes(c, split, dims) <= 1e9:
+            paths.append(mp)
+        if len(paths) == 24:
+            break
+    assert len(paths) == 24
+    b = eng.batch(hg, paths, fused=True)
+    nnz, dig, _ = b.run()
+    b.free()
+    og = oracle_mod.OracleGraph.from_synthetic(g)
+    for mp, n, d in zip(paths, nnz, dig):
+        r = og.chain(mp, oracle_mod.MODE_COUNT, threads=os.cpu_count() or 1, export=False, digest=True)
+        assert r.status == oracle_mod.ORC_OK and r.nnz == int(n) and r.digest == int(d), mp
+    og.close()
+    hg.close()
+    eng.close()
