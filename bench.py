@@ -76,6 +76,8 @@ def parse():
     ap.add_argument("--no-served", action="store_true", help="skip the served (query server) section")
     ap.add_argument("--no-stress", action="store_true", help="skip the stress (12-matrix uint64 chain) section")
     ap.add_argument("--no-parity", action="store_true", help="skip the parity check against the oracle")
+    ap.add_argument("--tune", action="append", default=[], metavar="NAME=VALUE",
+                    help="set a row-binning tunable of the engine before the run (rmcm_set_tuning)")
     return ap.parse_args()
 
 
@@ -172,6 +174,25 @@ def traffic_from_profiles():
         return {"bytes_per_alg_byte": float(out["dram_bytes_per_algorithmic_byte"]), "source": p}
     except (KeyError, ValueError):
         return None
+
+
+def sparse_bound_from_profiles():
+    """Issue and pipe figures of the dominant product's sparse kernel from the
+    committed ncu summary, if any: the bound it reaches (not HBM)."""
+    p = os.path.join(ROOT, "profiles", "dense_light_retail_half.md")
+    if not os.path.exists(p):
+        return None
+    out = {"source": os.path.relpath(p, ROOT)}
+    keys = {"issue active": "issue_active_pct", "L1 / shared pipe": "l1_shared_pipe_pct",
+            "DRAM throughput": "dram_pct"}
+    for ln in open(p):
+        for k, name in keys.items():
+            if ln.startswith("| " + k):
+                try:
+                    out[name] = float(ln.split("|")[2].strip().split("%")[0])
+                except (IndexError, ValueError):
+                    pass
+    return out
 
 
 def dist_env():
@@ -544,6 +565,8 @@ def main():
 
     stream = torch.cuda.current_stream()
     eng = rg.Engine(device=local, valtype=rg.VAL_AUTO, stream=stream.cuda_stream)
+    if args.tune:
+        eng.set_tuning(**{k: float(v) if "." in v else int(v) for k, v in (t.split("=", 1) for t in args.tune)})
     hg = rg.HeteroGraph.from_synthetic(eng, g)
     leaves = {mp: hg.leaves(mp, rg.VAL_U32) for mp in mps}
     # uint64 leaves too (used when a chain escalates on overflow), built untimed
@@ -615,7 +638,8 @@ def main():
                 "product": {k: b[k] for k in ("rows", "inner", "cols", "nnz_a", "nnz_c", "flops", "bin_rows",
                                               "gemm_inner", "gemm_limbs")},
                 "algorithmic_bytes": alg, "launch_ms": avg_ms[dom],
-                "multiply_adds_per_s": b["flops"] / (avg_ms[dom] / 1e3)}
+                "multiply_adds_per_s": b["flops"] / (avg_ms[dom] / 1e3),
+                "sparse_kernel_bound": sparse_bound_from_profiles()}
         # the tensor-core part (exact FP16 GEMM of the heavy inner indices):
         # the product with the most dense multiply-adds, and every GEMM
         gemm_ms = [0.0] * nprod
