@@ -38,6 +38,7 @@ namespace {
 constexpr int kSample = 8;            // A entries per counted one (column counts)
 constexpr int64_t kMaxHeavy = 65536;  // heavy indices at most (A panel row in shared memory)
 constexpr int kGatherThreads = 256;
+constexpr int kGatherPer = 8;          // A entries per thread per step of k_gather_a
 
 // Sampled column counts of A: cnt[u] += 1 for every kSample-th entry.
 __global__ void k_col_sample(DevCsr A, uint32_t *cnt) {
@@ -100,34 +101,48 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather_a(DevCsr A, const int
         __syncthreads();
         const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
         unsigned long long sum = 0, mx = 0;
-        // four entries per thread per step: their gathers overlap
-        for (int64_t k0 = a0; k0 < a1; k0 += 4 * kGatherThreads) {
-            int32_t c[4], sl[4];
-            uint32_t v[4];
+        // kGatherPer entries per thread per step: their gathers overlap; the
+        // light ones are placed with one shared reservation per warp and step
+        for (int64_t k0 = a0; k0 < a1; k0 += kGatherPer * kGatherThreads) {
+            int32_t c[kGatherPer], sl[kGatherPer];
+            uint32_t v[kGatherPer];
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
+            for (int u = 0; u < kGatherPer; u++) {
                 const int64_t k = k0 + u * kGatherThreads + threadIdx.x;
                 c[u] = k < a1 ? A.col[k] : -1;
                 v[u] = k < a1 ? av[k] : 0u;
             }
 #pragma unroll
-            for (int u = 0; u < 4; u++) sl[u] = c[u] >= 0 ? slot[c[u]] : -1;
+            for (int u = 0; u < kGatherPer; u++) sl[u] = c[u] >= 0 ? slot[c[u]] : -1;
+            uint32_t lm = 0;
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
+            for (int u = 0; u < kGatherPer; u++) {
                 if (sl[u] >= 0) {
                     row[sl[u]] = __uint2half_rn(v[u]);
                     sum += v[u];
                     mx = v[u] > mx ? v[u] : mx;
+                } else if (c[u] >= 0) {
+                    lm |= 1u << u;
                 }
-                const bool light = c[u] >= 0 && sl[u] < 0;
-                const unsigned lb = __ballot_sync(0xffffffffu, light);
-                int base = 0;
-                if (lane == 0 && lb) base = atomicAdd(&s_light, __popc(lb));
-                base = __shfl_sync(0xffffffffu, base, 0);
-                if (light) {
-                    const int64_t o = a0 + base + __popc(lb & ((1u << lane) - 1u));
+            }
+            const int nl = __popc(lm);
+            int incl = nl;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += t;
+            }
+            const int wtot = __shfl_sync(0xffffffffu, incl, 31);
+            int base = 0;
+            if (lane == 0 && wtot) base = atomicAdd(&s_light, wtot);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            int64_t o = a0 + base + incl - nl;
+#pragma unroll
+            for (int u = 0; u < kGatherPer; u++) {
+                if ((lm >> u) & 1u) {
                     lcol[o] = c[u];
                     lval[o] = v[u];
+                    o++;
                 }
             }
         }
