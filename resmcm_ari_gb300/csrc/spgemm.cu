@@ -631,7 +631,12 @@ __global__ void __launch_bounds__(256) k_tiny(DevCsr A, DevCsr B, DevCsr C, cons
             if (sizeof(V) == 4 && head) ovf |= s > 0xffffffffull;
             const int64_t base = C.rowptr[r];
             const int64_t rlen = C.rowptr[r + 1] - base;
-            if (lane == 0 && rlen != __popc(heads)) raise_status(st, kInvariant);
+            if (lane == 0) {
+                // single pass (cnt given): the row's slots bound its entries
+                const int64_t nh = __popc(heads);
+                if (cnt) cnt[r] = nh;
+                if (cnt ? nh > rlen : rlen != nh) raise_status(st, kInvariant);
+            }
             if (head) {
                 const int pos = __popc(heads & lt_mask);
                 if (pos < rlen) {
@@ -790,8 +795,13 @@ __global__ void __launch_bounds__(kWarpWarps * 32) k_warp(DevCsr A, DevCsr B, De
             }
         }
         if (lane == 0) {
-            if (!NUMERIC) cnt[r] = pos;
-            else if (pos != rlen) raise_status(st, kInvariant);
+            if (!NUMERIC) {
+                cnt[r] = pos;
+            } else {
+                // single pass (cnt given): the row's slots bound its entries
+                if (cnt) cnt[r] = pos;
+                if (cnt ? pos > rlen : pos != rlen) raise_status(st, kInvariant);
+            }
         }
         __syncwarp();
     }
@@ -875,7 +885,12 @@ __global__ void __launch_bounds__(256) k_micro(DevCsr A, DevCsr B, DevCsr C, con
             if (active) {
                 const int64_t base = C.rowptr[r];
                 const int64_t rlen = C.rowptr[r + 1] - base;
-                if (g == 0 && rlen != __popc(heads)) raise_status(st, kInvariant);
+                if (g == 0) {
+                    // single pass (cnt given): the row's slots bound its entries
+                    const int64_t nh = __popc(heads);
+                    if (cnt) cnt[r] = nh;
+                    if (cnt ? nh > rlen : rlen != nh) raise_status(st, kInvariant);
+                }
                 if (head) {
                     const int pos = __popc(heads & ((1u << g) - 1u));
                     if (pos < rlen) {
@@ -1379,7 +1394,11 @@ __global__ void __launch_bounds__(NT) k_hash(DevCsr A, DevCsr B, DevCsr C, const
             }
             const int64_t base = C.rowptr[r];
             const int64_t rlen = C.rowptr[r + 1] - base;
-            if (tid == 0 && rlen != n) raise_status(st, kInvariant);
+            if (tid == 0) {
+                // single pass (cnt given): the row's slots bound its entries
+                if (cnt) cnt[r] = n;
+                if (cnt ? (int64_t)n > rlen : rlen != n) raise_status(st, kInvariant);
+            }
             const int lim = (int)((int64_t)n < rlen ? (int64_t)n : rlen);
             for (int i = tid; i < lim; i += NT) {
                 C.col[base + i] = sk[i];
@@ -2294,6 +2313,35 @@ __global__ void __launch_bounds__(kRankThreads) k_rank_split_val(DevCsr A, DevCs
     if (__syncthreads_or(ovf) && threadIdx.x == 0) raise_status(st, kOverflow);
 }
 
+// Slots of the short-row temporary: min(products, columns) for a row of
+// the short-row bins, none for the others.
+__global__ void k_short_cap(int64_t m, const uint8_t *bin_of, const int64_t *flops, int64_t cols, uint32_t mask,
+                            int64_t *cap) {
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x) {
+        const int b = bin_of[r] & ~kRiskyBit;
+        cap[r] = (b != kEmptyBin && ((mask >> b) & 1u)) ? (flops[r] < cols ? flops[r] : cols) : 0;
+    }
+}
+
+// The short-row bins' rows from their slots in the temporary into C (a warp
+// per row; the row's length is C's, from the scan of the reported lengths).
+template <typename V>
+__global__ void __launch_bounds__(256) k_copy_short(int64_t m, const uint8_t *bin_of, uint32_t mask,
+                                                    const int64_t *trow, const int32_t *tcol, const V *tval,
+                                                    DevCsr C) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < m; r += nw) {
+        const int b = bin_of[r] & ~kRiskyBit;
+        if (b == kEmptyBin || !((mask >> b) & 1u)) continue;
+        const int64_t d0 = C.rowptr[r], len = C.rowptr[r + 1] - d0, s0 = trow[r];
+        for (int64_t i = lane; i < len; i += 32) {
+            C.col[d0 + i] = tcol[s0 + i];
+            ((V *)C.val)[d0 + i] = tval[s0 + i];
+        }
+    }
+}
+
 __global__ void k_iota(int32_t *v, int32_t n) {
     for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = i;
 }
@@ -2564,7 +2612,7 @@ template <typename V, bool NUMERIC>
 int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevCsr &C, const int32_t *lists,
                     const int32_t *counts, int32_t dense_max_alen, int64_t *cnt, int32_t *cursor_base,
                     int64_t cursor_cap, const DenseTemp *temp, const uint8_t *bin_of, bool positive,
-                    bool b_distinct, const RankSplit *rs) {
+                    bool b_distinct, const RankSplit *rs, uint32_t bin_mask = ~0u) {
     cudaStream_t s = h->stream;
     int *st = h->d_status;
     int32_t off = 0;
@@ -2574,7 +2622,7 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
         const int32_t n = counts[b];
         const int32_t *list = lists + off;
         off += n;
-        if (n == 0) continue;
+        if (n == 0 || !((bin_mask >> b) & 1u)) continue;
         switch (b) {
             case kBinWarp: {
                 const int64_t sm = (int64_t)kWarpWarps * (kWarpCols + (NUMERIC ? (int64_t)kWarpCols * sizeof(V) : 0));
@@ -3220,10 +3268,89 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         dtemp.split = false;
     };
 
+    // Single pass for the short-row bins (tiny, micro, hash, warp): each such
+    // row gets min(products, columns) slots in a temporary, their numeric
+    // kernels write there and report each row's length (the symbolic pass is
+    // skipped for them), and after the scan the rows are copied into C.
+    constexpr uint32_t kShortBins = (1u << kBinTiny) | (1u << kBinHash512) | (1u << kBinHash2k) |
+                                    (1u << kBinHash8k) | (1u << kBinMicro) | (1u << kBinWarp);
+    struct {
+        bool active = false;
+        int64_t *rowptr = nullptr;
+        int32_t *col = nullptr;
+        void *val = nullptr;
+        int64_t total = 0, rp_bytes = 0, c_bytes = 0, v_bytes = 0;
+    } stemp;
+    auto drop_short = [&]() {
+        if (stemp.rowptr) dev_free(h, stemp.rowptr, stemp.rp_bytes);
+        if (stemp.col) dev_free(h, stemp.col, stemp.c_bytes);
+        if (stemp.val) dev_free(h, stemp.val, stemp.v_bytes);
+        stemp.rowptr = nullptr;
+        stemp.col = nullptr;
+        stemp.val = nullptr;
+        stemp.active = false;
+    };
+    {
+        int64_t n_short = 0;
+        for (int b = 0; b < kNumBins; b++)
+            if ((kShortBins >> b) & 1u) n_short += counts[b];
+        bool want = replay ? plan->short_temp : (n_short > 0 && h->tune.short_single_pass);
+        if (want) {
+            // slots: a capacity per row (m of them, then scanned in place of
+            // a copy) and the row pointers of the temporary
+            stemp.rp_bytes = 16 * (m + 1);
+            if (dev_alloc(h, (void **)&stemp.rowptr, stemp.rp_bytes) == RMCM_OK) {
+                int64_t *capr = stemp.rowptr + (m + 1);
+                k_short_cap<<<grid_for(h, m, 256, 8), 256, 0, s>>>(m, bin_of, flops, B.cols, kShortBins, capr);
+                h->launches++;
+                int32_t src = cudaGetLastError() == cudaSuccess ? RMCM_OK : set_error(h, RMCM_ECUDA, "short capacity");
+                if (src == RMCM_OK)
+                    src = scan_rowptr(h, capr, m, stemp.rowptr, tiles, (unsigned long long *)(small + 44),
+                                      replay ? plan->short_total : -1);
+                if (src == RMCM_OK && !replay) {
+                    cudaError_t e = cudaMemcpyAsync(h->h_pinned, stemp.rowptr + m, 8, cudaMemcpyDeviceToHost, s);
+                    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+                    if (e != cudaSuccess) src = cuda_error(h, e, "short capacity download");
+                    else stemp.total = h->h_pinned[0];
+                }
+                if (replay) stemp.total = plan->short_total;
+                const int64_t room = h->budget - h->in_use;
+                stemp.c_bytes = 4 * std::max<int64_t>(stemp.total, 1);
+                stemp.v_bytes = (int64_t)sizeof(V) * std::max<int64_t>(stemp.total, 1);
+                if (src == RMCM_OK &&
+                    (replay || stemp.c_bytes + stemp.v_bytes <= std::min<int64_t>(h->tune.dense_temp_max_bytes, room / 2)) &&
+                    dev_alloc(h, (void **)&stemp.col, stemp.c_bytes) == RMCM_OK &&
+                    dev_alloc(h, &stemp.val, stemp.v_bytes) == RMCM_OK) {
+                    stemp.active = true;
+                } else {
+                    if (src != RMCM_OK) {
+                        drop_short();
+                        drop_cursors();
+                        drop_temp();
+                        drop_rank();
+                        return src;
+                    }
+                    drop_short();
+                    h->last_error.clear();
+                }
+            } else {
+                h->last_error.clear();
+            }
+        }
+        if (replay && plan->short_temp && !stemp.active)
+            return set_error(h, RMCM_ENOMEM, "replay: short-row temporary could not be allocated");
+        if (record) {
+            plan->short_temp = stemp.active;
+            plan->short_total = stemp.total;
+        }
+    }
+    const uint32_t other_bins = stemp.active ? ~kShortBins : ~0u;
+
     // symbolic
     rmcm_mat *C = nullptr;
     int32_t rc = mat_alloc(h, m, B.cols, -1, Am->valtype, &C);
     if (rc != RMCM_OK) {
+        drop_short();
         drop_cursors();
         drop_temp();
         drop_rank();
@@ -3237,9 +3364,19 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         h->launches++;
         if (cudaGetLastError() != cudaSuccess) rc = set_error(h, RMCM_ECUDA, "row list launch");
     }
+    if (rc == RMCM_OK && stemp.active) {
+        // the short-row bins, once, into the temporary (lengths to cnt)
+        DevCsr T = C->d;
+        T.rowptr = stemp.rowptr;
+        T.col = stemp.col;
+        T.val = stemp.val;
+        T.nnz = stemp.total;
+        rc = launch_bins<V, true>(h, A, B, T, lists, counts, dense_max_alen, cnt, cursors, cursor_cap, &dtemp, bin_of,
+                                  positive, Bm->distinct, &rsplit, kShortBins);
+    }
     if (rc == RMCM_OK)
         rc = launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap, &dtemp,
-                                   bin_of, positive, Bm->distinct, &rsplit);
+                                   bin_of, positive, Bm->distinct, &rsplit, other_bins);
     if (rc == RMCM_OK)
         rc = scan_rowptr(h, cnt, m, C->d.rowptr, tiles, (unsigned long long *)(small + 44), replay ? plan->nnz : -1);
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[3], s);
@@ -3265,6 +3402,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         if (e != cudaSuccess) rc = cuda_error(h, e, "spgemm status download");
         else if (h->h_status[kOverflow]) {
             cudaMemsetAsync(h->d_status + kOverflow, 0, sizeof(int), s);
+            drop_short();
             drop_cursors();
             drop_temp();
             drop_rank();
@@ -3288,9 +3426,16 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         rc = mat_alloc(h, m, B.cols, nnz, Am->valtype, &C);
     }
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[4], s);
+    if (rc == RMCM_OK && !adopt && stemp.active) {
+        k_copy_short<V><<<grid_for(h, m * 32, 256, 16), 256, 0, s>>>(m, bin_of, kShortBins, stemp.rowptr, stemp.col,
+                                                                       (const V *)stemp.val, C->d);
+        h->launches++;
+        if (cudaGetLastError() != cudaSuccess) rc = set_error(h, RMCM_ECUDA, "short-row copy launch");
+    }
     if (rc == RMCM_OK && !adopt)
         rc = launch_bins<V, true>(h, A, B, C->d, lists, counts, dense_max_alen, nullptr, cursors, cursor_cap, &dtemp,
-                                  bin_of, positive, Bm->distinct, &rsplit);
+                                  bin_of, positive, Bm->distinct, &rsplit, other_bins);
+    drop_short();
     const int32_t gemm_limbs = dtemp.dpart.S ? dtemp.dpart.limbs * dtemp.dpart.alimbs : 0;
     const int64_t gemm_inner = dtemp.dpart.S ? dtemp.dpart.heavy : 0;
     drop_cursors();
