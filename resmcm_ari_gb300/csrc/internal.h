@@ -223,7 +223,7 @@ struct DensePart {
     const void *S = nullptr;
     int64_t ld = 0;
     int32_t limbs = 0, bits = 0;      // B's limbs
-    int32_t alimbs = 1, abits = 0;    // A's limbs (uint64 products; 1 and 0 for uint32)
+    int32_t alimbs = 1, abits = 0;    // A's limbs (limb form; 1 and 0 for the one-limb uint32 form)
     int32_t chunks = 1;               // chunks of the heavy indices (uint64 products)
     int64_t heavy = 0;
     const uint8_t *skip = nullptr;
@@ -231,12 +231,17 @@ struct DensePart {
     const int32_t *lcol = nullptr;
     const uint32_t *lval = nullptr;
     const int32_t *lcnt = nullptr;
+    // with light_flops: row r's light products (B row lengths over its light
+    // entries), their largest row sum and their total
+    const int64_t *lflops = nullptr;
+    int64_t lmax = 0, ltotal = 0;
     void *mem = nullptr, *sel = nullptr, *amem = nullptr;
     int64_t bytes = 0, sel_bytes = 0, abytes = 0;
 };
-// ev_begin / ev_end (may be null) are recorded around the GEMMs.
+// ev_begin / ev_end (may be null) are recorded around the GEMMs; light_flops
+// also counts each row's light products (dp.lflops, dp.lmax, dp.ltotal).
 int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint64_t bmax, DensePart &dp,
-                         cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr);
+                         cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr, bool light_flops = false);
 // uint64 products: A split into limbs too and the heavy indices into chunks.
 int32_t dense_part_build64(rmcm_handle *h, const DevCsr &A, const DevCsr &B, DensePart &dp,
                            cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr);

@@ -1174,6 +1174,17 @@ __device__ __forceinline__ int hash_insert(int32_t *keys, V *vals, int32_t c, V 
     return 0;
 }
 
+// Inclusive prefix sum of v over the lanes of a full warp.
+__device__ __forceinline__ int warp_incl_scan(int v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int o = __shfl_up_sync(kFull, v, d);
+        if (lane >= d) v += o;
+    }
+    return v;
+}
+
 // Block-wide exclusive scan of one int per thread; returns the total.
 template <int NT>
 __device__ __forceinline__ int block_excl_scan(int v, int *excl, int *s_warp) {
@@ -1781,7 +1792,8 @@ __global__ void __launch_bounds__(kSplitThreads) k_dense_split(DevCsr A, DevCsr 
                                                                int32_t max_slots, int32_t W,
                                                                unsigned long long *G, uint32_t *Gbits,
                                                                const uint8_t *bin_of, int *st, int32_t wc,
-                                                               bool pull_ok, const uint32_t *pk, int32_t cbits) {
+                                                               bool pull_ok, const uint32_t *pk, int32_t cbits,
+                                                               const int32_t *lcnt) {
     constexpr int NT = kSplitThreads;
     constexpr int kPull = 4;   // register accumulators per thread: rows of up to 4 * NT columns
     static_assert(kChunk == NT, "one staged A entry per thread");
@@ -1814,7 +1826,8 @@ __global__ void __launch_bounds__(kSplitThreads) k_dense_split(DevCsr A, DevCsr 
         const int part = task - task_start[slot];
         const int np = parts[slot];
         const int32_t r = rows[row_of_slot[slot]];
-        const int64_t a0 = A.rowptr[r], alen = A.rowptr[r + 1] - a0;
+        // (lcnt: A holds the row's light entries only, lcnt[r] of them)
+        const int64_t a0 = A.rowptr[r], alen = lcnt ? (int64_t)lcnt[r] : A.rowptr[r + 1] - a0;
         const int64_t ka = a0 + alen * part / np, kb = a0 + alen * (part + 1) / np;
         const bool checked = (bin_of[r] & kRiskyBit) != 0;
         // B rows covering all wc columns ("full", as in the dense bin) are
@@ -1960,12 +1973,16 @@ __global__ void __launch_bounds__(kSplitThreads) k_dense_split(DevCsr A, DevCsr 
 
 // One CTA per split row: the accumulated row, in column order, into its
 // padded slot of the temporary (row ri at ri * tstride); its length to cnt.
+// With S (the tensor-core part's counts, row r at r * gld; every value
+// positive) a column is present when either part has it and its count is
+// the sum of both.
 template <typename V>
 __global__ void __launch_bounds__(kSplitThreads) k_split_finish(DevCsr T, const int32_t *rows,
                                                                 const int32_t *row_of_slot, const int32_t *nslots,
                                                                 int32_t max_slots, int64_t ncols, int32_t W,
                                                                 const unsigned long long *G, const uint32_t *Gbits,
-                                                                int64_t tstride, int64_t *cnt, int *st) {
+                                                                int64_t tstride, int64_t *cnt, int *st,
+                                                                const V *S, int64_t gld) {
     constexpr int NT = kSplitThreads, NW = NT / 32;
     __shared__ int64_t s_warp[NW];
     const int ns = min(*nslots, max_slots);
@@ -1977,11 +1994,21 @@ __global__ void __launch_bounds__(kSplitThreads) k_split_finish(DevCsr T, const 
         const int32_t r = rows[ri];
         const unsigned long long *g = G + (int64_t)slot * W;
         const uint32_t *gb = Gbits + (int64_t)slot * (W / 32);
+        const V *srow = S ? S + (int64_t)r * gld : nullptr;
         const int groups = (int)((ncols + 31) >> 5);
         const int gchunk = (groups + NW - 1) / NW;
         const int g0 = min(warp * gchunk, groups), g1 = min(g0 + gchunk, groups);
+        // presence bits of group q (warp-uniform)
+        auto word = [&](int q) -> unsigned {
+            unsigned bits = gb[q];
+            if (srow) {
+                const int64_t c = (int64_t)q * 32 + lane;
+                bits |= __ballot_sync(kFull, c < ncols && srow[c] != 0);
+            }
+            return bits;
+        };
         int64_t mine = 0;
-        for (int q = g0; q < g1; q++) mine += __popc(gb[q]);
+        for (int q = g0; q < g1; q++) mine += __popc(word(q));
         if (lane == 0) s_warp[warp] = mine;
         __syncthreads();
         int64_t base = 0, total = 0;
@@ -1991,11 +2018,16 @@ __global__ void __launch_bounds__(kSplitThreads) k_split_finish(DevCsr T, const 
         }
         int64_t pos = (int64_t)ri * tstride + base;
         for (int q = g0; q < g1; q++) {
-            const unsigned bits = gb[q];
+            const unsigned bits = word(q);
             if (bits & (1u << lane)) {
                 const int64_t o = pos + __popc(bits & lt_mask);
                 const int32_t c = q * 32 + lane;
-                const unsigned long long v = g[c];
+                unsigned long long v = g[c];
+                if (srow) {
+                    const unsigned long long sv = (unsigned long long)srow[c];
+                    ovf |= v > ~0ull - sv;
+                    v += sv;
+                }
                 if (sizeof(V) == 4) ovf |= v > 0xffffffffull;
                 T.col[o] = c;
                 ((V *)T.val)[o] = (V)v;
@@ -2014,12 +2046,14 @@ __global__ void __launch_bounds__(kSplitThreads) k_split_finish(DevCsr T, const 
 //
 // A CTA per row holds a bitmap of the whole output row in shared memory.
 // Symbolic: set the bit of every product's column, count the bits.  Numeric:
-// rebuild the bitmap, turn it into ranks (per 32-word block a prefix of set
-// bits, per word a prefix inside its block), write the sorted columns
+// rebuild the bitmap, turn it into ranks (per 128-word group a prefix of set
+// bits, per word a prefix inside its group), write the sorted columns
 // straight from the bitmap, zero the row's values, then stream the products
 // again and add each one at C.val[row start + rank(column)] with a global
-// atomic.  The cost per row is two or three passes over its products plus one
-// scan of the bitmap, whatever the row's width or product count.
+// atomic.  The cost per row is two or three passes over its products plus two
+// scans of the bitmap, whatever the row's width or product count; the scans
+// take a group per warp and four words per lane (one 16-byte load), since
+// most words of a wide row are empty.
 
 constexpr int kRankThreads = 512;
 
@@ -2029,11 +2063,11 @@ __global__ void __launch_bounds__(kRankThreads) k_rank(DevCsr A, DevCsr B, DevCs
     constexpr int NT = kRankThreads;
     using AtomV = typename std::conditional<sizeof(V) == 4, unsigned int, unsigned long long>::type;
     extern __shared__ __align__(16) unsigned char smem[];
-    const int nblocks = (int)((B.cols + 1023) >> 10);       // 32-word (1024-column) blocks
-    const int nwords = nblocks * 32;
+    const int ngroups = (int)((B.cols + 4095) >> 12);       // 128-word (4096-column) groups
+    const int nwords = ngroups * 128;
     uint32_t *bits = (uint32_t *)smem;
     uint16_t *wpre = (uint16_t *)(bits + nwords);             // NUMERIC only
-    uint32_t *bpre = (uint32_t *)(wpre + nwords);             // NUMERIC only
+    uint32_t *gpre = (uint32_t *)(wpre + nwords);             // NUMERIC only
     __shared__ ChunkStage<V> sg;
     __shared__ int s_warp[NT / 32];
     __shared__ int64_t s_cnt;
@@ -2055,32 +2089,41 @@ __global__ void __launch_bounds__(kRankThreads) k_rank(DevCsr A, DevCsr B, DevCs
         }
         if (!NUMERIC) {
             int mine = 0;
-            for (int w = tid; w < nwords; w += NT) mine += __popc(bits[w]);
+            for (int i = tid; i < nwords / 4; i += NT) {
+                const uint4 q = ((const uint4 *)bits)[i];
+                mine += __popc(q.x) + __popc(q.y) + __popc(q.z) + __popc(q.w);
+            }
             int excl;
             const int total = block_excl_scan<NT>(mine, &excl, s_warp);
             if (tid == 0) cnt[r] = total;
             continue;
         }
-        // ranks: thread t owns a contiguous run of 32-word blocks; per word the
-        // set bits before it inside its block, per block the set bits before it
+        const int lane = tid & 31;
+        // ranks: a warp per group, four words per lane: per word the set bits
+        // before it inside its group (the lane's own words, then a shuffle
+        // scan over the lanes; four uint16 in one 8-byte store), per group the
+        // set bits before it (a block scan over the group totals)
         {
-            const int per = (nblocks + NT - 1) / NT;
-            const int b0 = min(tid * per, nblocks), b1 = min(b0 + per, nblocks);
-            int mine = 0;
-            for (int b = b0; b < b1; b++) {
-                int run = 0;
-                for (int j = 0; j < 32; j++) {
-                    wpre[b * 32 + j] = (uint16_t)run;
-                    run += __popc(bits[b * 32 + j]);
-                }
-                bpre[b] = (uint32_t)run;
-                mine += run;
+            for (int g = tid >> 5; g < ngroups; g += NT / 32) {
+                const int w0 = g * 128 + lane * 4;
+                const uint4 q = *(const uint4 *)(bits + w0);
+                const int p0 = __popc(q.x), p1 = __popc(q.y), p2 = __popc(q.z);
+                const int t = p0 + p1 + p2 + __popc(q.w);
+                const int x = warp_incl_scan(t);
+                const uint32_t e = (uint32_t)(x - t);
+                *(uint2 *)(wpre + w0) = make_uint2(e | ((e + p0) << 16), (e + p0 + p1) | ((e + p0 + p1 + p2) << 16));
+                if (lane == 31) gpre[g] = (uint32_t)x;
             }
+            __syncthreads();
+            const int per = (ngroups + NT - 1) / NT;
+            const int g0 = min(tid * per, ngroups), g1 = min(g0 + per, ngroups);
+            int mine = 0;
+            for (int g = g0; g < g1; g++) mine += (int)gpre[g];
             int excl;
             const int total = block_excl_scan<NT>(mine, &excl, s_warp);
-            for (int b = b0; b < b1; b++) {
-                const uint32_t t = bpre[b];
-                bpre[b] = (uint32_t)excl;
+            for (int g = g0; g < g1; g++) {
+                const uint32_t t = gpre[g];
+                gpre[g] = (uint32_t)excl;
                 excl += (int)t;
             }
             if (tid == 0) s_cnt = total;
@@ -2089,18 +2132,25 @@ __global__ void __launch_bounds__(kRankThreads) k_rank(DevCsr A, DevCsr B, DevCs
         const int64_t base = C.rowptr[r];
         const int64_t rlen = C.rowptr[r + 1] - base;
         if (tid == 0 && s_cnt != rlen) raise_status(st, kInvariant);
-        // sorted columns straight from the bitmap; zero the row's values
-        for (int w = tid; w < nwords; w += NT) {
-            uint32_t word = bits[w];
-            int64_t pos = (int64_t)bpre[w >> 5] + wpre[w];
-            while (word) {
-                const int b = __ffs(word) - 1;
-                word &= word - 1;
-                if (pos < rlen) {
-                    C.col[base + pos] = w * 32 + b;
-                    ((V *)C.val)[base + pos] = 0;
+        // sorted columns straight from the bitmap (four words per lane, from
+        // the first one's rank); zero the row's values
+        for (int g = tid >> 5; g < ngroups; g += NT / 32) {
+            const int w0 = g * 128 + lane * 4;
+            const uint4 q = *(const uint4 *)(bits + w0);
+            int64_t pos = (int64_t)gpre[g] + wpre[w0];
+            const uint32_t ws[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                uint32_t word = ws[j];
+                while (word) {
+                    const int b = __ffs(word) - 1;
+                    word &= word - 1;
+                    if (pos < rlen) {
+                        C.col[base + pos] = (w0 + j) * 32 + b;
+                        ((V *)C.val)[base + pos] = 0;
+                    }
+                    pos++;
                 }
-                pos++;
             }
         }
         __syncthreads();
@@ -2108,7 +2158,7 @@ __global__ void __launch_bounds__(kRankThreads) k_rank(DevCsr A, DevCsr B, DevCs
         V *vals = (V *)C.val + base;
         auto rank_of = [&](int32_t c) -> int64_t {
             const int w = c >> 5;
-            return (int64_t)bpre[w >> 5] + wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u));
+            return (int64_t)gpre[w >> 7] + wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u));
         };
         auto add_plain = [&](int32_t c, V p) {
             const int64_t pos = rank_of(c);
@@ -2222,37 +2272,55 @@ __global__ void __launch_bounds__(kRankThreads) k_rank_split_prep(DevCsr C, cons
                                                                   const int32_t *row_of_slot, const int32_t *nslots,
                                                                   int32_t max_slots, int32_t nwords,
                                                                   const uint32_t *gbits, uint32_t *gpre, int *st) {
-    constexpr int NT = kRankThreads;
-    __shared__ int s_warp[NT / 32];
+    constexpr int NT = kRankThreads, NW = NT / 32;
+    __shared__ int s_warp[NW];
+    __shared__ uint32_t s_bpre[kRankCols / 1024];
     const int ns = min(*nslots, max_slots);
-    const int tid = threadIdx.x;
-    const int per = (nwords + NT - 1) / NT;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int nblocks = nwords >> 5;                          // nwords is a multiple of 32
+    const int per = (nblocks + NT - 1) / NT;
+    const int b0 = min(tid * per, nblocks), b1 = min(b0 + per, nblocks);
     for (int slot = blockIdx.x; slot < ns; slot += gridDim.x) {
         const int32_t r = rows[row_of_slot[slot]];
         const uint32_t *g = gbits + (int64_t)slot * nwords;
         uint32_t *pre = gpre + (int64_t)slot * nwords;
-        const int w0 = min(tid * per, nwords), w1 = min(w0 + per, nwords);
+        // set bits per 32-word block (a warp per block, coalesced)
+        for (int b = tid >> 5; b < nblocks; b += NW) {
+            const int x = warp_incl_scan(__popc(g[b * 32 + lane]));
+            if (lane == 31) s_bpre[b] = (uint32_t)x;
+        }
+        __syncthreads();
         int mine = 0;
-        for (int w = w0; w < w1; w++) mine += __popc(g[w]);
+        for (int b = b0; b < b1; b++) mine += (int)s_bpre[b];
         int excl;
         const int total = block_excl_scan<NT>(mine, &excl, s_warp);
+        for (int b = b0; b < b1; b++) {
+            const uint32_t t = s_bpre[b];
+            s_bpre[b] = (uint32_t)excl;
+            excl += (int)t;
+        }
+        __syncthreads();
         const int64_t base = C.rowptr[r];
         const int64_t rlen = C.rowptr[r + 1] - base;
         if (tid == 0 && total != rlen) raise_status(st, kInvariant);
-        int64_t pos = excl;
-        for (int w = w0; w < w1; w++) {
-            pre[w] = (uint32_t)pos;
+        // per-word ranks and the sorted columns, a warp per block again
+        for (int b = tid >> 5; b < nblocks; b += NW) {
+            const int w = b * 32 + lane;
             uint32_t word = g[w];
+            const int p = __popc(word);
+            int64_t pos = (int64_t)s_bpre[b] + warp_incl_scan(p) - p;
+            pre[w] = (uint32_t)pos;
             while (word) {
-                const int b = __ffs(word) - 1;
+                const int bit = __ffs(word) - 1;
                 word &= word - 1;
                 if (pos < rlen) {
-                    C.col[base + pos] = w * 32 + b;
+                    C.col[base + pos] = w * 32 + bit;
                     ((V *)C.val)[base + pos] = 0;
                 }
                 pos++;
             }
         }
+        __syncthreads();
     }
 }
 
@@ -2589,6 +2657,7 @@ struct RankSplit {
 
 // Rows with fewer products than this are never split.
 constexpr int64_t kSplitMinFlops = 1 << 20;
+constexpr int64_t kSplitMinLight = 1 << 18;   // light products of rows beside a tensor-core part
 
 // A rows with more entries than this are analysed by the whole grid.
 constexpr int64_t kLongAnalyze = 16384;
@@ -2674,8 +2743,9 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                 break;
             }
             case kBinRank: {
-                const int64_t nwords = (ncols + 1023) / 1024 * 32;
-                const int64_t sm = NUMERIC ? nwords * 4 + nwords * 2 + (nwords / 32) * 4 : nwords * 4;
+                // k_rank: 128-word groups (bitmap, per-word and per-group prefixes)
+                const int64_t nwords = (ncols + 4095) / 4096 * 128;
+                const int64_t sm = NUMERIC ? nwords * 4 + nwords * 2 + (nwords / 128) * 4 : nwords * 4;
                 auto kern = k_rank<V, NUMERIC>;
                 RMCM_TRY(set_smem(h, kern, sm));
                 const int per_sm = (int)std::max<int64_t>(1, std::min<int64_t>(4, (200 * 1024) / std::max<int64_t>(sm, 1)));
@@ -2686,21 +2756,23 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                     RMCM_CUDA(h, cudaEventRecord(h->ev_fork, s));
                     RMCM_CUDA(h, cudaStreamWaitEvent(h->aux, h->ev_fork, 0));
                     const int sgrid = h->sm_count * 2;
+                    // (the split kernels' bitmaps: 32-word blocks, rs->nwords per slot)
+                    const int64_t snw = rs->nwords;
                     if (!NUMERIC) {
                         auto ks = k_rank_split_sym<V>;
-                        RMCM_TRY(set_smem(h, ks, nwords * 4));
-                        k_rank_split_sym<V><<<sgrid, kRankThreads, nwords * 4, h->aux>>>(
+                        RMCM_TRY(set_smem(h, ks, snw * 4));
+                        k_rank_split_sym<V><<<sgrid, kRankThreads, snw * 4, h->aux>>>(
                             A, B, rs->perm, rs->row_of_slot, rs->parts, rs->task_start, rs->nslots, rs->max_slots,
-                            (int32_t)nwords, rs->gbits);
+                            (int32_t)snw, rs->gbits);
                         k_rank_split_count<<<rs->max_slots, 512, 0, h->aux>>>(
-                            rs->perm, rs->row_of_slot, rs->nslots, rs->max_slots, (int32_t)nwords, rs->gbits, cnt);
+                            rs->perm, rs->row_of_slot, rs->nslots, rs->max_slots, (int32_t)snw, rs->gbits, cnt);
                     } else {
                         k_rank_split_prep<V><<<rs->max_slots, kRankThreads, 0, h->aux>>>(
-                            C, rs->perm, rs->row_of_slot, rs->nslots, rs->max_slots, (int32_t)nwords, rs->gbits,
+                            C, rs->perm, rs->row_of_slot, rs->nslots, rs->max_slots, (int32_t)snw, rs->gbits,
                             rs->gpre, st);
                         k_rank_split_val<V><<<sgrid, kRankThreads, 0, h->aux>>>(
                             A, B, C, rs->perm, rs->row_of_slot, rs->parts, rs->task_start, rs->nslots,
-                            rs->max_slots, (int32_t)nwords, rs->gbits, rs->gpre, bin_of, st);
+                            rs->max_slots, (int32_t)snw, rs->gbits, rs->gpre, bin_of, st);
                     }
                     h->launches += 2;
                 }
@@ -2740,6 +2812,12 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                         DevCsr T = C;
                         T.col = temp->col;
                         T.val = temp->val;
+                        // with a tensor-core part, A's light entries only
+                        DevCsr Al = A;
+                        if (temp->dpart.S) {
+                            Al.col = const_cast<int32_t *>(temp->dpart.lcol);
+                            Al.val = const_cast<uint32_t *>(temp->dpart.lval);
+                        }
                         if (temp->split) {
                             // the split rows run on the second stream, beside the dense bin
                             const bool slite = positive && temp->no_risky;
@@ -2750,24 +2828,20 @@ int32_t launch_bins(rmcm_handle *h, const DevCsr &A, const DevCsr &B, const DevC
                             RMCM_CUDA(h, cudaStreamWaitEvent(h->aux, h->ev_fork, 0));
                             const int sper = (int)std::max<int64_t>(1, std::min<int64_t>(4, (200 * 1024) / std::max<int64_t>(ssm, 1)));
                             ks<<<(int)((int64_t)h->sm_count * sper), kSplitThreads, ssm, h->aux>>>(
-                                A, B, temp->perm, temp->row_of_slot, temp->parts, temp->task_start, temp->nslots,
+                                Al, B, temp->perm, temp->row_of_slot, temp->parts, temp->task_start, temp->nslots,
                                 temp->max_slots, (int32_t)W, temp->G, temp->Gbits, bin_of, st, (int32_t)ncols,
-                                b_distinct && ncols <= 4 * kSplitThreads, temp->pk, temp->cbits);
+                                b_distinct && ncols <= 4 * kSplitThreads, temp->pk, temp->cbits,
+                                temp->dpart.S ? temp->dpart.lcnt : nullptr);
                             k_split_finish<V><<<temp->max_slots, kSplitThreads, 0, h->aux>>>(
                                 T, temp->perm, temp->row_of_slot, temp->nslots, temp->max_slots, ncols, (int32_t)W,
-                                temp->G, temp->Gbits, temp->stride, cnt, st);
+                                temp->G, temp->Gbits, temp->stride, cnt, st, (const V *)temp->dpart.S,
+                                temp->dpart.ld);
                             h->launches += 2;
                         }
                         // split rows sit at the back of the permuted list: the dense
                         // kernel takes its front
                         const int32_t *dl = temp->split ? temp->perm : list;
                         const int32_t dn = temp->split ? temp->n_front : n;
-                        // with a tensor-core part, A's light entries only
-                        DevCsr Al = A;
-                        if (temp->dpart.S) {
-                            Al.col = const_cast<int32_t *>(temp->dpart.lcol);
-                            Al.val = const_cast<uint32_t *>(temp->dpart.lval);
-                        }
                         if (dn > 0)
                             kern<<<std::max(1, std::min(grid, dn)), kDenseThreads, sm, s>>>(
                                 Al, B, T, dl, dn, cnt, nullptr, 0, (int32_t)W, st, temp->stride, bin_of, positive,
@@ -3057,12 +3131,14 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         if (!replay) memcpy(&mdf, (int32_t *)h->h_pinned + 36, sizeof(int64_t));
         const int64_t fpart0 = std::max<int64_t>(kSplitMinFlops, flops_total / ((int64_t)h->sm_count * 4));
         // (uint64 products, whose dense parts are whole-row GEMMs in the
-        // retail and stress chains, take it even with skewed rows)
+        // retail and stress chains, take it even with skewed rows; uint32
+        // products with skewed rows count each row's light products, and the
+        // rows heavy in those are split over CTAs like skewed dense rows)
         // (the panel gathers store one value per (row, index): no repeated
         // column within a row of A or B)
+        const bool skewed = mdf > fpart0;
         bool want = !plan && dtemp.active && positive && dtemp.no_risky && Am->distinct && Bm->distinct &&
-                    flops_total >= (int64_t)h->tune.gemm_min_mflops * 1000000 && h->tune.gemm_inv_density > 0 &&
-                    (sizeof(V) == 8 || mdf <= fpart0);
+                    flops_total >= (int64_t)h->tune.gemm_min_mflops * 1000000 && h->tune.gemm_inv_density > 0;
         for (int b = 0; b < kNumBins && want; b++)
             if (b != kBinDense && counts[b] > 0) want = false;
         if (want) {
@@ -3071,7 +3147,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
             if (sizeof(V) == 4) {
                 uint64_t bmax = 1;
                 if (!Bm->ones) memcpy(&bmax, (int32_t *)h->h_pinned + 58, sizeof(uint64_t));
-                drc = dense_part_build(h, A, B, bmax, dtemp.dpart, e0, e1);
+                drc = dense_part_build(h, A, B, bmax, dtemp.dpart, e0, e1, skewed);
             } else {
                 drc = dense_part_build64(h, A, B, dtemp.dpart, e0, e1);
             }
@@ -3125,12 +3201,18 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     if (replay) max_dense_f = plan->max_dense_flops;
     else memcpy(&max_dense_f, (int32_t *)h->h_pinned + 36, sizeof(int64_t));
     if (record) plan->max_dense_flops = max_dense_f;
-    if (dtemp.active && !dtemp.dpart.S) {
-        // (with a tensor-core part the heaviest work is in the GEMM: no split)
-        const int64_t fpart = std::max<int64_t>(kSplitMinFlops, flops_total / ((int64_t)h->sm_count * 4));
-        if (max_dense_f > fpart) {
+    if (dtemp.active && (!dtemp.dpart.S || dtemp.dpart.lflops)) {
+        // (with a tensor-core part the rows' light products decide, in
+        // smaller parts: the GEMM has taken the bulk of the work; without
+        // their counts there is no split)
+        const bool light = dtemp.dpart.S != nullptr;
+        const int64_t ftot = light ? dtemp.dpart.ltotal : flops_total;
+        const int64_t fmax = light ? dtemp.dpart.lmax : max_dense_f;
+        const int64_t fpart =
+            std::max<int64_t>(light ? kSplitMinLight : kSplitMinFlops, ftot / ((int64_t)h->sm_count * 4));
+        if (fmax > fpart) {
             const int32_t nd = counts[kBinDense];
-            const int32_t max_slots = (int32_t)std::min<int64_t>(std::min<int64_t>(1024, nd), flops_total / fpart + 1);
+            const int32_t max_slots = (int32_t)std::min<int64_t>(std::min<int64_t>(1024, nd), ftot / fpart + 1);
             const int64_t Wt = (B.cols + 31) / 32 * 32;
             auto al = [](int64_t x) { return (x + 255) & ~255LL; };
             const int64_t o_perm = 0;
@@ -3144,7 +3226,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
             if (dev_alloc(h, &mem, total) == RMCM_OK) {
                 char *b = (char *)mem;
                 dtemp.split = true;
-                dtemp.flops = flops;
+                dtemp.flops = light ? dtemp.dpart.lflops : flops;
                 dtemp.fpart = fpart;
                 dtemp.pmax = h->sm_count * 2;
                 dtemp.max_slots = max_slots;
@@ -3172,7 +3254,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         int32_t dense_off = 0;
         for (int b = 0; b < kBinDense; b++) dense_off += counts[b];
         const int32_t nd = counts[kBinDense];
-        k_split_select<<<grid_for(h, nd, 256, 8), 256, 0, s>>>(lists + dense_off, nd, flops, dtemp.fpart, dtemp.pmax,
+        k_split_select<<<grid_for(h, nd, 256, 8), 256, 0, s>>>(lists + dense_off, nd, dtemp.flops, dtemp.fpart, dtemp.pmax,
                                                                dtemp.perm, dtemp.front, dtemp.nslots,
                                                                dtemp.row_of_slot, dtemp.parts, dtemp.max_slots);
         k_split_tasks<<<1, 1024, 0, s>>>(dtemp.parts, dtemp.nslots, dtemp.max_slots, dtemp.task_start);

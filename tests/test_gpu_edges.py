@@ -284,13 +284,19 @@ def test_dense_register_path_detects_overflow(native, engine):
     assert set(C.download()[2].tolist()) == {1 << 34}
 
 
-@pytest.mark.parametrize("n", [60_000, 1 << 20])
+@pytest.mark.parametrize("n", [60_000, 61_441, 65_535, 1 << 20])
 def test_rank_bin_for_wide_rows(native, engine, n):
-    """Rows wider than a dense window (up to 2^20 columns) with > 4096 products."""
+    """Rows wider than a dense window (up to 2^20 columns) with > 4096 products;
+    widths one past and one short of a 4096-column group, with entries on the
+    first and last columns of groups and of the row."""
     rng = np.random.default_rng(31)
     m, k = 40, 400
     A = _random_csr(rng, m, k, rng.integers(100, 300, m), vmax=4)
-    B = _random_csr(rng, k, n, rng.integers(20, 100, k), vmax=4)
+    B = _random_csr(rng, k, n, rng.integers(20, 100, k), vmax=4).tolil()
+    edges = [c for g in range(4096, n, 4096) for c in (g - 1, g)] + [0, n - 1]
+    for i, c in enumerate(edges):
+        B[(7 * i) % k, c] = 1 + i % 4
+    B = B.tocsr()
     for vt in (native.VAL_U32, native.VAL_U64):
         _check_product(native, engine, A, B, vt)
 
@@ -789,6 +795,71 @@ def test_tensor_core_part_uint64(native):
     assert st["gemm_inner"] >= 250 and st["gemm_limbs"] >= 4
     eng.set_tuning(gemm_inv_density=0)
     _check_product(native, eng, A, B, native.VAL_U64)
+    assert eng.product_stats()[-1]["gemm_inner"] == 0
+    eng.close()
+
+
+def _plant_wide_a(A, heavy, value=3000):
+    """Every third row of A gets `value` (> 2047: two FP16 limbs) at one of
+    the heavy inner indices."""
+    A = A.tolil()
+    for r in range(0, A.shape[0], 3):
+        A[r, r % heavy] = value
+    return A.tocsr()
+
+
+def test_tensor_core_part_uint32_limbs_of_a(native):
+    """A uint32 product whose heavy A values do not fit one FP16 limb (some
+    are 3000): the GEMM splits A into limbs too (2 x 1 limb pairs) and the
+    seeds are summed modulo 2^32 like the counters.  Equal to scipy and to
+    the GEMM off, bit for bit."""
+    rng = np.random.default_rng(74)
+    A, B = _heavy_inner(rng, 1200, 2500, 1500, 300)
+    A = _plant_wide_a(A, 300)
+    eng = native.Engine(device=0)
+    eng.set_tuning(gemm_min_mflops=0)
+    eng.set_profiling(1)
+    _check_product(native, eng, A, B, native.VAL_U32)
+    st = eng.product_stats()[-1]
+    assert st["gemm_inner"] >= 250 and st["gemm_limbs"] == 2
+    eng.set_tuning(gemm_inv_density=0)
+    _check_product(native, eng, A, B, native.VAL_U32)
+    assert eng.product_stats()[-1]["gemm_inner"] == 0
+    eng.close()
+
+
+@pytest.mark.parametrize("wide_a", [False, True])
+def test_tensor_core_part_with_skewed_rows(native, wide_a):
+    """A uint32 product with one row far heavier than a fair share: the GEMM
+    takes the heavy inner indices of every row, and the heavy row's light
+    entries (~1.5M products) are split over CTAs whose sums are added to the
+    row's GEMM seeds (one limb of A, or two with ``wide_a``).  Equal to scipy
+    and to the GEMM off, bit for bit."""
+    rng = np.random.default_rng(73)
+    m, heavy, light, n = 600, 300, 20000, 1500
+    dense_a = (rng.random((m, heavy)) < 0.8) * rng.integers(1, 4, (m, heavy))
+    light_a = sp.random(m, light, density=0.03, random_state=rng, format="lil")
+    light_a[7, :] = 1                                   # the skewed row: every light index
+    light_a = light_a.tocsr()
+    light_a.data[:] = rng.integers(1, 4, light_a.nnz)
+    A = sp.hstack([sp.csr_matrix(dense_a), light_a]).tocsr()
+    if wide_a:
+        A = _plant_wide_a(A, heavy)
+    dense_b = (rng.random((heavy, n)) < 0.5) * rng.integers(1, 4, (heavy, n))
+    light_b = sp.random(light, n, density=0.05, random_state=rng, format="csr")
+    light_b.data[:] = rng.integers(1, 4, light_b.nnz)
+    B = sp.vstack([sp.csr_matrix(dense_b), light_b]).tocsr()
+    A.eliminate_zeros()
+    B.eliminate_zeros()
+    eng = native.Engine(device=0)
+    eng.set_tuning(gemm_min_mflops=0)
+    eng.set_profiling(1)
+    _check_product(native, eng, A, B, native.VAL_U32)
+    st = eng.product_stats()[-1]
+    assert st["gemm_inner"] >= 250 and st["bin_rows"][4] == m
+    assert st["gemm_limbs"] == (2 if wide_a else 1)
+    eng.set_tuning(gemm_inv_density=0)
+    _check_product(native, eng, A, B, native.VAL_U32)
     assert eng.product_stats()[-1]["gemm_inner"] == 0
     eng.close()
 
