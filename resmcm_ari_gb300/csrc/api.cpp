@@ -315,8 +315,18 @@ int32_t load_text(rmcm_handle *h, const char *gfile, const char *vfile, const ch
 // leaf matrices (BoolMatrix(HIN, vt, src, sink, et, n), efficient/resmcm.cpp:374-396)
 // ---------------------------------------------------------------------------
 
+// What the device check of an upload found.
+struct CsrFlags {
+    bool bad = false, unsorted = false, dup = false, zero = false;
+};
+
+// Copies a host CSR to the device and checks it there (csr_check: one pass
+// of a warp per row, no host loop over the arrays); the longest row and the
+// estimator's list of long rows (ascending) come from the same pass.  With
+// ck the check's flags are returned for the caller to act on; without it
+// the arrays are trusted (built here, rows sorted).
 int32_t upload_csr(rmcm_handle *h, int64_t rows, int64_t cols, const int64_t *rowptr, const int32_t *col,
-                   const void *val, int32_t valtype, rmcm_mat **out) {
+                   const void *val, int32_t valtype, rmcm_mat **out, CsrFlags *ck) {
     const int64_t nnz = rows > 0 ? rowptr[rows] : 0;
     rmcm_mat *m = nullptr;
     RMCM_TRY(mat_alloc(h, rows, cols, nnz, valtype, &m));
@@ -330,25 +340,52 @@ int32_t upload_csr(rmcm_handle *h, int64_t rows, int64_t cols, const int64_t *ro
         return cuda_error(h, e, "upload");
     }
     {
-        int64_t mx = 0;
-        std::vector<int32_t> lng;
-        for (int64_t r = 0; r < rows; r++) {
-            const int64_t len = rowptr[r + 1] - rowptr[r];
-            mx = std::max<int64_t>(mx, len);
-            if (len > kEstLongRow) lng.push_back((int32_t)r);
+        // flags, then room for every row longer than kEstLongRow
+        const int64_t cap = nnz / (kEstLongRow + 1) + 1;
+        char *tmp = nullptr;
+        int32_t rc = dev_alloc(h, (void **)&tmp, 64 + 4 * cap);
+        if (rc != RMCM_OK) {
+            mat_release(h, m);
+            return rc;
         }
-        m->max_row = mx;
-        m->n_est_long = (int32_t)lng.size();
-        if (!lng.empty()) {
-            int32_t rc = dev_alloc(h, (void **)&m->est_long, 4 * (int64_t)lng.size());
-            if (rc == RMCM_OK) {
-                e = cudaMemcpyAsync(m->est_long, lng.data(), 4 * lng.size(), cudaMemcpyHostToDevice, s);
-                if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        unsigned long long *f = (unsigned long long *)tmp;
+        int32_t *lng = (int32_t *)(tmp + 64);
+        rc = csr_check(h, m->d, val ? m->d.val : nullptr, valtype, f, lng, cap);
+        if (rc == RMCM_OK) {
+            e = cudaMemcpyAsync(h->h_pinned, f, 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) rc = cuda_error(h, e, "upload");
+        }
+        const uint64_t *hf = (const uint64_t *)h->h_pinned;
+        const int64_t nlong = rc == RMCM_OK ? std::min<int64_t>((int64_t)hf[5], cap) : 0;
+        if (rc == RMCM_OK) {
+            if (ck) {
+                ck->bad = hf[0] != 0;
+                ck->unsorted = hf[1] != 0;
+                ck->dup = hf[2] != 0;
+                ck->zero = hf[3] != 0;
             }
-            if (rc != RMCM_OK || e != cudaSuccess) {
-                mat_release(h, m);
-                return rc != RMCM_OK ? rc : cuda_error(h, e, "upload");
+            m->max_row = (int64_t)hf[4];
+        }
+        if (rc == RMCM_OK && nlong > 0 && !(ck && (ck->bad || ck->unsorted))) {
+            // ascending: the estimator adds the long rows' terms in list order
+            std::vector<int32_t> list((size_t)nlong);
+            e = cudaMemcpy(list.data(), lng, 4 * nlong, cudaMemcpyDeviceToHost);
+            if (e == cudaSuccess) {
+                std::sort(list.begin(), list.end());
+                rc = dev_alloc(h, (void **)&m->est_long, 4 * nlong);
+                if (rc == RMCM_OK) {
+                    m->n_est_long = (int32_t)nlong;
+                    e = cudaMemcpyAsync(m->est_long, list.data(), 4 * nlong, cudaMemcpyHostToDevice, s);
+                    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+                }
             }
+            if (rc == RMCM_OK && e != cudaSuccess) rc = cuda_error(h, e, "upload");
+        }
+        dev_free(h, tmp, 64 + 4 * cap);
+        if (rc != RMCM_OK) {
+            mat_release(h, m);
+            return rc;
         }
     }
     if (!val) {
@@ -391,7 +428,7 @@ int32_t build_leaf(rmcm_handle *h, rmcm_graph *g, int32_t src, int32_t sink, int
 #pragma omp parallel for schedule(dynamic, 4096) reduction(| : dup)
     for (int64_t r = 0; r < rows; r++)
         for (int64_t q = rp[r] + 1; q < rp[r + 1]; q++) dup |= col[q] == col[q - 1];
-    int32_t rc = upload_csr(h, rows, cols, rp.data(), col.data(), nullptr, valtype, out);
+    int32_t rc = upload_csr(h, rows, cols, rp.data(), col.data(), nullptr, valtype, out, nullptr);
     if (rc == RMCM_OK) (*out)->distinct = !dup;
     return rc;
 }
@@ -1347,35 +1384,23 @@ RMCM_API int32_t rmcm_mat_upload(rmcm_handle *h, int64_t rows, int64_t cols, con
     *out = nullptr;
     const int64_t nnz = rowptr[rows];
     if (rowptr[0] != 0 || nnz < 0 || (nnz > 0 && !col)) return set_error(h, RMCM_EINVAL, "upload: bad row pointer");
-    // validate (rows ascending, columns in range); sort rows that are not ascending
-    int bad = 0, unsorted = 0, dup = 0;
-#pragma omp parallel for schedule(dynamic, 4096) reduction(| : bad, unsorted, dup)
-    for (int64_t r = 0; r < rows; r++) {
-        const int64_t a = rowptr[r], b = rowptr[r + 1];
-        if (b < a || b > nnz) { bad = 1; continue; }
-        for (int64_t q = a; q < b; q++) {
-            if (col[q] < 0 || col[q] >= cols) bad = 1;
-            if (q > a && col[q] < col[q - 1]) unsorted = 1;
-            if (q > a && col[q] == col[q - 1]) dup = 1;
+    // copy, then validate on the device (rows ascending, columns in range);
+    // rows that are not ascending are sorted here and uploaded again
+    CsrFlags ck;
+    {
+        rmcm_mat *m = nullptr;
+        RMCM_TRY(upload_csr(h, rows, cols, rowptr, col, val, valtype, &m, &ck));
+        if (!ck.bad && !ck.unsorted) {
+            if (val) m->positive = !ck.zero;
+            m->distinct = !ck.dup;
+            *out = m;
+            return RMCM_OK;
         }
+        mat_release(h, m);
     }
-    if (bad) return set_error(h, RMCM_EINVAL, "upload: row pointer not monotone or column out of range");
-    bool positive = true;
-    if (val) {
-        int zero = 0;
-#pragma omp parallel for schedule(static) reduction(| : zero)
-        for (int64_t q = 0; q < nnz; q++)
-            zero |= valtype == RMCM_VAL_U64 ? ((const uint64_t *)val)[q] == 0 : ((const uint32_t *)val)[q] == 0;
-        positive = !zero;
-    }
-    if (!unsorted) {
-        int32_t rc = upload_csr(h, rows, cols, rowptr, col, val, valtype, out);
-        if (rc == RMCM_OK) {
-            if (val) (*out)->positive = positive;
-            (*out)->distinct = !dup;
-        }
-        return rc;
-    }
+    if (ck.bad) return set_error(h, RMCM_EINVAL, "upload: row pointer not monotone or column out of range");
+    const bool positive = !ck.zero;
+    int dup = 0;
     std::vector<int32_t> c2(col, col + nnz);
     std::vector<char> v2;
     const int64_t vb = val_bytes(valtype);
@@ -1391,11 +1416,10 @@ RMCM_API int32_t rmcm_mat_upload(rmcm_handle *h, int64_t rows, int64_t cols, con
             if (val) memcpy(&v2[(a + q) * vb], (const char *)val + idx[q] * vb, vb);
         }
     }
-    dup = 0;
 #pragma omp parallel for schedule(dynamic, 4096) reduction(| : dup)
     for (int64_t r = 0; r < rows; r++)
         for (int64_t q = rowptr[r] + 1; q < rowptr[r + 1]; q++) dup |= c2[q] == c2[q - 1];
-    int32_t rc = upload_csr(h, rows, cols, rowptr, c2.data(), val ? v2.data() : nullptr, valtype, out);
+    int32_t rc = upload_csr(h, rows, cols, rowptr, c2.data(), val ? v2.data() : nullptr, valtype, out, nullptr);
     if (rc == RMCM_OK) {
         if (val) (*out)->positive = positive;
         (*out)->distinct = !dup;

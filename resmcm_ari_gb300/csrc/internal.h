@@ -213,6 +213,12 @@ inline int64_t val_bytes(int32_t valtype) { return valtype == RMCM_VAL_U64 ? 8 :
 int32_t spgemm(rmcm_handle *h, const rmcm_mat *A, const rmcm_mat *B, rmcm_mat **C, int64_t *flops_out,
                ProductPlan *plan = nullptr);
 int32_t fill_ones(rmcm_handle *h, void *val, int64_t nnz, int32_t valtype);
+// One device pass over an uploaded CSR (val may be null): f[0] bad row
+// pointer or column, [1] unsorted row, [2] repeated column, [3] zero value,
+// [4] longest row, [5] rows longer than kEstLongRow, listed (unordered, at
+// most cap) in long_rows.  Queued on h->stream.
+int32_t csr_check(rmcm_handle *h, const DevCsr &M, const void *val, int32_t valtype, unsigned long long *f,
+                  int32_t *long_rows, int64_t cap);
 int32_t convert_values(rmcm_handle *h, const rmcm_mat *src, int32_t valtype, rmcm_mat **out);
 // dense_gemm.cu: tensor-core part of a dense-bin product.  S holds the
 // dense part's exact counts in the product's value type (A.rows x ld): the

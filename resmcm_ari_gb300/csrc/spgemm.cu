@@ -3621,6 +3621,70 @@ int32_t convert_values(rmcm_handle *h, const rmcm_mat *src, int32_t valtype, rmc
     return RMCM_OK;
 }
 
+// Checks of an uploaded CSR in one pass, a warp per row: row pointers
+// non-decreasing and within [0, nnz], columns in [0, cols), each row's
+// columns ascending and distinct, and (with val) whether a value is 0; the
+// longest row and the rows longer than kEstLongRow (in any order, at most
+// cap of them).  f[0] bad, [1] unsorted, [2] duplicate, [3] zero value,
+// [4] longest row, [5] long rows.
+template <typename V>
+__global__ void __launch_bounds__(256) k_check_csr(DevCsr M, int64_t nnz, const V *val, unsigned long long *f,
+                                                   int32_t *long_rows, int64_t cap) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    bool bad = false, unsorted = false, dup = false, zero = false;
+    unsigned long long longest = 0;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < M.rows; r += nwarps) {
+        const int64_t a = M.rowptr[r], b = M.rowptr[r + 1];
+        if (a < 0 || b < a || b > nnz) {
+            bad = true;
+            continue;
+        }
+        for (int64_t q = a + lane; q < b; q += 32) {
+            const int32_t c = M.col[q];
+            if (c < 0 || c >= M.cols) bad = true;
+            if (q > a) {
+                const int32_t p = M.col[q - 1];
+                unsorted |= c < p;
+                dup |= c == p;
+            }
+            if (val) zero |= val[q] == 0;
+        }
+        const unsigned long long len = (unsigned long long)(b - a);
+        longest = len > longest ? len : longest;
+        if (lane == 0 && len > (unsigned long long)kEstLongRow) {
+            const unsigned long long slot = atomicAdd(f + 5, 1ull);
+            if ((int64_t)slot < cap) long_rows[slot] = (int32_t)r;
+        }
+    }
+    bad = __any_sync(kFull, bad);
+    unsorted = __any_sync(kFull, unsorted);
+    dup = __any_sync(kFull, dup);
+    zero = __any_sync(kFull, zero);
+    if (lane == 0) {
+        if (bad) atomicOr(f, 1ull);
+        if (unsorted) atomicOr(f + 1, 1ull);
+        if (dup) atomicOr(f + 2, 1ull);
+        if (zero) atomicOr(f + 3, 1ull);
+        if (longest) atomicMax(f + 4, longest);
+    }
+}
+
+int32_t csr_check(rmcm_handle *h, const DevCsr &M, const void *val, int32_t valtype, unsigned long long *f,
+                  int32_t *long_rows, int64_t cap) {
+    RMCM_CUDA(h, cudaMemsetAsync(f, 0, 6 * sizeof(unsigned long long), h->stream));
+    if (M.rows > 0) {
+        const int grid = grid_for(h, M.rows * 32, 256, 8);
+        if (valtype == RMCM_VAL_U64)
+            k_check_csr<uint64_t><<<grid, 256, 0, h->stream>>>(M, M.nnz, (const uint64_t *)val, f, long_rows, cap);
+        else
+            k_check_csr<uint32_t><<<grid, 256, 0, h->stream>>>(M, M.nnz, (const uint32_t *)val, f, long_rows, cap);
+        h->launches++;
+        RMCM_CUDA(h, cudaGetLastError());
+    }
+    return RMCM_OK;
+}
+
 int32_t fill_ones(rmcm_handle *h, void *val, int64_t nnz, int32_t valtype) {
     if (nnz <= 0) return RMCM_OK;
     const int grid = grid_for(h, nnz, 256, 8);
