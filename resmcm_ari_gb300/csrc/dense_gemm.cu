@@ -186,17 +186,20 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather_a(DevCsr A, const int
 // Limb l of B's heavy rows, transposed for the tensor cores (K contiguous):
 // BdT[l][c][h] = (B[list[h]][c] >> (bits l)) & (2^bits - 1) as FP16, for
 // c < ldn and h < ldk (zero where B has no entry, for h >= nh and c >= cols).
-// A CTA stages the 64 heavy rows h0.. over kBtCols columns in shared memory
-// (33-word pitch: the scatter of a warp's columns hits distinct banks) and
-// writes each output row's 128 bytes coalesced.  stats[2] = largest value.
+// A CTA stages the 64 heavy rows h0.. over kBtCols columns in shared memory,
+// one tile per limb filled in a single pass over the entries (33-word pitch:
+// the scatter of a warp's columns hits distinct banks), and writes each
+// output row's 128 bytes coalesced.  stats[2] = largest value.
 constexpr int kBtCols = 256;
 constexpr int kBtPitch = 66;   // halves per staged row: 64 heavy rows + 2
+constexpr int64_t kBtTileBytes = (int64_t)kBtCols * kBtPitch * 2;
 
 template <typename V>
 __global__ void __launch_bounds__(kGatherThreads) k_gather_bt(DevCsr B, const int32_t *list, int32_t nh, int32_t ldk,
                                                               int32_t ldn, int32_t limbs, int32_t bits, __half *BdT,
                                                               int64_t limb_stride, unsigned long long *stats) {
-    __shared__ __align__(16) __half tile[kBtCols * kBtPitch];
+    extern __shared__ __align__(16) unsigned char smem[];
+    __half *tiles = (__half *)smem;   // limbs x kBtCols x kBtPitch
     __shared__ int64_t s_beg[64], s_end[64];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int32_t h0 = (int32_t)blockIdx.x * 64;
@@ -230,25 +233,27 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather_bt(DevCsr B, const in
     const V *bv = (const V *)B.val;
     const V mask = ((V)1 << bits) - (V)1;
     unsigned long long mx = 0;
-    uint32_t *tw = (uint32_t *)tile;
-    for (int l = 0; l < limbs; l++) {
-        for (int i = threadIdx.x; i < kBtCols * kBtPitch / 2; i += kGatherThreads) tw[i] = 0u;
-        __syncthreads();
-        for (int hr = warp; hr < 64; hr += kGatherThreads / 32) {
-            const int64_t e = s_end[hr];
-            for (int64_t k = s_beg[hr] + lane; k < e; k += 32) {
-                const int32_t c = B.col[k];
-                const V v = bv[k];
-                if (l == 0) mx = (unsigned long long)v > mx ? (unsigned long long)v : mx;
-                tile[(c - c0) * kBtPitch + hr] = __uint2half_rn((uint32_t)((v >> (bits * l)) & mask));
-            }
+    uint32_t *tw = (uint32_t *)tiles;
+    for (int i = threadIdx.x; i < limbs * (kBtCols * kBtPitch / 2); i += kGatherThreads) tw[i] = 0u;
+    __syncthreads();
+    for (int hr = warp; hr < 64; hr += kGatherThreads / 32) {
+        const int64_t e = s_end[hr];
+        for (int64_t k = s_beg[hr] + lane; k < e; k += 32) {
+            const int32_t c = B.col[k];
+            const V v = bv[k];
+            mx = (unsigned long long)v > mx ? (unsigned long long)v : mx;
+            for (int l = 0; l < limbs; l++)
+                tiles[(int64_t)l * (kBtCols * kBtPitch) + (c - c0) * kBtPitch + hr] =
+                    __uint2half_rn((uint32_t)((v >> (bits * l)) & mask));
         }
-        __syncthreads();
+    }
+    __syncthreads();
+    for (int l = 0; l < limbs; l++) {
+        const uint32_t *tl = tw + (int64_t)l * (kBtCols * kBtPitch / 2);
         for (int cr = warp; cr < nc; cr += kGatherThreads / 32) {
             uint32_t *dst = (uint32_t *)(BdT + l * limb_stride + (int64_t)(c0 + cr) * ldk + h0);
-            dst[lane] = tw[cr * (kBtPitch / 2) + lane];
+            dst[lane] = tl[cr * (kBtPitch / 2) + lane];
         }
-        __syncthreads();
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
@@ -259,35 +264,51 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather_bt(DevCsr B, const in
 }
 
 // Per row of A the number of heavy entries and the largest heavy value
-// (stats[3], stats[4]: maxima over rows); TA is A's value type.  A warp per row.
+// (stats[3], stats[4]: maxima over rows); TA is A's value type.  A CTA per
+// row, kGatherPer entries per thread per step (the column -> slot gathers
+// overlap, so a long row does not serialise a warp).
 template <typename TA>
-__global__ void k_heavy_stats(DevCsr A, const int32_t *slot, unsigned long long *stats) {
+__global__ void __launch_bounds__(kGatherThreads) k_heavy_stats(DevCsr A, const int32_t *slot,
+                                                                unsigned long long *stats) {
+    __shared__ unsigned long long s_cnt;
     const int lane = threadIdx.x & 31;
     const TA *av = (const TA *)A.val;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     unsigned long long cmax = 0, vmax = 0;
-    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < A.rows; r += nwarps) {
+    for (int64_t r = blockIdx.x; r < A.rows; r += gridDim.x) {
+        if (threadIdx.x == 0) s_cnt = 0;
+        __syncthreads();
+        const int64_t a0 = A.rowptr[r], a1 = A.rowptr[r + 1];
         unsigned long long c = 0;
-        for (int64_t k = A.rowptr[r] + lane; k < A.rowptr[r + 1]; k += 32) {
-            if (slot[A.col[k]] >= 0) {
-                c++;
-                const unsigned long long v = (unsigned long long)av[k];
-                vmax = v > vmax ? v : vmax;
+        for (int64_t k0 = a0; k0 < a1; k0 += kGatherPer * kGatherThreads) {
+            int32_t col[kGatherPer];
+#pragma unroll
+            for (int u = 0; u < kGatherPer; u++) {
+                const int64_t k = k0 + u * kGatherThreads + threadIdx.x;
+                col[u] = k < a1 ? A.col[k] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < kGatherPer; u++) {
+                if (col[u] >= 0 && slot[col[u]] >= 0) {
+                    c++;
+                    const unsigned long long v = (unsigned long long)av[k0 + u * kGatherThreads + threadIdx.x];
+                    vmax = v > vmax ? v : vmax;
+                }
             }
         }
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) c += __shfl_xor_sync(0xffffffffu, c, d);
-        cmax = c > cmax ? c : cmax;
+        if (lane == 0 && c) atomicAdd(&s_cnt, c);
+        __syncthreads();
+        if (threadIdx.x == 0) cmax = s_cnt > cmax ? s_cnt : cmax;
+        __syncthreads();
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
         const unsigned long long o = __shfl_xor_sync(0xffffffffu, vmax, d);
         vmax = o > vmax ? o : vmax;
     }
-    if (lane == 0) {
-        if (cmax) atomicMax(stats + 3, cmax);
-        if (vmax) atomicMax(stats + 4, vmax);
-    }
+    if (lane == 0 && vmax) atomicMax(stats + 4, vmax);
+    if (threadIdx.x == 0 && cmax) atomicMax(stats + 3, cmax);
 }
 
 // Row panels of A in limbs (TA: A's value type): limb l of each heavy
@@ -395,6 +416,18 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather_al(DevCsr A, const in
     }
 }
 
+// Opts k_gather_bt<V> in to the shared memory of `limbs` tiles; false when
+// the device refuses (the caller keeps the product sparse).
+template <typename V>
+bool gather_bt_smem(int32_t limbs) {
+    const int64_t bytes = limbs * kBtTileBytes;
+    if (bytes <= 48 * 1024) return true;
+    if (cudaFuncSetAttribute(k_gather_bt<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess)
+        return true;
+    cudaGetLastError();
+    return false;
+}
+
 }  // namespace
 
 // Heavy inner indices of C = A B: sampled column counts of A and the density
@@ -435,7 +468,8 @@ int32_t select_heavy(rmcm_handle *h, const DevCsr &A, const DevCsr &B, bool stat
                                                   (int32_t)kMaxHeavy);
     h->launches += 2;
     if (stats64) {
-        k_heavy_stats<uint64_t><<<h->sm_count * 8, 256, 0, s>>>(A, hs.slot, hs.stats);
+        k_heavy_stats<uint64_t><<<(int)std::min<int64_t>(std::max<int64_t>(A.rows, 1), (int64_t)h->sm_count * 8),
+                                  kGatherThreads, 0, s>>>(A, hs.slot, hs.stats);
         h->launches++;
     }
     RMCM_CUDA(h, cudaGetLastError());
@@ -577,7 +611,9 @@ int32_t dense_part_build(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint6
     };
     {
         dim3 grid((unsigned)(ldk / 64), (unsigned)((ldn + kBtCols - 1) / kBtCols));
-        k_gather_bt<uint32_t><<<grid, kGatherThreads, 0, s>>>(B, list, (int32_t)nh, (int32_t)ldk, (int32_t)ldn,
+        if (!gather_bt_smem<uint32_t>(limbs)) return fail3(RMCM_OK);
+        k_gather_bt<uint32_t><<<grid, kGatherThreads, limbs * kBtTileBytes, s>>>(B, list, (int32_t)nh, (int32_t)ldk,
+                                                                                  (int32_t)ldn,
                                                              limbs, bits, BdT, b_limb, stats);
         h->launches++;
         RMCM_CUDA(h, cudaGetLastError());
@@ -732,7 +768,9 @@ int32_t build_limbs(rmcm_handle *h, const DevCsr &A, const DevCsr &B, uint64_t b
                                                           a_limb, pre ? nullptr : lcol, lval, lcnt, stats, B.rowptr,
                                                           pre ? nullptr : lflops);
         dim3 bgrid((unsigned)(ldk / 64), (unsigned)((ldn + kBtCols - 1) / kBtCols));
-        k_gather_bt<V><<<bgrid, kGatherThreads, 0, s>>>(B, list, (int32_t)nh, (int32_t)ldk, (int32_t)ldn, lb, bits,
+        if (!gather_bt_smem<V>(lb)) return fail3(RMCM_OK);
+        k_gather_bt<V><<<bgrid, kGatherThreads, lb * kBtTileBytes, s>>>(B, list, (int32_t)nh, (int32_t)ldk, (int32_t)ldn,
+                                                                        lb, bits,
                                                        BdT, b_limb, stats);
         h->launches += 2;
         RMCM_CUDA(h, cudaGetLastError());
