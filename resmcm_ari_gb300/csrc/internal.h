@@ -67,7 +67,7 @@ struct Tuning {
     int32_t gemm_min_mflops = 512;   // products with fewer multiply-adds (millions) stay sparse
     double hash_load = 0.5;         // hash table load factor bound: slots >= min(f, cols) / load, load <= 0.75
     bool dense_single_pass = true;  // dense rows in one window: one pass into a padded temporary
-    bool short_single_pass = true;  // tiny, micro, hash and warp rows: one pass into a bounded temporary
+    bool short_single_pass = true;  // tiny, micro, hash, warp and unsplit rank rows: one pass into a bounded temporary
     int64_t dense_temp_max_bytes = 8LL << 30;
 };
 
@@ -99,6 +99,7 @@ struct ProductPlan {
     int32_t pack_cbits = 0;          // column bits of the packed copy of B (0: not packed)
     bool short_temp = false;         // short-row bins ran in one pass into a temporary
     int64_t short_total = 0;         // its slots
+    uint32_t short_mask = 0;         // the bins that ran in that pass
 };
 
 }  // namespace rmcm

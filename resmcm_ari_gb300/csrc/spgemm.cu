@@ -2129,9 +2129,14 @@ __global__ void __launch_bounds__(kRankThreads) k_rank(DevCsr A, DevCsr B, DevCs
             if (tid == 0) s_cnt = total;
             __syncthreads();
         }
+        // (with cnt: C is the single-pass temporary, rlen the row's capacity,
+        // and the row's length is reported)
         const int64_t base = C.rowptr[r];
         const int64_t rlen = C.rowptr[r + 1] - base;
-        if (tid == 0 && s_cnt != rlen) raise_status(st, kInvariant);
+        if (tid == 0) {
+            if (cnt) cnt[r] = s_cnt;
+            if (cnt ? s_cnt > rlen : s_cnt != rlen) raise_status(st, kInvariant);
+        }
         // sorted columns straight from the bitmap (four words per lane, from
         // the first one's rank); zero the row's values
         for (int g = tid >> 5; g < ngroups; g += NT / 32) {
@@ -2391,8 +2396,9 @@ __global__ void k_short_cap(int64_t m, const uint8_t *bin_of, const int64_t *flo
     }
 }
 
-// The short-row bins' rows from their slots in the temporary into C (a warp
-// per row; the row's length is C's, from the scan of the reported lengths).
+// The single-pass bins' rows from their slots in the temporary into C (a
+// warp per row, four entries per lane in flight; the row's length is C's,
+// from the scan of the reported lengths).
 template <typename V>
 __global__ void __launch_bounds__(256) k_copy_short(int64_t m, const uint8_t *bin_of, uint32_t mask,
                                                     const int64_t *trow, const int32_t *tcol, const V *tval,
@@ -2403,9 +2409,25 @@ __global__ void __launch_bounds__(256) k_copy_short(int64_t m, const uint8_t *bi
         const int b = bin_of[r] & ~kRiskyBit;
         if (b == kEmptyBin || !((mask >> b) & 1u)) continue;
         const int64_t d0 = C.rowptr[r], len = C.rowptr[r + 1] - d0, s0 = trow[r];
-        for (int64_t i = lane; i < len; i += 32) {
-            C.col[d0 + i] = tcol[s0 + i];
-            ((V *)C.val)[d0 + i] = tval[s0 + i];
+        for (int64_t i0 = lane; i0 < len; i0 += 128) {
+            int32_t c[4];
+            V v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int64_t i = i0 + 32 * u;
+                if (i < len) {
+                    c[u] = tcol[s0 + i];
+                    v[u] = tval[s0 + i];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int64_t i = i0 + 32 * u;
+                if (i < len) {
+                    C.col[d0 + i] = c[u];
+                    ((V *)C.val)[d0 + i] = v[u];
+                }
+            }
         }
     }
 }
@@ -3350,12 +3372,15 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         dtemp.split = false;
     };
 
-    // Single pass for the short-row bins (tiny, micro, hash, warp): each such
-    // row gets min(products, columns) slots in a temporary, their numeric
-    // kernels write there and report each row's length (the symbolic pass is
-    // skipped for them), and after the scan the rows are copied into C.
+    // Single pass for the short-row bins (tiny, micro, hash, warp) and, when
+    // none of its rows is split over CTAs, the rank bin: each such row gets
+    // min(products, columns) slots in a temporary, their numeric kernels
+    // write there and report each row's length (the symbolic pass is skipped
+    // for them), and after the scan the rows are copied into C.
     constexpr uint32_t kShortBins = (1u << kBinTiny) | (1u << kBinHash512) | (1u << kBinHash2k) |
                                     (1u << kBinHash8k) | (1u << kBinMicro) | (1u << kBinWarp);
+    uint32_t short_mask = kShortBins | (rsplit.active ? 0u : (1u << kBinRank));
+    if (replay && plan->short_temp) short_mask = plan->short_mask;
     struct {
         bool active = false;
         int64_t *rowptr = nullptr;
@@ -3375,7 +3400,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     {
         int64_t n_short = 0;
         for (int b = 0; b < kNumBins; b++)
-            if ((kShortBins >> b) & 1u) n_short += counts[b];
+            if ((short_mask >> b) & 1u) n_short += counts[b];
         bool want = replay ? plan->short_temp : (n_short > 0 && h->tune.short_single_pass);
         if (want) {
             // slots: a capacity per row (m of them, then scanned in place of
@@ -3383,7 +3408,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
             stemp.rp_bytes = 16 * (m + 1);
             if (dev_alloc(h, (void **)&stemp.rowptr, stemp.rp_bytes) == RMCM_OK) {
                 int64_t *capr = stemp.rowptr + (m + 1);
-                k_short_cap<<<grid_for(h, m, 256, 8), 256, 0, s>>>(m, bin_of, flops, B.cols, kShortBins, capr);
+                k_short_cap<<<grid_for(h, m, 256, 8), 256, 0, s>>>(m, bin_of, flops, B.cols, short_mask, capr);
                 h->launches++;
                 int32_t src = cudaGetLastError() == cudaSuccess ? RMCM_OK : set_error(h, RMCM_ECUDA, "short capacity");
                 if (src == RMCM_OK)
@@ -3424,9 +3449,10 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         if (record) {
             plan->short_temp = stemp.active;
             plan->short_total = stemp.total;
+            plan->short_mask = short_mask;
         }
     }
-    const uint32_t other_bins = stemp.active ? ~kShortBins : ~0u;
+    const uint32_t other_bins = stemp.active ? ~short_mask : ~0u;
 
     // symbolic
     rmcm_mat *C = nullptr;
@@ -3454,7 +3480,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         T.val = stemp.val;
         T.nnz = stemp.total;
         rc = launch_bins<V, true>(h, A, B, T, lists, counts, dense_max_alen, cnt, cursors, cursor_cap, &dtemp, bin_of,
-                                  positive, Bm->distinct, &rsplit, kShortBins);
+                                  positive, Bm->distinct, &rsplit, short_mask);
     }
     if (rc == RMCM_OK)
         rc = launch_bins<V, false>(h, A, B, C->d, lists, counts, dense_max_alen, cnt, cursors, cursor_cap, &dtemp,
@@ -3509,7 +3535,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     }
     if (rec) cudaEventRecord(h->prof[rec_idx].ev[4], s);
     if (rc == RMCM_OK && !adopt && stemp.active) {
-        k_copy_short<V><<<grid_for(h, m * 32, 256, 16), 256, 0, s>>>(m, bin_of, kShortBins, stemp.rowptr, stemp.col,
+        k_copy_short<V><<<grid_for(h, m * 32, 256, 16), 256, 0, s>>>(m, bin_of, short_mask, stemp.rowptr, stemp.col,
                                                                        (const V *)stemp.val, C->d);
         h->launches++;
         if (cudaGetLastError() != cudaSuccess) rc = set_error(h, RMCM_ECUDA, "short-row copy launch");
