@@ -164,8 +164,11 @@ RMCM_API int32_t rmcm_metapath_format(const int32_t *vts, const int32_t *ets, in
 RMCM_API int32_t rmcm_leaf(rmcm_handle *h, rmcm_graph *g, int32_t src_vt, int32_t sink_vt, int32_t et,
                            int32_t valtype, rmcm_mat **out);
 /* Upload a CSR from host memory (rowptr[rows+1], col[nnz], val[nnz] of
- * valtype or NULL for all ones).  Rows need not be sorted: they are sorted on
- * the device.  Columns are checked against cols. */
+ * valtype or NULL for all ones).  The arrays are checked on the device after
+ * the copy (row pointers non-decreasing and within nnz, columns in
+ * [0, cols): RMCM_EINVAL otherwise).  Rows need not be sorted: a matrix with
+ * an unsorted row is sorted on the host (stable, values follow their
+ * columns) and copied again. */
 RMCM_API int32_t rmcm_mat_upload(rmcm_handle *h, int64_t rows, int64_t cols, const int64_t *rowptr,
                                  const int32_t *col, const void *val, int32_t valtype, rmcm_mat **out);
 RMCM_API int32_t rmcm_mat_info(const rmcm_mat *m, int64_t *rows, int64_t *cols, int64_t *nnz,
