@@ -127,9 +127,16 @@ void mat_release(rmcm_handle *h, rmcm_mat *m) {
     delete m;
 }
 
-int32_t check_status(rmcm_handle *h) {
+// Queues the copy of the device status words to the host (read them with
+// status_eval once the stream has passed it).
+int32_t status_fetch(rmcm_handle *h) {
     RMCM_CUDA(h, cudaMemcpyAsync(h->h_status, h->d_status, sizeof(int) * kNumStatus, cudaMemcpyDeviceToHost, h->stream));
-    RMCM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return RMCM_OK;
+}
+
+// The status words fetched last: RMCM_OK, or the error they report (the
+// words are cleared on the device).
+int32_t status_eval(rmcm_handle *h) {
     int st[kNumStatus];
     memcpy(st, h->h_status, sizeof(st));
     bool any = false;
@@ -140,6 +147,12 @@ int32_t check_status(rmcm_handle *h) {
     if (st[kTimeout]) return set_error(h, RMCM_ETIMEOUT, "a bounded device wait gave up");
     if (st[kArena]) return set_error(h, RMCM_ENOMEM, "device arena exhausted");
     return set_error(h, RMCM_EOVERFLOW, "a path count overflowed the value type");
+}
+
+int32_t check_status(rmcm_handle *h) {
+    RMCM_TRY(status_fetch(h));
+    RMCM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return status_eval(h);
 }
 
 }  // namespace rmcm
@@ -905,10 +918,24 @@ int32_t chain_exec(rmcm_handle *h, rmcm_mat *const *mats, int32_t len, const int
             continue;
         }
         if (rc != RMCM_OK) break;
-        cudaEventSynchronize(ev[4]);
+        // one wait for the product and, when it may overflow, its status
+        const bool want_status = widen && cur == RMCM_VAL_U32;
+        if (want_status) {
+            rc = status_fetch(h);
+            if (rc == RMCM_OK) {
+                const cudaError_t e = cudaStreamSynchronize(s);
+                if (e != cudaSuccess) rc = cuda_error(h, e, "chain");
+            }
+            if (rc != RMCM_OK) {
+                mat_release(h, C);
+                break;
+            }
+        } else {
+            cudaEventSynchronize(ev[4]);
+        }
         spgemm_s += elapsed_s(ev[3], ev[4]);
-        if (widen && cur == RMCM_VAL_U32) {
-            const int32_t st = check_status(h);
+        if (want_status) {
+            const int32_t st = status_eval(h);
             if (st == RMCM_EOVERFLOW) {
                 // escalate: drop C, widen the live intermediates, redo this product
                 mat_release(h, C);

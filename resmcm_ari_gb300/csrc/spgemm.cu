@@ -158,6 +158,8 @@ struct AnalyzeOut {
     unsigned long long *rank_max_flops;
     int32_t *risky_rows;
     unsigned long long *max_total;        // largest row total bound S
+    unsigned long long *short_cap;        // sum of min(flops, cols) over the short-row bins' rows
+    unsigned long long *rank_cap;         // the same over the rank bin's rows
 };
 
 struct AnalyzeShared {
@@ -169,6 +171,7 @@ struct AnalyzeShared {
     unsigned long long max_flops;
     unsigned long long max_rank_flops;
     unsigned long long max_total;
+    unsigned long long short_cap, rank_cap;
 };
 
 __device__ __forceinline__ void analyze_shared_init(AnalyzeShared &sh) {
@@ -181,6 +184,8 @@ __device__ __forceinline__ void analyze_shared_init(AnalyzeShared &sh) {
         sh.max_flops = 0;
         sh.max_rank_flops = 0;
         sh.max_total = 0;
+        sh.short_cap = 0;
+        sh.rank_cap = 0;
     }
 }
 
@@ -194,6 +199,8 @@ __device__ __forceinline__ void analyze_shared_flush(AnalyzeShared &sh, const An
         if (sh.certain) atomicOr(o.certain, 1);
         if (sh.risky) atomicAdd(o.risky_rows, sh.risky);
         if (sh.max_total) atomicMax(o.max_total, sh.max_total);
+        if (sh.short_cap) atomicAdd(o.short_cap, sh.short_cap);
+        if (sh.rank_cap) atomicAdd(o.rank_cap, sh.rank_cap);
     }
 }
 
@@ -217,6 +224,10 @@ __device__ __forceinline__ void analyze_row(int64_t r, int64_t f, unsigned long 
     }
     if (b != kEmptyBin) {
         atomicAdd(&sh.cnt[b], 1);
+        // slots of the single-pass temporary, should the row take it
+        const unsigned long long cap = (unsigned long long)(f < ncols ? f : ncols);
+        if (b == kBinRank) atomicAdd(&sh.rank_cap, cap);
+        else if (b != kBinDense) atomicAdd(&sh.short_cap, cap);
         if (b == kBinDense) {
             atomicMax(&sh.max_alen, (int32_t)(alen < (int64_t)INT_MAX ? alen : (int64_t)INT_MAX));
             atomicMax(&sh.max_flops, (unsigned long long)f);
@@ -2976,7 +2987,9 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     // profiling sums, [52] rank split slots, [53] unsplit rank rows,
     // [54..55] largest rank-row flops (u64), [56] rows that may overflow,
     // [58..59] largest value of B (u64, when B may be packed), [60..61]
-    // largest total bound S of a row that may overflow (uint32)
+    // largest total bound S of a row that may overflow (uint32), [18..19]
+    // and [20..21] slots of the single-pass temporary for the short-row bins'
+    // and the rank bin's rows (u64)
     int32_t *small = (int32_t *)(sc + o_small);
     RMCM_CUDA(h, cudaMemsetAsync(small, 0, 256, s));
     // B may be packed for the dense bin (uint32, positive, one window)
@@ -3016,7 +3029,9 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
                       (unsigned long long *)(small + 36),
                       (unsigned long long *)(small + 54),
                       small + 56,
-                      (unsigned long long *)(small + 60)};
+                      (unsigned long long *)(small + 60),
+                      (unsigned long long *)(small + 18),
+                      (unsigned long long *)(small + 20)};
         // rows longer than kLongAnalyze entries: walked by the whole grid
         const bool long_rows = Am->max_row > kLongAnalyze;
         const int64_t max_long = A.nnz / kLongAnalyze + 1;
@@ -3057,6 +3072,7 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
     int32_t counts[kNumBins];
     int32_t dense_max_alen = 0;
     int64_t flops_total = 0;
+    int64_t cap_short = 0, cap_rank = 0;
     bool certain = false;
     if (replay) {
         memcpy(counts, plan->counts, sizeof(counts));
@@ -3068,6 +3084,8 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
         memcpy(counts, h->h_pinned, sizeof(counts));
         dense_max_alen = ((int32_t *)h->h_pinned)[16];
         memcpy(&flops_total, (int32_t *)h->h_pinned + 32, sizeof(int64_t));
+        memcpy(&cap_short, (int32_t *)h->h_pinned + 18, sizeof(int64_t));
+        memcpy(&cap_rank, (int32_t *)h->h_pinned + 20, sizeof(int64_t));
         certain = ((int32_t *)h->h_pinned)[40] != 0;
         if (sizeof(V) == 4 && h->abort_on_certain_overflow && !certain) {
             // a row whose total exceeds 16 x 2^32 averages more than 2^32/128
@@ -3411,16 +3429,12 @@ int32_t spgemm_t(rmcm_handle *h, const rmcm_mat *Am, const rmcm_mat *Bm, rmcm_ma
                 k_short_cap<<<grid_for(h, m, 256, 8), 256, 0, s>>>(m, bin_of, flops, B.cols, short_mask, capr);
                 h->launches++;
                 int32_t src = cudaGetLastError() == cudaSuccess ? RMCM_OK : set_error(h, RMCM_ECUDA, "short capacity");
+                // the total came with the analysis (no read-back here); the
+                // scan checks it on the device
+                stemp.total = replay ? plan->short_total
+                                     : cap_short + (((short_mask >> kBinRank) & 1u) ? cap_rank : 0);
                 if (src == RMCM_OK)
-                    src = scan_rowptr(h, capr, m, stemp.rowptr, tiles, (unsigned long long *)(small + 44),
-                                      replay ? plan->short_total : -1);
-                if (src == RMCM_OK && !replay) {
-                    cudaError_t e = cudaMemcpyAsync(h->h_pinned, stemp.rowptr + m, 8, cudaMemcpyDeviceToHost, s);
-                    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-                    if (e != cudaSuccess) src = cuda_error(h, e, "short capacity download");
-                    else stemp.total = h->h_pinned[0];
-                }
-                if (replay) stemp.total = plan->short_total;
+                    src = scan_rowptr(h, capr, m, stemp.rowptr, tiles, (unsigned long long *)(small + 44), stemp.total);
                 const int64_t room = h->budget - h->in_use;
                 stemp.c_bytes = 4 * std::max<int64_t>(stemp.total, 1);
                 stemp.v_bytes = (int64_t)sizeof(V) * std::max<int64_t>(stemp.total, 1);
