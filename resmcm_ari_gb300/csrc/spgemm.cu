@@ -1548,6 +1548,8 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                 const int n = (int)(a1 - k0 < (int64_t)kChunk ? a1 - k0 : (int64_t)kChunk);
                 int64_t len[IPT];
                 bool full = false, lng = false;
+                int64_t own_lo = 0, own_hi = 0;   // this thread's entry (plain path)
+                V own_a = 0;
 #pragma unroll
                 for (int i = 0; i < IPT; i++) {
                     const int t = tid * IPT + i;
@@ -1578,6 +1580,11 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                         sg.len[t] = (int32_t)(hi - lo);
                         if (NUMERIC) sg.va[t] = Aval[k];
                         len[i] = (full || lng) ? 0 : hi - lo;   // short segments: flattened stream
+                        if (!full && !lng) {
+                            own_lo = lo;
+                            own_hi = hi;
+                            if (NUMERIC) own_a = Aval[k];
+                        }
                     }
                 }
                 // lists of long and full entries (one entry per thread: kChunk == NT)
@@ -1624,7 +1631,22 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(DevCsr A, DevCsr B, Dev
                             if (ex.pk) stream_long_packed(sg, sg.nlong, ex.pk, ex.cbits, add);
                             else stream_long_plain<V>(sg, sg.nlong, B, add);
                         }
-                        stream_chunk<NT, V, NUMERIC>(sg, n, B, false, ovf, add);
+                        // short segments: each thread adds its own entry's
+                        // products (four loads in flight), no flattening
+                        const int32_t *bc = B.col;
+                        int64_t q = own_lo;
+                        for (; q + 3 < own_hi; q += 4) {
+                            int32_t c[4];
+                            V v[4];
+#pragma unroll
+                            for (int u = 0; u < 4; u++) {
+                                c[u] = __ldg(bc + q + u);
+                                v[u] = __ldg(Bval + q + u);
+                            }
+#pragma unroll
+                            for (int u = 0; u < 4; u++) add(c[u], (V)(own_a * v[u]));
+                        }
+                        for (; q < own_hi; q++) add(__ldg(bc + q), (V)(own_a * __ldg(Bval + q)));
                     }
                 }
                 if (!plain) {
